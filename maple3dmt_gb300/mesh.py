@@ -1,0 +1,198 @@
+"""Octree meshes and synthetic surveys for the forward solve.
+
+`build_octree` calls the native leaf builder (include/m3d_mesh.h), a p4est
+stand-in that follows the refinement rules of the reference's
+OctreeMesh::setup (src/octree/octree_mesh.cpp:25-63).  The survey helpers
+apply the domain and refinement-radius rules of the reference driver
+(examples/real_inversion_octree.cpp:298-379) to the workloads the solver is
+measured on.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi, _loader
+
+MU0 = 4.0e-7 * math.pi
+SIGMA_AIR = 1e-8
+
+
+@dataclass
+class Leaves:
+    """Leaf list of an octree: the mesh input of the solver."""
+    domain: tuple
+    min_level: int
+    max_level: int
+    level: np.ndarray      # int32 [nc]
+    qxyz: np.ndarray       # int32 [nc, 3] lower corners, root length 2**19
+    cx: np.ndarray         # float64 [nc]
+    cy: np.ndarray
+    cz: np.ndarray
+    cell_type: np.ndarray  # int32 [nc] 0 earth, 1 air
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.level.shape[0])
+
+
+def build_octree(domain, min_level, max_level, stations, freqs, *, station_refine_radius,
+                 station_refine_level=None, sigma_bg=0.01, max_interest_depth=0.0,
+                 air_surface_thickness=2000.0, air_mid_thickness=8000.0,
+                 air_upper_thickness=20000.0, transition_padding=0.0, regions=(),
+                 lib=None) -> Leaves:
+    lib = lib or _loader.load()
+    st = np.ascontiguousarray(np.asarray(stations, dtype=np.float64).reshape(-1, 3))
+    fr = np.ascontiguousarray(np.asarray(freqs, dtype=np.float64).reshape(-1))
+    p = _abi.MeshParams()
+    for i in range(6):
+        p.domain[i] = float(domain[i])
+    p.min_level = int(min_level)
+    p.max_level = int(max_level)
+    p.station_refine_radius = float(station_refine_radius)
+    p.station_refine_level = int(max_level if station_refine_level is None else station_refine_level)
+    p.sigma_bg = float(sigma_bg)
+    p.max_interest_depth = float(max_interest_depth)
+    p.air_surface_thickness = float(air_surface_thickness)
+    p.air_mid_thickness = float(air_mid_thickness)
+    p.air_upper_thickness = float(air_upper_thickness)
+    p.transition_padding = float(transition_padding)
+    if st.shape[0]:
+        p.station_bbox[0] = float(st[:, 0].min()); p.station_bbox[1] = float(st[:, 0].max())
+        p.station_bbox[2] = float(st[:, 1].min()); p.station_bbox[3] = float(st[:, 1].max())
+    reg = np.ascontiguousarray(np.asarray(regions, dtype=np.float64).reshape(-1, 8))
+    p.n_regions = int(reg.shape[0])
+    p.regions = reg.ctypes.data_as(_abi.c_double_p) if reg.shape[0] else None
+    h = C.c_void_p()
+    rc = lib.m3d_octree_build(C.byref(p), st.ctypes.data_as(_abi.c_double_p), int(st.shape[0]),
+                              fr.ctypes.data_as(_abi.c_double_p), int(fr.shape[0]), C.byref(h))
+    if rc != 0:
+        raise RuntimeError(f"m3d_octree_build failed with code {rc}")
+    try:
+        nc = lib.m3d_octree_num_cells(h)
+        level = np.zeros(nc, np.int32)
+        q = np.zeros((nc, 3), np.int32)
+        cx = np.zeros(nc); cy = np.zeros(nc); cz = np.zeros(nc)
+        ty = np.zeros(nc, np.int32)
+        ip = lambda a: a.ctypes.data_as(_abi.c_int_p)  # noqa: E731
+        dp = lambda a: a.ctypes.data_as(_abi.c_double_p)  # noqa: E731
+        rc = lib.m3d_octree_get(h, ip(level), ip(q), dp(cx), dp(cy), dp(cz), ip(ty))
+        if rc != 0:
+            raise RuntimeError(f"m3d_octree_get failed with code {rc}")
+        balanced = lib.m3d_octree_is_balanced(h)
+    finally:
+        lib.m3d_octree_destroy(h)
+    if not balanced:
+        raise RuntimeError("octree leaf builder produced an unbalanced tree")
+    return Leaves(tuple(float(d) for d in domain), int(min_level), int(max_level),
+                  level, q, cx, cy, cz, ty)
+
+
+def skin_depth(freq, sigma):
+    return math.sqrt(2.0 / (2.0 * math.pi * freq * MU0 * sigma))
+
+
+@dataclass
+class Survey:
+    """A synthetic MT survey: mesh, conductivity, stations and frequencies."""
+    name: str
+    leaves: Leaves
+    sigma: np.ndarray          # [nc] S/m
+    sigma_bg: float
+    stations: np.ndarray       # [ns, 3]
+    freqs: np.ndarray          # [nf] Hz
+    meta: dict = field(default_factory=dict)
+
+
+def station_grid(n, spacing):
+    c = (np.arange(n) - (n - 1) / 2.0) * spacing
+    xx, yy = np.meshgrid(c, c, indexing="xy")
+    return np.stack([xx.ravel(), yy.ravel(), np.zeros(n * n)], axis=1)
+
+
+def _driver_mesh(stations, freqs, half_width, sigma0, min_level, max_level, radius=None):
+    """Domain and station radius rules of examples/real_inversion_octree.cpp:298-379."""
+    fmin = float(np.min(freqs))
+    dmax = skin_depth(fmin, sigma0)
+    domain = (-half_width, half_width, -half_width, half_width, -3.0 * dmax, dmax)
+    if radius is None:
+        st = np.asarray(stations)
+        d = np.sqrt(((st[:, None, :2] - st[None, :, :2]) ** 2).sum(-1))
+        d = d[d > 100]
+        min_sp = float(d.min()) if d.size else 1000.0
+        finest = 2.0 * half_width / 2.0 ** max_level
+        radius = max(3.0 * finest, min_sp, 2000.0)
+        radius = min(radius, dmax * 0.1)
+    return domain, radius
+
+
+def assign_sigma(leaves: Leaves, earth_fn) -> np.ndarray:
+    """Air cells get 1e-8 S/m (examples/halfspace_1d_test.cpp:89-92); earth cells earth_fn."""
+    s = np.where(leaves.cell_type == 0, earth_fn(leaves.cx, leaves.cy, leaves.cz), SIGMA_AIR)
+    return np.ascontiguousarray(s, dtype=np.float64)
+
+
+def halfspace_survey(*, half_width=50000.0, min_level=3, max_level=5, n_side=5, spacing=2000.0,
+                     freqs=(1.0,), rho=100.0, lib=None) -> Survey:
+    """Uniform 100 ohm-m halfspace under 1e-8 S/m air, 5x5 stations at 2 km, 1 Hz."""
+    st = station_grid(n_side, spacing)
+    fr = np.asarray(freqs, dtype=np.float64)
+    sigma0 = 0.01
+    domain, radius = _driver_mesh(st, fr, half_width, sigma0, min_level, max_level)
+    lv = build_octree(domain, min_level, max_level, st, fr, station_refine_radius=radius,
+                      sigma_bg=sigma0, lib=lib)
+    sig = assign_sigma(lv, lambda x, y, z: np.full_like(z, 1.0 / rho))
+    return Survey("halfspace", lv, sig, sigma0, st, fr,
+                  {"station_refine_radius": radius, "rho": rho})
+
+
+def layered_block_sigma(x, y, z):
+    """10/100/1000 ohm-m layers (interfaces -1 km, -10 km) with a 0.5 ohm-m block
+    x in [-0.5, 0.5] km, y in [-1, 1] km, z in [-2.25, -0.25] km."""
+    s = np.where(z > -1000.0, 0.1, np.where(z > -10000.0, 0.01, 0.001))
+    blk = (np.abs(x) <= 500.0) & (np.abs(y) <= 1000.0) & (z <= -250.0) & (z >= -2250.0)
+    return np.where(blk, 2.0, s)
+
+
+def layered_block_survey(*, half_width=50000.0, min_level=5, max_level=7, n_side=11,
+                         spacing=1000.0, freqs=None, radius=None, noise_std=0.0, seed=0,
+                         lib=None) -> Survey:
+    """Three-layer earth plus conductive block, 11x11 stations at 1 km, 8 frequencies
+    log-spaced 0.01-100 Hz; optional seeded Gaussian noise on log10 sigma of earth cells."""
+    st = station_grid(n_side, spacing)
+    fr = np.logspace(-2, 2, 8) if freqs is None else np.asarray(freqs, dtype=np.float64)
+    sigma0 = 0.01
+    domain, radius = _driver_mesh(st, fr, half_width, sigma0, min_level, max_level, radius)
+    lv = build_octree(domain, min_level, max_level, st, fr, station_refine_radius=radius,
+                      sigma_bg=sigma0, lib=lib)
+    sig = assign_sigma(lv, layered_block_sigma)
+    if noise_std > 0:
+        rng = np.random.default_rng(seed)
+        earth = lv.cell_type == 0
+        sig[earth] = sig[earth] * 10.0 ** rng.normal(0.0, noise_std, int(earth.sum()))
+    return Survey("layered_block", lv, sig, sigma0, st, fr,
+                  {"station_refine_radius": radius})
+
+
+def small_survey(*, min_level=2, max_level=4, n_side=2, spacing=4000.0, freqs=(0.5,),
+                 half_width=20000.0, block=True, lib=None) -> Survey:
+    """A few-thousand-edge mesh with hanging faces, for parity tests."""
+    st = station_grid(n_side, spacing)
+    fr = np.asarray(freqs, dtype=np.float64)
+    sigma0 = 0.01
+    dmax = skin_depth(float(fr.min()), sigma0)
+    domain = (-half_width, half_width, -half_width, half_width, -1.5 * dmax, 0.5 * dmax)
+    lv = build_octree(domain, min_level, max_level, st, fr, station_refine_radius=3000.0,
+                      sigma_bg=sigma0, lib=lib)
+
+    def earth(x, y, z):
+        s = np.where(z > -2000.0, 0.02, 0.005)
+        if block:
+            b = (np.abs(x) < 3000) & (np.abs(y) < 3000) & (z < -500) & (z > -4000)
+            s = np.where(b, 0.5, s)
+        return s
+    sig = assign_sigma(lv, earth)
+    return Survey("small", lv, sig, sigma0, st, fr, {})

@@ -1,0 +1,45 @@
+/* C restatement of the reference's octree-FV forward + adjoint solve.
+ * ORACLE / TEST INFRASTRUCTURE ONLY -- see m3d_oracle.c. Complex arrays are
+ * interleaved (re, im) doubles. */
+#ifndef M3D_ORACLE_H
+#define M3D_ORACLE_H
+
+#include "m3d_case.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct m3d_oracle m3d_oracle;
+
+/* ForwardSolverFV::setup + set_sigma (staggered grid and operators built here) */
+m3d_oracle* m3d_oracle_create(const m3d_case* cs);
+void m3d_oracle_destroy(m3d_oracle* S);
+int m3d_oracle_sizes(const m3d_oracle* S, int* ne, int* nf, int* nc, int* nn);
+int m3d_oracle_set_sigma(m3d_oracle* S, const double* sigma);
+int m3d_oracle_set_tol_override(m3d_oracle* S, double tol);
+/* compute_single_frequency: both polarisations, Z_out [ns][4] complex (xx, xy, yx, yy) */
+int m3d_oracle_solve_frequency(m3d_oracle* S, double freq, double* Z_out);
+int m3d_oracle_factorize(m3d_oracle* S, double freq);
+int m3d_oracle_release(m3d_oracle* S);
+int m3d_oracle_get_E(const m3d_oracle* S, int pol, double* out);
+int m3d_oracle_set_E(m3d_oracle* S, const double* E1, const double* E2);
+int m3d_oracle_adjoint_rhs(m3d_oracle* S, const double* wr, double* rhs1, double* rhs2);
+int m3d_oracle_adjoint_solve(m3d_oracle* S, const double* rhs, double* lam);
+int m3d_oracle_sensitivity(m3d_oracle* S, const double* E, const double* lam, double* g);
+int m3d_oracle_perturbation_rhs(m3d_oracle* S, int pol, const double* dsig, double* out);
+int m3d_oracle_delta_impedance(m3d_oracle* S, const double* dE, int pol, double* dZ);
+int m3d_oracle_last_iters(const m3d_oracle* S, int* out, int cap);
+int m3d_oracle_station_cells(const m3d_oracle* S, int* out);
+int m3d_oracle_matrix_nnz(const m3d_oracle* S);
+int m3d_oracle_get_matrix(const m3d_oracle* S, int* ptr, int* idx, double* val);
+int m3d_oracle_get_edges(const m3d_oracle* S, double* xyz, double* len, int* dir, double* adual,
+                         int* dead, int* node1, int* node2);
+int m3d_oracle_gradient(m3d_oracle* S, const double* freqs, int nf, const double* obs_Z,
+                        const double* obs_err, double* Z_out, double* grad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
