@@ -4,16 +4,22 @@
  * maple3dmt::forward::IForwardSolver (include/maple3dmt/forward/iforward_solver.h:31-115)
  * and its octree implementation ForwardSolverFV
  * (include/maple3dmt/forward/forward_solver_fv.h:77-253).  Every entry point
- * below names the reference member it replaces.
+ * names the reference member it replaces.
  *
  * Conventions
  *  - Plain host pointers and sizes only; all buffers are caller-owned host
  *    memory; complex vectors are interleaved (re, im) doubles.
  *  - Edge vectors use the reference's edge numbering (StaggeredGrid edge ids,
- *    src/octree/staggered_grid.cpp:82-121); cell vectors the leaf order.
- *  - Every function returns M3D_OK (0) or one M3D_ERR_* code and synchronises
- *    the device before returning; m3d_last_error() gives the message.
+ *    src/octree/staggered_grid.cpp:82-121); cell vectors the leaf order;
+ *    impedances are [station][4] in the order Zxx, Zxy, Zyx, Zyy.
+ *  - Every function returns M3D_OK (0) or one M3D_ERR_* code and has
+ *    synchronised the device before it returns; m3d_last_error() gives the
+ *    message of the last failure on that handle.
  *  - A solver handle is single-threaded, like the reference (not re-entrant).
+ *  - Solver state follows the reference's ordering rules: a frequency must be
+ *    solved (m3d_compute_single_frequency) or factorised before the adjoint,
+ *    sensitivity and J.v calls of that frequency
+ *    (src/inversion/inversion_fv.cpp:250-291); M3D_ERR_STATE otherwise.
  */
 #ifndef M3D_GB300_H
 #define M3D_GB300_H
@@ -30,6 +36,156 @@ extern "C" {
 #define M3D_ERR_NO_DEVICE 5   /* no usable CUDA device */
 #define M3D_ERR_TOO_LARGE 6   /* size beyond a fixed limit of the entry point */
 #define M3D_ERR_NUMERIC 7     /* non-finite values met in a solve */
+
+/* Per-right-hand-side solve status (m3d_stats.status). */
+#define M3D_SOLVE_CONVERGED 1
+#define M3D_SOLVE_BREAKDOWN 2
+#define M3D_SOLVE_MAXITER 3
+#define M3D_SOLVE_STAGNATED 4
+#define M3D_SOLVE_DIVERGED 5
+
+/* ---------------------------------------------------------------------- */
+/* Mesh input: the finished octree leaf list.                              */
+/* Replaces the octree::OctreeMesh& argument of ForwardSolverFV::setup     */
+/* (include/maple3dmt/forward/forward_solver_fv.h:82-83), read through     */
+/* OctreeMesh::cell_center / cell_level / cell_type / params               */
+/* (include/maple3dmt/octree/octree_mesh.h:124-177).                        */
+/* ---------------------------------------------------------------------- */
+typedef struct m3d_leaves {
+    double domain[6];      /* x_min x_max y_min y_max z_min z_max (m) */
+    int min_level;
+    int max_level;         /* <= 14 */
+    int n_cells;
+    const int* level;      /* [n_cells] */
+    const double* cx;      /* [n_cells] cell centres (m) */
+    const double* cy;
+    const double* cz;
+    const int* cell_type;  /* [n_cells] 0 earth, 1 air, 2 ocean */
+} m3d_leaves;
+
+/* ---------------------------------------------------------------------- */
+/* Layout introspection (host only, no device needed).                     */
+/* StaggeredGrid::build + DiscreteOperators::build                          */
+/* (src/octree/staggered_grid.cpp:70-409, src/octree/operators.cpp:19-170). */
+/* ---------------------------------------------------------------------- */
+typedef struct m3d_layout m3d_layout;
+
+int m3d_layout_build(const m3d_leaves* leaves, m3d_layout** out);
+void m3d_layout_destroy(m3d_layout* L);
+/* nnz = stiffness pattern size (including the diagonal of every edge). */
+int m3d_layout_sizes(const m3d_layout* L, int* n_edges, int* n_faces, int* n_cells, int* n_nodes,
+                     int* nnz, int* n_hanging);
+/* Any pointer may be NULL. xyz [ne][3]; node1/node2: edge end-point node ids. */
+int m3d_layout_edges(const m3d_layout* L, double* xyz, double* length, int* direction,
+                     double* dual_area, int* dead, int* node1, int* node2);
+/* S = Ce^T Mf^-1 Ce (real): rowptr [ne+1], col [nnz], val [nnz]. */
+int m3d_layout_stiffness(const m3d_layout* L, int* rowptr, int* col, double* val);
+/* hanging pairs [n_hanging][3]: coarse, child1, child2. */
+int m3d_layout_hanging(const m3d_layout* L, int* pairs);
+
+/* ---------------------------------------------------------------------- */
+/* Solver                                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* Mirrors ForwardParamsFV (include/maple3dmt/forward/forward_solver_fv.h:31-69)
+ * plus the GPU's own knobs. m3d_params_default() fills the reference defaults
+ * (bicgstab_maxiter 2000, tol 1e-7, ...). */
+typedef struct m3d_params {
+    double bicgstab_tol;
+    int bicgstab_maxiter;
+    int scattered_field;      /* 1: solve for E_sec, E = E_pri + E_sec */
+    double air_z_threshold;   /* m */
+    int div_correction;
+    int div_corr_iters;
+    double div_corr_tol;
+    int divcorr_outer_max;
+    int divcorr_iter_per_dc;
+    double sigma_bg;          /* background sigma of the 1-D primary field (RefinementParams::sigma_bg) */
+    /* GPU */
+    int precision;            /* 0: complex128 Krylov; 1: complex64 Krylov inside FP64 refinement */
+    int true_residual_check;  /* 1: confirm ||b - A x|| / ||b|| <= tol in FP64 and refine until met */
+    int max_refinements;      /* FP64 refinement steps allowed on top of the Krylov solve */
+    int print_level;
+} m3d_params;
+
+typedef struct m3d_solver m3d_solver;
+
+/* Counters of the last solving call (all right-hand sides of that call). */
+typedef struct m3d_stats {
+    int n_rhs;
+    int iterations[64];        /* Krylov iterations per RHS (first 64) */
+    int status[64];            /* M3D_SOLVE_* per RHS */
+    double true_residual[64];  /* ||b - A x||_2 / ||b||_2 in FP64, before divergence correction */
+    int total_iterations;
+    int refinements;
+    double seconds;
+    long long kernel_launches;
+} m3d_stats;
+
+void m3d_params_default(m3d_params* p);
+
+/* Handle creation binds to CUDA device `device` (no device work yet). */
+int m3d_solver_create(int device, m3d_solver** out);
+void m3d_solver_destroy(m3d_solver* s);
+const char* m3d_last_error(const m3d_solver* s);
+
+/* ForwardSolverFV::setup (forward_solver_fv.cpp:28-47): layout + device upload. */
+int m3d_solver_setup(m3d_solver* s, const m3d_leaves* leaves, const m3d_params* params);
+int m3d_solver_sizes(const m3d_solver* s, int* n_edges, int* n_cells, int* n_nodes, int* n_colours);
+/* ForwardSolverFV::set_sigma (:49-51) / update_sigma (:53-58). */
+int m3d_set_sigma(m3d_solver* s, const double* sigma, int n_cells);
+/* Station positions (x, y, z) [n][3]; mapped to cells as find_stations_ (:1393-1485). */
+int m3d_set_stations(m3d_solver* s, const double* xyz, int n_stations);
+/* set_solver_tolerance_override (forward_solver_fv.h:181); 0 restores. */
+int m3d_set_tolerance_override(m3d_solver* s, double tol);
+/* current_omega (forward_solver_fv.h:104); 0 before any frequency. */
+int m3d_current_omega(const m3d_solver* s, double* omega);
+
+/* compute_single_frequency (:1732-1738): assemble, solve both polarisations,
+ * divergence correction, impedances. Z_out [n_stations][4] complex, may be NULL. */
+int m3d_compute_single_frequency(m3d_solver* s, double freq_hz, double* Z_out);
+/* factorize_frequency (:1743-1750): assemble only. */
+int m3d_factorize_frequency(m3d_solver* s, double freq_hz);
+/* release_factorization (:1755-1757). */
+int m3d_release_factorization(m3d_solver* s);
+/* background_E (forward_solver_fv.h:132-134): pol 0 or 1, E_out [n_edges] complex. */
+int m3d_background_E(m3d_solver* s, int pol, double* E_out);
+/* set_background_fields_complex (:1762-1765). */
+int m3d_set_background_fields(m3d_solver* s, const double* E1, const double* E2);
+
+/* build_adjoint_rhs_from_residual (:1804-2013): wr [n_stations][4] complex. */
+int m3d_build_adjoint_rhs(m3d_solver* s, const double* wr, double* rhs1, double* rhs2);
+/* adjoint_solve_complex (:1770-1773 -> :914-924). */
+int m3d_adjoint_solve(m3d_solver* s, const double* rhs, double* lambda);
+/* solve_rhs_complex (:1796-1799 -> :930-940). */
+int m3d_solve_rhs(m3d_solver* s, const double* rhs, double* x);
+/* compute_sensitivity_complex (:1778-1782 -> :989-1059): g [n_cells]. */
+int m3d_compute_sensitivity(m3d_solver* s, const double* E, const double* lambda, double* g);
+/* build_perturbation_rhs_complex (:1787-1791 -> :945-984): pol 1 or 2. */
+int m3d_build_perturbation_rhs(m3d_solver* s, int pol, const double* delta_sigma, double* rhs);
+/* extract_delta_impedance_complex (:2018-2065): pol 1 or 2, dZ [n_stations][4]. */
+int m3d_extract_delta_impedance(m3d_solver* s, const double* dE, int pol, double* dZ);
+
+/* ---------------------------------------------------------------------- */
+/* Batched entry points: every frequency of an inversion iteration in one   */
+/* multi-right-hand-side solve (the GPU counterpart of the frequency loop   */
+/* in compute_responses :63-79 and InversionFV::compute_gradient_           */
+/* src/inversion/inversion_fv.cpp:230-312).                                 */
+/* ---------------------------------------------------------------------- */
+
+/* All frequencies, both polarisations: Z_out [n_freqs][n_stations][4];
+ * E_out (nullable) [n_freqs][2][n_edges]. Fields stay on the device for
+ * m3d_gradient_batch's adjoint phase. */
+int m3d_forward_batch(m3d_solver* s, const double* freqs, int n_freqs, double* Z_out, double* E_out);
+
+/* Forward + weighted residual + adjoint + sensitivity for all frequencies:
+ * obs_Z [n_stations][n_freqs][4] complex, obs_err [n_stations][n_freqs][4]
+ * (components with err <= 0 carry no weight). grad [n_cells] = sum over
+ * frequencies and polarisations; Z_out nullable [n_freqs][n_stations][4]. */
+int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const double* obs_Z,
+                       const double* obs_err, double* Z_out, double* grad);
+
+int m3d_get_stats(const m3d_solver* s, m3d_stats* out);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,21 @@ class MeshParams(C.Structure):
     ]
 
 
+class Leaves(C.Structure):
+    """struct m3d_leaves (include/m3d_gb300.h)."""
+    _fields_ = [
+        ("domain", C.c_double * 6),
+        ("min_level", C.c_int),
+        ("max_level", C.c_int),
+        ("n_cells", C.c_int),
+        ("level", c_int_p),
+        ("cx", c_double_p),
+        ("cy", c_double_p),
+        ("cz", c_double_p),
+        ("cell_type", c_int_p),
+    ]
+
+
 def _fn(lib, name, res, args):
     f = getattr(lib, name)
     f.restype = res
@@ -44,6 +59,13 @@ def declare(lib) -> None:
         [vp, c_int_p, c_int_p, c_double_p, c_double_p, c_double_p, c_int_p])
     _fn(lib, "m3d_octree_is_balanced", C.c_int, [vp])
     _fn(lib, "m3d_octree_destroy", None, [vp])
+    _fn(lib, "m3d_layout_build", C.c_int, [C.POINTER(Leaves), C.POINTER(vp)])
+    _fn(lib, "m3d_layout_destroy", None, [vp])
+    _fn(lib, "m3d_layout_sizes", C.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p])
+    _fn(lib, "m3d_layout_edges", C.c_int,
+        [vp, c_double_p, c_double_p, c_int_p, c_double_p, c_int_p, c_int_p, c_int_p])
+    _fn(lib, "m3d_layout_stiffness", C.c_int, [vp, c_int_p, c_int_p, c_double_p])
+    _fn(lib, "m3d_layout_hanging", C.c_int, [vp, c_int_p])
     if hasattr(lib, "m3d_solver_create"):
         from . import _abi_solver
         _abi_solver.declare(lib)

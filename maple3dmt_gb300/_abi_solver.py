@@ -1,0 +1,80 @@
+"""ctypes declarations of the solver entry points of include/m3d_gb300.h."""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._abi import Leaves, _fn, c_double_p, c_int_p
+
+
+class Params(C.Structure):
+    """struct m3d_params."""
+    _fields_ = [
+        ("bicgstab_tol", C.c_double),
+        ("bicgstab_maxiter", C.c_int),
+        ("scattered_field", C.c_int),
+        ("air_z_threshold", C.c_double),
+        ("div_correction", C.c_int),
+        ("div_corr_iters", C.c_int),
+        ("div_corr_tol", C.c_double),
+        ("divcorr_outer_max", C.c_int),
+        ("divcorr_iter_per_dc", C.c_int),
+        ("sigma_bg", C.c_double),
+        ("precision", C.c_int),
+        ("true_residual_check", C.c_int),
+        ("max_refinements", C.c_int),
+        ("print_level", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    """struct m3d_stats."""
+    _fields_ = [
+        ("n_rhs", C.c_int),
+        ("iterations", C.c_int * 64),
+        ("status", C.c_int * 64),
+        ("true_residual", C.c_double * 64),
+        ("total_iterations", C.c_int),
+        ("refinements", C.c_int),
+        ("seconds", C.c_double),
+        ("kernel_launches", C.c_longlong),
+    ]
+
+
+SOLVER_SYMBOLS = [
+    "m3d_params_default", "m3d_solver_create", "m3d_solver_destroy", "m3d_last_error",
+    "m3d_solver_setup", "m3d_solver_sizes", "m3d_set_sigma", "m3d_set_stations",
+    "m3d_set_tolerance_override", "m3d_current_omega", "m3d_compute_single_frequency",
+    "m3d_factorize_frequency", "m3d_release_factorization", "m3d_background_E",
+    "m3d_set_background_fields", "m3d_build_adjoint_rhs", "m3d_adjoint_solve", "m3d_solve_rhs",
+    "m3d_compute_sensitivity", "m3d_build_perturbation_rhs", "m3d_extract_delta_impedance",
+    "m3d_forward_batch", "m3d_gradient_batch", "m3d_get_stats",
+]
+
+
+def declare(lib) -> None:
+    vp = C.c_void_p
+    _fn(lib, "m3d_params_default", None, [C.POINTER(Params)])
+    _fn(lib, "m3d_solver_create", C.c_int, [C.c_int, C.POINTER(vp)])
+    _fn(lib, "m3d_solver_destroy", None, [vp])
+    _fn(lib, "m3d_last_error", C.c_char_p, [vp])
+    _fn(lib, "m3d_solver_setup", C.c_int, [vp, C.POINTER(Leaves), C.POINTER(Params)])
+    _fn(lib, "m3d_solver_sizes", C.c_int, [vp, c_int_p, c_int_p, c_int_p, c_int_p])
+    _fn(lib, "m3d_set_sigma", C.c_int, [vp, c_double_p, C.c_int])
+    _fn(lib, "m3d_set_stations", C.c_int, [vp, c_double_p, C.c_int])
+    _fn(lib, "m3d_set_tolerance_override", C.c_int, [vp, C.c_double])
+    _fn(lib, "m3d_current_omega", C.c_int, [vp, c_double_p])
+    _fn(lib, "m3d_compute_single_frequency", C.c_int, [vp, C.c_double, c_double_p])
+    _fn(lib, "m3d_factorize_frequency", C.c_int, [vp, C.c_double])
+    _fn(lib, "m3d_release_factorization", C.c_int, [vp])
+    _fn(lib, "m3d_background_E", C.c_int, [vp, C.c_int, c_double_p])
+    _fn(lib, "m3d_set_background_fields", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_build_adjoint_rhs", C.c_int, [vp, c_double_p, c_double_p, c_double_p])
+    _fn(lib, "m3d_adjoint_solve", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_solve_rhs", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_compute_sensitivity", C.c_int, [vp, c_double_p, c_double_p, c_double_p])
+    _fn(lib, "m3d_build_perturbation_rhs", C.c_int, [vp, C.c_int, c_double_p, c_double_p])
+    _fn(lib, "m3d_extract_delta_impedance", C.c_int, [vp, c_double_p, C.c_int, c_double_p])
+    _fn(lib, "m3d_forward_batch", C.c_int, [vp, c_double_p, C.c_int, c_double_p, c_double_p])
+    _fn(lib, "m3d_gradient_batch", C.c_int,
+        [vp, c_double_p, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p])
+    _fn(lib, "m3d_get_stats", C.c_int, [vp, C.POINTER(Stats)])

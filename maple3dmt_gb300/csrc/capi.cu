@@ -1,0 +1,228 @@
+// extern "C" boundary of include/m3d_gb300.h over GpuSolver.  Every entry
+// point catches exceptions, maps them to an M3D_ERR_* code, records the
+// message on the handle and synchronises before returning.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "m3d_gb300.h"
+#include "solver.hpp"
+
+struct m3d_solver {
+    m3d::GpuSolver* s = nullptr;
+    std::string err;
+};
+
+namespace {
+
+int fail(m3d_solver* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+template <class F>
+int guarded(m3d_solver* h, F&& f) {
+    if (!h || !h->s) return M3D_ERR_ARG;
+    try {
+        f(*h->s);
+        h->err.clear();
+        return M3D_OK;
+    } catch (const std::bad_alloc&) {
+        cudaGetLastError();
+        return fail(h, M3D_ERR_OOM, "allocation failed");
+    } catch (const std::invalid_argument& e) {
+        return fail(h, M3D_ERR_ARG, e.what());
+    } catch (const std::logic_error& e) {
+        return fail(h, M3D_ERR_STATE, e.what());
+    } catch (const std::runtime_error& e) {
+        return fail(h, M3D_ERR_CUDA, e.what());
+    } catch (...) {
+        return fail(h, M3D_ERR_CUDA, "unknown failure");
+    }
+}
+
+bool ready(const m3d_solver* h) { return h && h->s && h->s->ready; }
+
+}  // namespace
+
+namespace m3d {
+bool leaves_valid(const m3d_leaves* lv);
+}
+
+extern "C" void m3d_params_default(m3d_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    // ForwardParamsFV defaults (include/maple3dmt/forward/forward_solver_fv.h:36-64)
+    p->bicgstab_tol = 1e-7;
+    p->bicgstab_maxiter = 2000;
+    p->scattered_field = 1;
+    p->air_z_threshold = 1.0;
+    p->div_correction = 1;
+    p->div_corr_iters = 10;
+    p->div_corr_tol = 2e-3;
+    p->divcorr_outer_max = 20;
+    p->divcorr_iter_per_dc = 500;
+    p->sigma_bg = 0.01;
+    p->precision = 0;
+    p->true_residual_check = 1;
+    p->max_refinements = 3;
+    p->print_level = 0;
+}
+
+extern "C" int m3d_solver_create(int device, m3d_solver** out) {
+    if (!out) return M3D_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return M3D_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n) return M3D_ERR_ARG;
+    auto* h = new (std::nothrow) m3d_solver;
+    if (!h) return M3D_ERR_OOM;
+    h->s = new (std::nothrow) m3d::GpuSolver(device);
+    if (!h->s) { delete h; return M3D_ERR_OOM; }
+    *out = h;
+    return M3D_OK;
+}
+
+extern "C" void m3d_solver_destroy(m3d_solver* h) {
+    if (!h) return;
+    delete h->s;
+    delete h;
+}
+
+extern "C" const char* m3d_last_error(const m3d_solver* h) { return h ? h->err.c_str() : "null handle"; }
+
+extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m3d_params* params) {
+    if (!h || !m3d::leaves_valid(leaves) || !params) return fail(h, M3D_ERR_ARG, "invalid leaves or params");
+    if (params->bicgstab_tol <= 0 || params->bicgstab_maxiter < 1 || params->divcorr_iter_per_dc < 1 ||
+        params->sigma_bg <= 0 || params->precision < 0 || params->precision > 1)
+        return fail(h, M3D_ERR_ARG, "invalid solver parameters");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
+}
+
+extern "C" int m3d_solver_sizes(const m3d_solver* h, int* ne, int* nc, int* nn, int* ncol) {
+    if (!ready(h)) return M3D_ERR_STATE;
+    if (ne) *ne = h->s->n_edges();
+    if (nc) *nc = h->s->n_cells();
+    if (nn) *nn = h->s->n_nodes();
+    if (ncol) *ncol = h->s->n_colours();
+    return M3D_OK;
+}
+
+extern "C" int m3d_set_sigma(m3d_solver* h, const double* sigma, int n) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!sigma || n != h->s->n_cells()) return fail(h, M3D_ERR_ARG, "sigma must have n_cells entries");
+    for (int i = 0; i < n; ++i)
+        if (!(sigma[i] > 0.0) || !std::isfinite(sigma[i])) return fail(h, M3D_ERR_ARG, "sigma must be finite and > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.set_sigma(sigma, n); });
+}
+
+extern "C" int m3d_set_stations(m3d_solver* h, const double* xyz, int n) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (n < 1 || !xyz) return fail(h, M3D_ERR_ARG, "need at least one station");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.set_stations(xyz, n); });
+}
+
+extern "C" int m3d_set_tolerance_override(m3d_solver* h, double tol) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (tol < 0) return fail(h, M3D_ERR_ARG, "tolerance must be >= 0");
+    h->s->tol_override = tol;
+    return M3D_OK;
+}
+
+extern "C" int m3d_current_omega(const m3d_solver* h, double* omega) {
+    if (!h || !h->s || !omega) return M3D_ERR_ARG;
+    *omega = h->s->current_omega;
+    return M3D_OK;
+}
+
+extern "C" int m3d_compute_single_frequency(m3d_solver* h, double freq, double* Z_out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!(freq > 0)) return fail(h, M3D_ERR_ARG, "frequency must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.compute_single_frequency(freq, Z_out); });
+}
+
+extern "C" int m3d_factorize_frequency(m3d_solver* h, double freq) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!(freq > 0)) return fail(h, M3D_ERR_ARG, "frequency must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.factorize(std::vector<double>{freq}); });
+}
+
+extern "C" int m3d_release_factorization(m3d_solver* h) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.release(); });
+}
+
+extern "C" int m3d_background_E(m3d_solver* h, int pol, double* E_out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if ((pol != 0 && pol != 1) || !E_out) return fail(h, M3D_ERR_ARG, "pol must be 0 or 1");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.background_E(pol, E_out); });
+}
+
+extern "C" int m3d_set_background_fields(m3d_solver* h, const double* E1, const double* E2) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!E1 || !E2) return fail(h, M3D_ERR_ARG, "null field");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.set_background(E1, E2); });
+}
+
+extern "C" int m3d_build_adjoint_rhs(m3d_solver* h, const double* wr, double* rhs1, double* rhs2) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!wr || !rhs1 || !rhs2) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.build_adjoint_rhs(wr, rhs1, rhs2); });
+}
+
+extern "C" int m3d_adjoint_solve(m3d_solver* h, const double* rhs, double* lambda) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!rhs || !lambda) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.adjoint_solve(rhs, lambda, false); });
+}
+
+extern "C" int m3d_solve_rhs(m3d_solver* h, const double* rhs, double* x) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!rhs || !x) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.adjoint_solve(rhs, x, true); });
+}
+
+extern "C" int m3d_compute_sensitivity(m3d_solver* h, const double* E, const double* lambda, double* g) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!E || !lambda || !g) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.sensitivity(E, lambda, g); });
+}
+
+extern "C" int m3d_build_perturbation_rhs(m3d_solver* h, int pol, const double* dsig, double* rhs) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if ((pol != 1 && pol != 2) || !dsig || !rhs) return fail(h, M3D_ERR_ARG, "pol must be 1 or 2");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.perturbation_rhs(pol, dsig, rhs); });
+}
+
+extern "C" int m3d_extract_delta_impedance(m3d_solver* h, const double* dE, int pol, double* dZ) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if ((pol != 1 && pol != 2) || !dE || !dZ) return fail(h, M3D_ERR_ARG, "pol must be 1 or 2");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.delta_impedance(dE, pol, dZ); });
+}
+
+extern "C" int m3d_forward_batch(m3d_solver* h, const double* freqs, int nf, double* Z_out, double* E_out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!freqs || nf < 1) return fail(h, M3D_ERR_ARG, "need frequencies");
+    for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.forward_batch(freqs, nf, Z_out, E_out); });
+}
+
+extern "C" int m3d_gradient_batch(m3d_solver* h, const double* freqs, int nf, const double* obs_Z,
+                                  const double* obs_err, double* Z_out, double* grad) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!freqs || nf < 1 || !obs_Z || !obs_err || !grad) return fail(h, M3D_ERR_ARG, "null buffer");
+    for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.gradient_batch(freqs, nf, obs_Z, obs_err, Z_out, grad); });
+}
+
+extern "C" int m3d_get_stats(const m3d_solver* h, m3d_stats* out) {
+    if (!h || !h->s || !out) return M3D_ERR_ARG;
+    *out = h->s->stats;
+    return M3D_OK;
+}

@@ -1,0 +1,129 @@
+// Device helpers shared by the solver kernels: complex arithmetic on
+// double2 / float2, warp and block reductions, and a deterministic grid
+// reduction (per-block partials summed in block order by the last block).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace m3d {
+namespace dev {
+
+constexpr int kWarp = 32;
+constexpr int kBlock = 256;               // threads per block for every kernel here
+constexpr int kWarpsPerBlock = kBlock / kWarp;
+constexpr int kSlice = 32;                // sliced-ELL slice height (rows per warp)
+constexpr int kMaxRhs = 16;               // right-hand sides per batched launch
+constexpr int kMaxQ = 3;                  // reduced quantities per kernel
+
+template <class R> struct CTraits;
+template <> struct CTraits<double> { using C = double2; };
+template <> struct CTraits<float> { using C = float2; };
+template <class R> using cplx = typename CTraits<R>::C;
+
+template <class R> __host__ __device__ __forceinline__ cplx<R> cm(R a, R b) {
+    cplx<R> z; z.x = a; z.y = b; return z;
+}
+template <class C> __host__ __device__ __forceinline__ C cadd(C a, C b) { a.x += b.x; a.y += b.y; return a; }
+template <class C> __host__ __device__ __forceinline__ C csub(C a, C b) { a.x -= b.x; a.y -= b.y; return a; }
+template <class C> __host__ __device__ __forceinline__ C cneg(C a) { a.x = -a.x; a.y = -a.y; return a; }
+template <class C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
+    C z; z.x = a.x * b.x - a.y * b.y; z.y = a.x * b.y + a.y * b.x; return z;
+}
+// conj(a) * b
+template <class C> __host__ __device__ __forceinline__ C cjmul(C a, C b) {
+    C z; z.x = a.x * b.x + a.y * b.y; z.y = a.x * b.y - a.y * b.x; return z;
+}
+template <class C, class R> __host__ __device__ __forceinline__ C cscale(C a, R s) { a.x *= s; a.y *= s; return a; }
+template <class C> __host__ __device__ __forceinline__ double cabs2(C a) { return (double)a.x * a.x + (double)a.y * a.y; }
+__host__ __device__ __forceinline__ double cabsd(double2 a) { return hypot(a.x, a.y); }
+// Smith's algorithm for a / b (R. L. Smith, CACM 5(8), 1962).
+__host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+    double2 z;
+    if (fabs(b.x) >= fabs(b.y)) {
+        const double r = b.y / b.x, d = b.x + b.y * r;
+        z.x = (a.x + a.y * r) / d; z.y = (a.y - a.x * r) / d;
+    } else {
+        const double r = b.x / b.y, d = b.x * r + b.y;
+        z.x = (a.x * r + a.y) / d; z.y = (a.y * r - a.x) / d;
+    }
+    return z;
+}
+__host__ __device__ __forceinline__ double2 to_d(double2 a) { return a; }
+__host__ __device__ __forceinline__ double2 to_d(float2 a) { return make_double2(a.x, a.y); }
+template <class C> __host__ __device__ __forceinline__ C from_d(double2 a);
+template <> __host__ __device__ __forceinline__ double2 from_d<double2>(double2 a) { return a; }
+template <> __host__ __device__ __forceinline__ float2 from_d<float2>(double2 a) {
+    return make_float2((float)a.x, (float)a.y);
+}
+
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double2 shfl_xor(double2 v, int m) {
+    v.x = __shfl_xor_sync(0xffffffffu, v.x, m);
+    v.y = __shfl_xor_sync(0xffffffffu, v.y, m);
+    return v;
+}
+
+// Scratch for grid reductions: partial[block][kMaxQ * kMaxRhs] and a counter
+// that the last block resets.
+struct RedScratch {
+    double2* partial;
+    double2* final_;      // [kMaxQ * kMaxRhs], result of the last reduction
+    unsigned int* counter;
+    int max_blocks;
+};
+
+// Sums, over the grid, NQ complex quantities for each of K right-hand sides.
+// `acc[kt][q]` is this thread's contribution for right-hand side rhs0 + kt.
+// Lanes are combined through shared memory in lane order, warps in warp
+// order and blocks in block order by the last block to arrive, so the result
+// is deterministic for a fixed launch shape.  Returns true in the last block;
+// then `out[q * K + k]` (shared memory, NQ*K entries) holds the totals.
+template <int NQ, int K, int KT>
+__device__ bool grid_reduce(const double2 (&acc)[KT][NQ], int rhs0, RedScratch rs, double2* out) {
+    __shared__ double2 sm[kWarpsPerBlock][NQ][K];
+    __shared__ bool am_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < kWarpsPerBlock * NQ * K; i += blockDim.x)
+        (&sm[0][0][0])[i] = make_double2(0.0, 0.0);
+    __syncthreads();
+    for (int l = 0; l < 32; ++l) {
+        if (lane == l) {
+#pragma unroll
+            for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+                for (int q = 0; q < NQ; ++q)
+                    sm[warp][q][rhs0 + kt] = cadd(sm[warp][q][rhs0 + kt], acc[kt][q]);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (threadIdx.x < NQ * K) {
+        const int q = threadIdx.x / K, k = threadIdx.x % K;
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < kWarpsPerBlock; ++w) s = cadd(s, sm[w][q][k]);
+        __stcg(&rs.partial[(size_t)blockIdx.x * (NQ * K) + threadIdx.x], s);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(rs.counter, 1u);
+        am_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!am_last) return false;
+    __threadfence();
+    if (threadIdx.x < NQ * K) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int b = 0; b < (int)gridDim.x; ++b)
+            s = cadd(s, __ldcg(&rs.partial[(size_t)b * (NQ * K) + threadIdx.x]));
+        out[threadIdx.x] = s;
+        rs.final_[threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) *rs.counter = 0u;
+    __syncthreads();
+    return true;
+}
+
+}  // namespace dev
+}  // namespace m3d

@@ -1,0 +1,505 @@
+// Batched SSOR-BiCGStab kernels.  See krylov.cuh for what they restate.
+#include "krylov.cuh"
+
+#include <stdexcept>
+
+namespace m3d {
+
+using namespace dev;
+
+namespace {
+
+// Right-hand sides handled by one thread in the SpMV / SSOR kernels: the
+// gathers of x[col][rhs0 .. rhs0+KT) are 32 contiguous bytes or more.
+template <class R, int K> struct KtOf { static constexpr int v = (K < 2 ? K : 2); };
+template <int K> struct KtOf<float, K> { static constexpr int v = (K < 4 ? K : 4); };
+
+// ---------------------------------------------------------------------------
+// Scalar recurrences of BiCGStabSolver::solve (src/forward/bicgstab.cpp),
+// run by thread k < K of the last block of each reduction.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double cabs_(double2 z) { return hypot(z.x, z.y); }
+
+// r = b - A x0; r0 = r: |b|^2, |r|^2, (r0, r)   (bicgstab.cpp:24-41, :51)
+__device__ void ep_init(BicgState& S, const double2* out, int k, int K) {
+    if (S.status == kInactive) return;
+    double bn = sqrt(out[0 * K + k].x);
+    if (bn < 1e-30) bn = 1.0;
+    S.bnorm = bn;
+    S.rnorm = sqrt(out[1 * K + k].x);
+    S.iter = 0;
+    S.pend_x = 0;
+    S.breakdown = 0;
+    S.res = S.rnorm / bn;
+    if (S.res < S.tol) { S.status = kConverged; return; }
+    S.status = kRunning;
+    S.rho = out[2 * K + k];
+    S.rho_old = make_double2(1.0, 0.0);
+    S.alpha = make_double2(1.0, 0.0);
+    S.omega = make_double2(1.0, 0.0);
+    if (cabs_(S.rho) < 1e-30) { S.status = kBreakdown; S.breakdown = 1; S.iter = 1; }
+}
+
+// (r0, v) -> alpha   (bicgstab.cpp:79-87)
+__device__ void ep_r0v(BicgState& S, const double2* out, int k, int K) {
+    if (S.status != kRunning) return;
+    const double2 r0v = out[k];
+    if (cabs_(r0v) < 1e-30) {
+        S.status = kBreakdown; S.breakdown = 2; S.iter += 1; S.res = S.rnorm / S.bnorm;
+        return;
+    }
+    S.alpha = cdiv(S.rho, r0v);
+}
+
+// |s| -> early exit   (bicgstab.cpp:89-103)
+__device__ void ep_s(BicgState& S, const double2* out, int k, int K) {
+    if (S.status != kRunning) return;
+    S.snorm = sqrt(out[k].x);
+    if (S.snorm / S.bnorm < S.tol) {
+        S.status = kConverged; S.pend_x = 1; S.iter += 1; S.res = S.snorm / S.bnorm;
+    }
+}
+
+// (t, t), (t, s) -> omega   (bicgstab.cpp:116-125)
+__device__ void ep_omega(BicgState& S, const double2* out, int k, int K) {
+    if (S.status != kRunning) return;
+    const double2 tt = out[0 * K + k], ts = out[1 * K + k];
+    if (cabs_(tt) < 1e-30) {
+        S.status = kBreakdown; S.breakdown = 3; S.pend_x = 1; S.iter += 1; S.res = S.snorm / S.bnorm;
+        return;
+    }
+    S.omega = cdiv(ts, tt);
+}
+
+// |r|, (r0, r) -> stop tests, next rho and beta   (bicgstab.cpp:127-160, :51-62)
+__device__ void ep_xr(BicgState& S, const double2* out, int k, int K) {
+    if (S.pend_x) { S.pend_x = 0; return; }
+    if (S.status != kRunning) return;
+    S.iter += 1;
+    S.rnorm = sqrt(out[0 * K + k].x);
+    const double rel = S.rnorm / S.bnorm;
+    S.res = rel;
+    if (rel < S.tol) { S.status = kConverged; return; }
+    if (cabs_(S.omega) < 1e-30) { S.status = kBreakdown; S.breakdown = 4; return; }
+    S.rho_old = S.rho;
+    S.rho = out[1 * K + k];
+    if (S.iter >= S.maxiter) { S.status = kMaxIter; return; }
+    if (cabs_(S.rho) < 1e-30) { S.status = kBreakdown; S.breakdown = 1; return; }
+    S.beta = cmul(cdiv(S.rho, S.rho_old), cdiv(S.alpha, S.omega));
+}
+
+// |b - A x| / |b|
+__device__ void ep_trueres(BicgState& S, const double2* out, int k, int K) {
+    if (S.status == kInactive) return;
+    double bn = sqrt(out[1 * K + k].x);
+    if (bn < 1e-30) bn = 1.0;
+    S.true_res = sqrt(out[0 * K + k].x) / bn;
+}
+
+// ---------------------------------------------------------------------------
+// Sliced-ELL SpMV with fused reductions.  Warp task = (slice, subgroup g);
+// lane = row within the slice; the thread handles right-hand sides
+// g*KT .. g*KT+KT-1.  The warp stride of the grid is a multiple of G, so a
+// warp keeps the same subgroup across its tasks.
+// ---------------------------------------------------------------------------
+template <class R, int K, int MODE>
+__global__ void __launch_bounds__(kBlock) k_spmv(EllView<R> A, DiagView<R> D, BatchView B,
+                                                 const cplx<R>* __restrict__ x, cplx<R>* __restrict__ y,
+                                                 const cplx<R>* __restrict__ aux,
+                                                 cplx<R>* __restrict__ aux_out, BicgState* st,
+                                                 RedScratch rs) {
+    using C = cplx<R>;
+    constexpr int KT = KtOf<R, K>::v;
+    constexpr int G = K / KT;
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kSpmvAs || MODE == kSpmvTrueRes) ? 2 : 3;
+    constexpr bool REDUCE = MODE != kSpmvPlain;
+    const int lane = threadIdx.x & 31;
+    const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long W = ((long)gridDim.x * blockDim.x) >> 5;
+    const int g = (int)(wg % G);
+    const int rhs0 = g * KT;
+    double2 acc[KT][NQ];
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[kt][q] = make_double2(0.0, 0.0);
+
+    const long tasks = (long)A.n_slices * G;
+    for (long t = wg; t < tasks; t += W) {
+        const int s = (int)(t / G);
+        const int row = s * kSlice + lane;
+        const int off = A.slice_off[s];
+        const int w = A.slice_wl[s] + A.slice_wu[s];
+        C sum[KT];
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
+        for (int k = 0; k < w; ++k) {
+            const int c = __ldg(&A.col[off + k * kSlice + lane]);
+            const R v = __ldg(&A.val[off + k * kSlice + lane]);
+            const C* xp = x + (size_t)c * K + rhs0;
+#pragma unroll
+            for (int kt = 0; kt < KT; ++kt) {
+                const C xv = xp[kt];
+                sum[kt].x += v * xv.x;
+                sum[kt].y += v * xv.y;
+            }
+        }
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) {
+            const int rhs = rhs0 + kt;
+            const size_t i = (size_t)row * K + rhs;
+            const C d = D.d[(size_t)B.fmap[rhs] * D.n_pad + row];
+            const C yv = cadd(sum[kt], cmul(d, x[i]));
+            if (MODE == kSpmvPlain) {
+                y[i] = yv;
+            } else if (MODE == kSpmvAp) {
+                y[i] = yv;
+                acc[kt][0] = cadd(acc[kt][0], cjmul(to_d(aux[i]), to_d(yv)));
+            } else if (MODE == kSpmvAs) {
+                y[i] = yv;
+                const double2 tv = to_d(yv);
+                acc[kt][0].x += tv.x * tv.x + tv.y * tv.y;
+                acc[kt][1] = cadd(acc[kt][1], cjmul(tv, to_d(aux[i])));
+            } else if (MODE == kSpmvInit) {
+                const C bv = aux[i];
+                const C rv = csub(bv, yv);
+                y[i] = rv;
+                aux_out[i] = rv;
+                const double2 bd = to_d(bv), rd = to_d(rv);
+                acc[kt][0].x += bd.x * bd.x + bd.y * bd.y;
+                acc[kt][1].x += rd.x * rd.x + rd.y * rd.y;
+                acc[kt][2] = cadd(acc[kt][2], cjmul(rd, rd));
+            } else {  // kSpmvTrueRes
+                const C bv = aux[i];
+                const C rv = csub(bv, yv);
+                y[i] = rv;
+                const double2 bd = to_d(bv), rd = to_d(rv);
+                acc[kt][0].x += rd.x * rd.x + rd.y * rd.y;
+                acc[kt][1].x += bd.x * bd.x + bd.y * bd.y;
+            }
+        }
+    }
+    if (!REDUCE) return;
+    __shared__ double2 out[NQ * K];
+    if (grid_reduce<NQ, K, KT>(acc, rhs0, rs, out)) {
+        if (threadIdx.x < K) {
+            BicgState S = st[threadIdx.x];
+            if (MODE == kSpmvAp) ep_r0v(S, out, threadIdx.x, K);
+            else if (MODE == kSpmvAs) ep_omega(S, out, threadIdx.x, K);
+            else if (MODE == kSpmvInit) ep_init(S, out, threadIdx.x, K);
+            else ep_trueres(S, out, threadIdx.x, K);
+            st[threadIdx.x] = S;
+        }
+    }
+}
+
+// SSOR forward sweep over the slices of one colour:
+//   y_i = (in_i - sum_{j in earlier colours} a_ij y_j) / d_i      (ssor.h:58-66)
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_ssor_fwd(EllView<R> A, DiagView<R> D, BatchView B,
+                                                     int s_begin, int s_end,
+                                                     const cplx<R>* __restrict__ in, cplx<R>* y) {
+    using C = cplx<R>;
+    constexpr int KT = KtOf<R, K>::v;
+    constexpr int G = K / KT;
+    const int lane = threadIdx.x & 31;
+    const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long W = ((long)gridDim.x * blockDim.x) >> 5;
+    const long tasks = (long)(s_end - s_begin) * G;
+    for (long t = wg; t < tasks; t += W) {
+        const int s = s_begin + (int)(t / G);
+        const int rhs0 = (int)(t % G) * KT;
+        const int row = s * kSlice + lane;
+        const int off = A.slice_off[s];
+        const int wl = A.slice_wl[s];
+        C sum[KT];
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
+        for (int k = 0; k < wl; ++k) {
+            const int c = __ldg(&A.col[off + k * kSlice + lane]);
+            const R v = __ldg(&A.val[off + k * kSlice + lane]);
+            const C* yp = y + (size_t)c * K + rhs0;
+#pragma unroll
+            for (int kt = 0; kt < KT; ++kt) {
+                const C yv = yp[kt];
+                sum[kt].x += v * yv.x;
+                sum[kt].y += v * yv.y;
+            }
+        }
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) {
+            const int rhs = rhs0 + kt;
+            const size_t i = (size_t)row * K + rhs;
+            const C di = D.dinv[(size_t)B.fmap[rhs] * D.n_pad + row];
+            y[i] = cmul(csub(in[i], sum[kt]), di);
+        }
+    }
+}
+
+// SSOR backward sweep over the slices of one colour:
+//   out_i = y_i - (sum_{j in later colours} a_ij out_j) / d_i      (ssor.h:69-78)
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_ssor_bwd(EllView<R> A, DiagView<R> D, BatchView B,
+                                                     int s_begin, int s_end,
+                                                     const cplx<R>* __restrict__ y, cplx<R>* out) {
+    using C = cplx<R>;
+    constexpr int KT = KtOf<R, K>::v;
+    constexpr int G = K / KT;
+    const int lane = threadIdx.x & 31;
+    const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long W = ((long)gridDim.x * blockDim.x) >> 5;
+    const long tasks = (long)(s_end - s_begin) * G;
+    for (long t = wg; t < tasks; t += W) {
+        const int s = s_begin + (int)(t / G);
+        const int rhs0 = (int)(t % G) * KT;
+        const int row = s * kSlice + lane;
+        const int off = A.slice_off[s];
+        const int wl = A.slice_wl[s], wu = A.slice_wu[s];
+        C sum[KT];
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
+        for (int k = wl; k < wl + wu; ++k) {
+            const int c = __ldg(&A.col[off + k * kSlice + lane]);
+            const R v = __ldg(&A.val[off + k * kSlice + lane]);
+            const C* op = out + (size_t)c * K + rhs0;
+#pragma unroll
+            for (int kt = 0; kt < KT; ++kt) {
+                const C ov = op[kt];
+                sum[kt].x += v * ov.x;
+                sum[kt].y += v * ov.y;
+            }
+        }
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) {
+            const int rhs = rhs0 + kt;
+            const size_t i = (size_t)row * K + rhs;
+            const C di = D.dinv[(size_t)B.fmap[rhs] * D.n_pad + row];
+            out[i] = csub(y[i], cmul(sum[kt], di));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Vector updates (thread per element (row, rhs); rhs = element % K is fixed
+// per thread because the grid stride is a multiple of K).
+// ---------------------------------------------------------------------------
+
+// p = r (first iteration) or r + beta (p - omega v)   (bicgstab.cpp:60-67)
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_update_p(long n, const cplx<R>* __restrict__ r,
+                                                     cplx<R>* __restrict__ p, const cplx<R>* __restrict__ v,
+                                                     const BicgState* __restrict__ st) {
+    using C = cplx<R>;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    if (i0 >= n) return;
+    const BicgState S = st[i0 % K];
+    const bool run = S.status == kRunning;
+    const bool first = S.iter == 0;
+    const C beta = from_d<C>(S.beta), om = from_d<C>(S.omega);
+    for (long i = i0; i < n; i += stride) {
+        if (!run) { p[i] = cm<R>(0, 0); continue; }
+        if (first) { p[i] = r[i]; continue; }
+        p[i] = cadd(r[i], cmul(beta, csub(p[i], cmul(om, v[i]))));
+    }
+}
+
+// s = r - alpha v, |s|^2   (bicgstab.cpp:89-94)
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_update_s(long n, const cplx<R>* __restrict__ r,
+                                                     const cplx<R>* __restrict__ v, cplx<R>* __restrict__ s,
+                                                     BicgState* st, RedScratch rs) {
+    using C = cplx<R>;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int rhs = (int)(i0 % K);
+    const BicgState S = st[rhs];
+    const bool run = S.status == kRunning;
+    const C al = from_d<C>(S.alpha);
+    double2 acc[1][1] = {{make_double2(0.0, 0.0)}};
+    for (long i = i0; i < n; i += stride) {
+        if (!run) { s[i] = cm<R>(0, 0); continue; }
+        const C sv = csub(r[i], cmul(al, v[i]));
+        s[i] = sv;
+        const double2 d = to_d(sv);
+        acc[0][0].x += d.x * d.x + d.y * d.y;
+    }
+    __shared__ double2 out[K];
+    if (grid_reduce<1, K, 1>(acc, rhs, rs, out)) {
+        if (threadIdx.x < K) {
+            BicgState T = st[threadIdx.x];
+            ep_s(T, out, threadIdx.x, K);
+            st[threadIdx.x] = T;
+        }
+    }
+}
+
+// x += alpha p_hat + omega s_hat; r = s - omega t; |r|^2, (r0, r)
+// (bicgstab.cpp:127-133); right-hand sides that stopped at the s test or at
+// a (t, t) breakdown take x += alpha p_hat only (:96, :123).
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restrict__ x, cplx<R>* __restrict__ r,
+                                                      const cplx<R>* __restrict__ r0,
+                                                      const cplx<R>* __restrict__ ph,
+                                                      const cplx<R>* __restrict__ sh,
+                                                      const cplx<R>* __restrict__ s,
+                                                      const cplx<R>* __restrict__ t, BicgState* st,
+                                                      RedScratch rs) {
+    using C = cplx<R>;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int rhs = (int)(i0 % K);
+    const BicgState S = st[rhs];
+    const bool run = S.status == kRunning;
+    const bool pend = S.pend_x != 0;
+    const C al = from_d<C>(S.alpha), om = from_d<C>(S.omega);
+    double2 acc[1][2] = {{make_double2(0.0, 0.0), make_double2(0.0, 0.0)}};
+    for (long i = i0; i < n; i += stride) {
+        if (pend) { x[i] = cadd(x[i], cmul(al, ph[i])); continue; }
+        if (!run) continue;
+        x[i] = cadd(x[i], cadd(cmul(al, ph[i]), cmul(om, sh[i])));
+        const C rv = csub(s[i], cmul(om, t[i]));
+        r[i] = rv;
+        const double2 d = to_d(rv);
+        acc[0][0].x += d.x * d.x + d.y * d.y;
+        acc[0][1] = cadd(acc[0][1], cjmul(to_d(r0[i]), d));
+    }
+    __shared__ double2 out[2 * K];
+    if (grid_reduce<2, K, 1>(acc, rhs, rs, out)) {
+        if (threadIdx.x < K) {
+            BicgState T = st[threadIdx.x];
+            ep_xr(T, out, threadIdx.x, K);
+            st[threadIdx.x] = T;
+        }
+    }
+}
+
+inline void check_launch(long long* counter) {
+    if (counter) ++*counter;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+}
+
+inline int blocks_for(long work, int per_block, int cap) {
+    long b = (work + per_block - 1) / per_block;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+template <class R, int K>
+void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
+            cplx<R>* aux_out, BicgState* st) {
+    constexpr int G = K / KtOf<R, K>::v;
+    const long warps = (long)c.A.n_slices * G;
+    int grid;
+    if (mode == kSpmvPlain) {
+        grid = blocks_for(warps, kWarpsPerBlock, 1 << 20);
+    } else {
+        grid = c.grid_spmv;  // multiple of 2, so the warp stride is a multiple of G
+    }
+    switch (mode) {
+        case kSpmvPlain:
+            k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            break;
+        case kSpmvAp:
+            k_spmv<R, K, kSpmvAp><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            break;
+        case kSpmvAs:
+            k_spmv<R, K, kSpmvAs><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            break;
+        case kSpmvInit:
+            k_spmv<R, K, kSpmvInit><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            break;
+        default:
+            k_spmv<R, K, kSpmvTrueRes><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            break;
+    }
+    check_launch(c.launches);
+}
+
+template <class R, int K>
+void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
+    constexpr int G = K / KtOf<R, K>::v;
+    const int nc = (int)c.colour_slices.size() - 1;
+    for (int col = 0; col < nc; ++col) {
+        const int s0 = c.colour_slices[col], s1 = c.colour_slices[col + 1];
+        if (s1 <= s0) continue;
+        const int grid = blocks_for((long)(s1 - s0) * G, kWarpsPerBlock, 1 << 20);
+        k_ssor_fwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, s0, s1, in, y);
+        check_launch(c.launches);
+    }
+    for (int col = nc - 1; col >= 0; --col) {
+        const int s0 = c.colour_slices[col], s1 = c.colour_slices[col + 1];
+        if (s1 <= s0) continue;
+        const int grid = blocks_for((long)(s1 - s0) * G, kWarpsPerBlock, 1 << 20);
+        k_ssor_bwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, s0, s1, y, out);
+        check_launch(c.launches);
+    }
+}
+
+template <class R, int K>
+void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+    const long n = (long)c.n_pad * K;
+    const int gv = c.grid_vec;
+    k_update_p<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.p, v.v, st);
+    check_launch(c.launches);
+    ssor_k<R, K>(c, v.p, v.y, v.ph);
+    spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
+    k_update_s<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
+    check_launch(c.launches);
+    ssor_k<R, K>(c, v.s, v.y, v.sh);
+    spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
+    k_update_xr<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
+    check_launch(c.launches);
+}
+
+}  // namespace
+
+#define M3D_DISPATCH_K(K_, CALL)                                    \
+    switch (K_) {                                                   \
+        case 2: CALL(2); break;                                     \
+        case 4: CALL(4); break;                                     \
+        case 8: CALL(8); break;                                     \
+        case 16: CALL(16); break;                                   \
+        default: throw std::runtime_error("batch size must be 2, 4, 8 or 16"); \
+    }
+
+template <class R>
+void spmv(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
+          cplx<R>* aux_out, BicgState* st) {
+#define CALL(K) spmv_k<R, K>(c, mode, x, y, aux, aux_out, st)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
+template <class R>
+void ssor_apply(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
+#define CALL(K) ssor_k<R, K>(c, in, y, out)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
+template <class R>
+void bicg_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+    spmv(c, kSpmvInit, v.x, v.r, v.b, v.r0, st);
+}
+
+template <class R>
+void bicg_iteration(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+#define CALL(K) iteration_k<R, K>(c, v, st)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
+template void spmv<double>(const KrylovCtx<double>&, int, const double2*, double2*, const double2*, double2*, BicgState*);
+template void spmv<float>(const KrylovCtx<float>&, int, const float2*, float2*, const float2*, float2*, BicgState*);
+template void ssor_apply<double>(const KrylovCtx<double>&, const double2*, double2*, double2*);
+template void ssor_apply<float>(const KrylovCtx<float>&, const float2*, float2*, float2*);
+template void bicg_init<double>(const KrylovCtx<double>&, const KrylovVecs<double>&, BicgState*);
+template void bicg_init<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
+template void bicg_iteration<double>(const KrylovCtx<double>&, const KrylovVecs<double>&, BicgState*);
+template void bicg_iteration<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
+
+}  // namespace m3d

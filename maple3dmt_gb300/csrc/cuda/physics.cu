@@ -1,0 +1,876 @@
+// Non-Krylov kernels of the solve path.  See physics.cuh for the reference
+// code each launcher restates.
+#include "physics.cuh"
+
+#include <stdexcept>
+#include <vector>
+
+namespace m3d {
+namespace phys {
+
+using namespace dev;
+
+namespace {
+
+constexpr double kMu0 = 4.0e-7 * 3.14159265358979323846;
+
+inline void ck() {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+}
+
+inline int grid1(long n, int cap = 65536) {
+    long b = (n + kBlock - 1) / kBlock;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+__device__ __forceinline__ double2 zero2() { return make_double2(0.0, 0.0); }
+
+// principal square root (Kahan's formulation of the half-angle formula)
+__device__ double2 csqrt_d(double2 z) {
+    const double r = hypot(z.x, z.y);
+    if (r == 0.0) return zero2();
+    const double t = sqrt((r + fabs(z.x)) * 0.5);
+    if (z.x >= 0.0) return make_double2(t, z.y / (2.0 * t));
+    return make_double2(fabs(z.y) / (2.0 * t), copysign(t, z.y));
+}
+
+// exp(a + ib) = e^a (cos b, sin b)
+__device__ double2 cexp_d(double2 z) {
+    double s, c;
+    sincos(z.y, &s, &c);
+    const double e = exp(z.x);
+    return make_double2(e * c, e * s);
+}
+
+// ---------------------------------------------------------------------------
+// assembly
+// ---------------------------------------------------------------------------
+
+__global__ void k_edge_mass(MeshDev m, const double* __restrict__ sigma, double* __restrict__ Me,
+                            double* __restrict__ me_dc) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= m.n_pad) return;
+    const unsigned char fl = m.flags[row];
+    if (fl & kFlagPad) { Me[row] = 0.0; me_dc[row] = 0.0; return; }
+    const int a0 = m.adj_ptr[row], a1 = m.adj_ptr[row + 1];
+    double sum = 0.0;
+    int count = 0;
+    for (int k = a0; k < a1; ++k) { sum += sigma[m.adj_cell[k]]; ++count; }
+    const double sa = count > 0 ? sum / count : 1e-8;
+    const bool dead = (fl & kFlagDead) != 0;
+    Me[row] = (dead || a1 == a0) ? 0.0 : sa * m.me_geom[row];      // operators.cpp:494-517
+    me_dc[row] = dead ? 0.0 : sa * m.adual[row] * m.elen[row];      // operators.cpp:958-972
+}
+
+__global__ void k_assemble_diag(MeshDev m, const double* __restrict__ Me, const double* __restrict__ omegas,
+                                int nf, double2* d, double2* dinv, float2* d32, float2* dinv32) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)m.n_pad * nf) return;
+    const int f = (int)(i / m.n_pad), row = (int)(i % m.n_pad);
+    double2 dv, di;
+    if (m.flags[row] & (kFlagConstrained | kFlagPad)) {
+        dv = make_double2(1.0, 0.0);
+        di = dv;
+    } else {
+        dv = make_double2(m.s_diag[row], omegas[f] * Me[row]);
+        di = (hypot(dv.x, dv.y) > 1e-30) ? cdiv(make_double2(1.0, 0.0), dv) : make_double2(1.0, 0.0);
+    }
+    d[i] = dv;
+    dinv[i] = di;
+    if (d32) { d32[i] = make_float2((float)dv.x, (float)dv.y); dinv32[i] = make_float2((float)di.x, (float)di.y); }
+}
+
+// ---------------------------------------------------------------------------
+// right-hand sides and post-processing
+// ---------------------------------------------------------------------------
+
+__global__ void k_primary(MeshDev m, VecK out, RhsInfo info, int bc_only) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = out.K;
+    if (i >= (long)m.n_pad * K) return;
+    const int row = (int)(i / K), k = (int)(i % K);
+    const unsigned char fl = m.flags[row];
+    double2 v = zero2();
+    const int pol = info.pol[k];
+    if (!(fl & kFlagPad) && pol >= 0 && m.dir[row] == pol && (!bc_only || (fl & kFlagBc))) {
+        const double z = m.ez[row];
+        const double2 ik = info.ik[k];
+        if (z >= 0.0) v = make_double2(1.0 + ik.x * z, ik.y * z);
+        else v = cexp_d(make_double2(ik.x * z, ik.y * z));
+    }
+    out.p[i] = v;
+}
+
+__global__ void k_lift(MeshDev m, VecK ebc, VecK rhs) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = rhs.K;
+    if (i >= (long)m.n_pad * K) return;
+    const int row = (int)(i / K), k = (int)(i % K);
+    const unsigned char fl = m.flags[row];
+    double2 v = zero2();
+    if (fl & kFlagPad) {
+    } else if (fl & kFlagBc) {
+        v = ebc.p[i];
+    } else if (!(fl & kFlagConstrained)) {
+        for (int q = m.lift_ptr[row]; q < m.lift_ptr[row + 1]; ++q) {
+            const double a = m.lift_val[q];
+            const double2 e = ebc.p[(size_t)m.lift_col[q] * K + k];
+            v.x -= a * e.x;
+            v.y -= a * e.y;
+        }
+    }
+    rhs.p[i] = v;
+}
+
+__global__ void k_vsub(long n, const double2* __restrict__ a, const double2* __restrict__ b, double2* out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = csub(a[i], b[i]);
+}
+
+__global__ void k_hanging(MeshDev m, VecK x) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = x.K;
+    if (i >= (long)m.nhp * K) return;
+    const int h = (int)(i / K), k = (int)(i % K);
+    const int c = m.hp[3 * h], c1 = m.hp[3 * h + 1], c2 = m.hp[3 * h + 2];
+    const double2 a = x.p[(size_t)c1 * K + k], b = x.p[(size_t)c2 * K + k];
+    x.p[(size_t)c * K + k] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+}
+
+// list order matters when a child is itself a coarse edge: one thread per rhs
+__global__ void k_hanging_seq(MeshDev m, VecK x) {
+    const int k = threadIdx.x;
+    if (k >= x.K) return;
+    const int K = x.K;
+    for (int h = 0; h < m.nhp; ++h) {
+        const int c = m.hp[3 * h], c1 = m.hp[3 * h + 1], c2 = m.hp[3 * h + 2];
+        const double2 a = x.p[(size_t)c1 * K + k], b = x.p[(size_t)c2 * K + k];
+        x.p[(size_t)c * K + k] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+    }
+}
+
+__global__ void k_combine(MeshDev m, VecK epri, VecK esec, VecK ebc, VecK e) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = e.K;
+    if (i >= (long)m.n_pad * K) return;
+    const int row = (int)(i / K);
+    const unsigned char fl = m.flags[row];
+    e.p[i] = (fl & kFlagBc) ? ebc.p[i] : cadd(epri.p[i], esec.p[i]);
+}
+
+__global__ void k_to_perm(MeshDev m, const double2* __restrict__ ref, VecK dst, int k) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m.ne) dst.p[(size_t)m.iperm[e] * dst.K + k] = ref[e];
+}
+
+__global__ void k_from_perm(MeshDev m, VecK src, int k, double2* __restrict__ ref) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < m.ne) ref[e] = src.p[(size_t)m.iperm[e] * src.K + k];
+}
+
+// ---------------------------------------------------------------------------
+// divergence correction
+// ---------------------------------------------------------------------------
+
+__global__ void k_dc_lap(MeshDev m, const double* __restrict__ me, DcWork w) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= m.nn) return;
+    const int a = m.inc_ptr[v], b = m.inc_ptr[v + 1];
+    if (m.node_bc[v]) {
+        w.lap_diag[v] = 1.0;
+        w.jac_diag[v] = 1.0;
+        for (int q = a; q < b; ++q) w.lap_off[q] = 0.0;
+        return;
+    }
+    double diag = 0.0;
+    bool any = false;
+    for (int q = a; q < b; ++q) {
+        const int e = m.inc_edge[q];
+        const double we = me[e];
+        double off = 0.0;
+        if (we >= 1e-30) {
+            const double gv = m.inc_gv[q], gw = m.inc_gw[q];
+            diag += gv * we * gv;
+            any = true;
+            if (!m.node_bc[m.inc_other[q]]) off = gv * we * gw;
+        }
+        w.lap_off[q] = off;
+    }
+    w.lap_diag[v] = diag;
+    w.jac_diag[v] = any ? diag : 1.0;
+}
+
+// phi0_v = sum_e G[e,v] rhs_e / (i omega)
+__global__ void k_dc_phi0(MeshDev m, VecK rhs, RhsInfo info, DcWork w) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = rhs.K;
+    if (i >= (long)m.nn * K) return;
+    const int v = (int)(i / K), k = (int)(i % K);
+    double2 acc = zero2();
+    for (int q = m.inc_ptr[v]; q < m.inc_ptr[v + 1]; ++q) {
+        const int e = m.inc_edge[q];
+        if (m.flags[e] & kFlagDead) continue;
+        const double2 r = rhs.p[(size_t)e * K + k];
+        acc.x += m.inc_gv[q] * r.x;
+        acc.y += m.inc_gv[q] * r.y;
+    }
+    w.phi0[i] = cdiv(acc, make_double2(0.0, info.omega[k]));
+}
+
+// divJ = G^T (me E) - phi0, zero on BC nodes; |divJ| -> outer-loop test
+__global__ void k_dc_divj(MeshDev m, const double* __restrict__ me, VecK E, int use_phi0, DcWork w,
+                          double tol, RedScratch rs) {
+    const int K = E.K;
+    const long n = (long)m.nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int k = (int)(i0 % K);
+    const bool act = w.st[k].active && !w.st[k].done;
+    double2 acc[1][1] = {{zero2()}};
+    for (long i = i0; i < n && act; i += stride) {
+        const int v = (int)(i / K);
+        double2 d = zero2();
+        if (!m.node_bc[v]) {
+            for (int q = m.inc_ptr[v]; q < m.inc_ptr[v + 1]; ++q) {
+                const int e = m.inc_edge[q];
+                const double we = me[e];
+                if (m.flags[e] & kFlagDead) continue;
+                const double2 ev = E.p[(size_t)e * K + k];
+                const double2 wev = make_double2(we * ev.x, we * ev.y);
+                d.x += m.inc_gv[q] * wev.x;
+                d.y += m.inc_gv[q] * wev.y;
+            }
+            if (use_phi0) d = csub(d, w.phi0[i]);
+        }
+        w.divJ[i] = d;
+        acc[0][0].x += hypot(d.x, d.y) * hypot(d.x, d.y);
+    }
+    __shared__ double2 out[kMaxRhs];
+    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+        if (threadIdx.x < K) {
+            DcState S = w.st[threadIdx.x];
+            if (S.active && !S.done) {
+                const double dn = sqrt(out[threadIdx.x].x);
+                S.dn = dn;
+                if (S.outer == 0) S.div0 = dn;
+                const double rel = (S.div0 > 1e-30) ? dn / S.div0 : 0.0;
+                if ((rel < tol && S.outer > 0) || dn < 1e-12) {
+                    S.done = 1;
+                    S.cg_run = 0;
+                } else {
+                    S.cg_run = 1;
+                    S.cg_iter = 0;
+                }
+            }
+            w.st[threadIdx.x] = S;
+        }
+    }
+}
+
+__device__ __forceinline__ double2 jac_apply(double2 r, double d) {
+    return (fabs(d) > 1e-30) ? make_double2(r.x / d, r.y / d) : r;
+}
+
+// phi = 0, r = divJ, z = r / diag, p = z, rz = (r, z)
+__global__ void k_dc_cg_init(int nn, int K, DcWork w, RedScratch rs) {
+    const long n = (long)nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int k = (int)(i0 % K);
+    const bool run = w.st[k].cg_run;
+    double2 acc[1][1] = {{zero2()}};
+    for (long i = i0; i < n && run; i += stride) {
+        const int v = (int)(i / K);
+        const double2 r = w.divJ[i];
+        const double2 z = jac_apply(r, w.jac_diag[v]);
+        w.phi[i] = zero2();
+        w.r[i] = r;
+        w.z[i] = z;
+        w.p[i] = z;
+        acc[0][0] = cadd(acc[0][0], cjmul(r, z));
+    }
+    __shared__ double2 out[kMaxRhs];
+    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+        if (threadIdx.x < K && w.st[threadIdx.x].cg_run) w.st[threadIdx.x].rz = out[threadIdx.x];
+    }
+}
+
+// Ap = L p, (p, Ap) -> alpha   (forward_solver_fv.cpp:681-692)
+__global__ void k_dc_cg_ap(MeshDev m, int K, DcWork w, RedScratch rs) {
+    const long n = (long)m.nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int k = (int)(i0 % K);
+    const bool run = w.st[k].cg_run;
+    double2 acc[1][1] = {{zero2()}};
+    for (long i = i0; i < n && run; i += stride) {
+        const int v = (int)(i / K);
+        const double2 pv = w.p[i];
+        double2 s = make_double2(w.lap_diag[v] * pv.x, w.lap_diag[v] * pv.y);
+        for (int q = m.inc_ptr[v]; q < m.inc_ptr[v + 1]; ++q) {
+            const double a = w.lap_off[q];
+            const double2 pw = w.p[(size_t)m.inc_other[q] * K + k];
+            s.x += a * pw.x;
+            s.y += a * pw.y;
+        }
+        w.Ap[i] = s;
+        acc[0][0] = cadd(acc[0][0], cjmul(pv, s));
+    }
+    __shared__ double2 out[kMaxRhs];
+    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+        if (threadIdx.x < K) {
+            DcState S = w.st[threadIdx.x];
+            if (S.cg_run) {
+                const double2 pAp = out[threadIdx.x];
+                if (hypot(pAp.x, pAp.y) < 1e-30) S.cg_run = 0;
+                else S.alpha = cdiv(S.rz, pAp);
+            }
+            w.st[threadIdx.x] = S;
+        }
+    }
+}
+
+// phi += alpha p, r -= alpha Ap, |r| test, z = r / diag, beta   (:693-710)
+__global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch rs) {
+    const long n = (long)nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int k = (int)(i0 % K);
+    const DcState S0 = w.st[k];
+    const bool run = S0.cg_run;
+    const double2 al = S0.alpha;
+    double2 acc[1][2] = {{zero2(), zero2()}};
+    for (long i = i0; i < n && run; i += stride) {
+        const int v = (int)(i / K);
+        w.phi[i] = cadd(w.phi[i], cmul(al, w.p[i]));
+        const double2 r = csub(w.r[i], cmul(al, w.Ap[i]));
+        w.r[i] = r;
+        const double2 z = jac_apply(r, w.jac_diag[v]);
+        w.z[i] = z;
+        const double ar = hypot(r.x, r.y);
+        acc[0][0].x += ar * ar;
+        acc[0][1] = cadd(acc[0][1], cjmul(r, z));
+    }
+    __shared__ double2 out[2 * kMaxRhs];
+    if (grid_reduce<2, kMaxRhs, 1>(acc, k, rs, out)) {
+        if (threadIdx.x < K) {
+            DcState S = w.st[threadIdx.x];
+            if (S.cg_run) {
+                S.rn = out[threadIdx.x].x;
+                S.cg_iter += 1;
+                if (sqrt(S.rn) < 1e-10 * S.dn) {
+                    S.cg_run = 0;
+                } else {
+                    const double2 rzn = out[kMaxRhs + threadIdx.x];
+                    S.beta = cdiv(rzn, make_double2(S.rz.x + 1e-30, S.rz.y));
+                    S.rz = rzn;
+                    if (S.cg_iter >= cg_max) S.cg_run = 0;
+                }
+            }
+            w.st[threadIdx.x] = S;
+        }
+    }
+}
+
+// p = z + beta p
+__global__ void k_dc_cg_p(int nn, int K, DcWork w) {
+    const long n = (long)nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    if (i0 >= n) return;
+    const int k = (int)(i0 % K);
+    if (!w.st[k].cg_run) return;
+    const double2 be = w.st[k].beta;
+    for (long i = i0; i < n; i += stride) w.p[i] = cadd(w.z[i], cmul(be, w.p[i]));
+}
+
+// E -= G phi on edges that are not BC (:714-720), for rhs still in the outer loop
+__global__ void k_dc_grad(MeshDev m, VecK E, DcWork w) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int K = E.K;
+    if (i >= (long)m.n_pad * K) return;
+    const int row = (int)(i / K), k = (int)(i % K);
+    const DcState& S = w.st[k];
+    if (!S.active || S.done) return;
+    const unsigned char fl = m.flags[row];
+    if (fl & (kFlagPad | kFlagDcBc)) return;
+    const int n0 = m.e_node[2 * row], n1 = m.e_node[2 * row + 1];
+    const double g0 = m.e_g[2 * row], g1 = m.e_g[2 * row + 1];
+    const double2 a = w.phi[(size_t)n0 * K + k], b = w.phi[(size_t)n1 * K + k];
+    const double2 gr = make_double2(g0 * a.x + g1 * b.x, g0 * a.y + g1 * b.y);
+    E.p[i] = csub(E.p[i], gr);
+}
+
+__global__ void k_dc_outer_done(int K, DcWork w) {
+    const int k = threadIdx.x;
+    if (k < K) {
+        DcState S = w.st[k];
+        if (S.active && !S.done) S.outer += 1;
+        w.st[k] = S;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// stations
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ double2 cdivn(double2 a, int n) { return cdiv(a, make_double2((double)n, 0.0)); }
+__device__ __forceinline__ double2 chalf(double2 a, double2 b) {
+    return cmul(cadd(a, b), make_double2(0.5, 0.0));
+}
+
+__global__ void k_station_z(StationDev st, VecK E, const double* __restrict__ omegas, int nf,
+                            HCache* hc, double2* Z) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf * st.ns) return;
+    const int f = i / st.ns, s = i % st.ns;
+    const int K = E.K;
+    HCache H;
+    H.Hx1 = H.Hy1 = H.Hx2 = H.Hy2 = H.det = H.Zxx = H.Zxy = H.Zyx = H.Zyy = zero2();
+    H.cdx = H.cdy = H.cdz = 0.0; H.pad_ = 0.0;
+    double2* zo = Z + (size_t)i * 4;
+    const int cell = st.cell[s];
+    if (cell < 0) {
+        hc[i] = H;
+        zo[0] = zo[1] = zo[2] = zo[3] = zero2();
+        return;
+    }
+    const double omega = omegas[f];
+    const double2 iwmu = make_double2(0.0, omega * kMu0);
+    const double cdx = st.geom[6 * s + 3], cdy = st.geom[6 * s + 4], cdz = st.geom[6 * s + 5];
+    double2 Ex1t = zero2(), Ex1b = zero2(), Ex2t = zero2(), Ex2b = zero2();
+    double2 Ey1t = zero2(), Ey1b = zero2(), Ey2t = zero2(), Ey2b = zero2();
+    double2 Ez1px = zero2(), Ez1mx = zero2(), Ez2px = zero2(), Ez2mx = zero2();
+    double2 Ez1py = zero2(), Ez1my = zero2(), Ez2py = zero2(), Ez2my = zero2();
+    int nxt = 0, nxb = 0, nyt = 0, nyb = 0, npx = 0, nmx = 0, npy = 0, nmy = 0;
+    for (int q = st.e_ptr[s]; q < st.e_ptr[s + 1]; ++q) {
+        const int row = st.e_row[q];
+        const unsigned char code = st.e_code[q];
+        const int d = code & 3;
+        const double2 e1 = E.p[(size_t)row * K + 2 * f], e2 = E.p[(size_t)row * K + 2 * f + 1];
+        if (d == 0) {
+            if (code & 4) { Ex1t = cadd(Ex1t, e1); Ex2t = cadd(Ex2t, e2); ++nxt; }
+            else { Ex1b = cadd(Ex1b, e1); Ex2b = cadd(Ex2b, e2); ++nxb; }
+        } else if (d == 1) {
+            if (code & 4) { Ey1t = cadd(Ey1t, e1); Ey2t = cadd(Ey2t, e2); ++nyt; }
+            else { Ey1b = cadd(Ey1b, e1); Ey2b = cadd(Ey2b, e2); ++nyb; }
+        } else {
+            if (code & 8) { Ez1px = cadd(Ez1px, e1); Ez2px = cadd(Ez2px, e2); ++npx; }
+            else { Ez1mx = cadd(Ez1mx, e1); Ez2mx = cadd(Ez2mx, e2); ++nmx; }
+            if (code & 16) { Ez1py = cadd(Ez1py, e1); Ez2py = cadd(Ez2py, e2); ++npy; }
+            else { Ez1my = cadd(Ez1my, e1); Ez2my = cadd(Ez2my, e2); ++nmy; }
+        }
+    }
+    if (nxt > 0) { Ex1t = cdivn(Ex1t, nxt); Ex2t = cdivn(Ex2t, nxt); }
+    if (nxb > 0) { Ex1b = cdivn(Ex1b, nxb); Ex2b = cdivn(Ex2b, nxb); }
+    if (nyt > 0) { Ey1t = cdivn(Ey1t, nyt); Ey2t = cdivn(Ey2t, nyt); }
+    if (nyb > 0) { Ey1b = cdivn(Ey1b, nyb); Ey2b = cdivn(Ey2b, nyb); }
+    if (npx > 0) { Ez1px = cdivn(Ez1px, npx); Ez2px = cdivn(Ez2px, npx); }
+    if (nmx > 0) { Ez1mx = cdivn(Ez1mx, nmx); Ez2mx = cdivn(Ez2mx, nmx); }
+    if (npy > 0) { Ez1py = cdivn(Ez1py, npy); Ez2py = cdivn(Ez2py, npy); }
+    if (nmy > 0) { Ez1my = cdivn(Ez1my, nmy); Ez2my = cdivn(Ez2my, nmy); }
+    const bool bx = nxt > 0 && nxb > 0, by = nyt > 0 && nyb > 0;
+    const double2 Ex1 = bx ? chalf(Ex1t, Ex1b) : (nxt > 0 ? Ex1t : Ex1b);
+    const double2 Ey1 = by ? chalf(Ey1t, Ey1b) : (nyt > 0 ? Ey1t : Ey1b);
+    const double2 Ex2 = bx ? chalf(Ex2t, Ex2b) : (nxt > 0 ? Ex2t : Ex2b);
+    const double2 Ey2 = by ? chalf(Ey2t, Ey2b) : (nyt > 0 ? Ey2t : Ey2b);
+    double2 dEx1 = zero2(), dEx2 = zero2(), dEy1 = zero2(), dEy2 = zero2();
+    if (bx) { dEx1 = cscale(csub(Ex1t, Ex1b), 1.0 / 1.0); dEx1 = make_double2(dEx1.x / cdz, dEx1.y / cdz);
+              dEx2 = csub(Ex2t, Ex2b); dEx2 = make_double2(dEx2.x / cdz, dEx2.y / cdz); }
+    if (by) { dEy1 = csub(Ey1t, Ey1b); dEy1 = make_double2(dEy1.x / cdz, dEy1.y / cdz);
+              dEy2 = csub(Ey2t, Ey2b); dEy2 = make_double2(dEy2.x / cdz, dEy2.y / cdz); }
+    double2 dEz1x = zero2(), dEz2x = zero2(), dEz1y = zero2(), dEz2y = zero2();
+    if (npx > 0 && nmx > 0) {
+        dEz1x = csub(Ez1px, Ez1mx); dEz1x = make_double2(dEz1x.x / cdx, dEz1x.y / cdx);
+        dEz2x = csub(Ez2px, Ez2mx); dEz2x = make_double2(dEz2x.x / cdx, dEz2x.y / cdx);
+    }
+    if (npy > 0 && nmy > 0) {
+        dEz1y = csub(Ez1py, Ez1my); dEz1y = make_double2(dEz1y.x / cdy, dEz1y.y / cdy);
+        dEz2y = csub(Ez2py, Ez2my); dEz2y = make_double2(dEz2y.x / cdy, dEz2y.y / cdy);
+    }
+    const double2 Hx1 = cdiv(csub(dEz1y, dEy1), iwmu);
+    const double2 Hy1 = cdiv(csub(dEx1, dEz1x), iwmu);
+    const double2 Hx2 = cdiv(csub(dEz2y, dEy2), iwmu);
+    const double2 Hy2 = cdiv(csub(dEx2, dEz2x), iwmu);
+    const double2 det = csub(cmul(Hx1, Hy2), cmul(Hx2, Hy1));
+    H.Hx1 = Hx1; H.Hy1 = Hy1; H.Hx2 = Hx2; H.Hy2 = Hy2; H.det = det;
+    H.cdx = cdx; H.cdy = cdy; H.cdz = cdz;
+    double2 Zxx, Zxy, Zyx, Zyy;
+    if (hypot(det.x, det.y) > 1e-30) {
+        Zxx = cdiv(csub(cmul(Ex1, Hy2), cmul(Ex2, Hy1)), det);
+        Zxy = cdiv(csub(cmul(Ex2, Hx1), cmul(Ex1, Hx2)), det);
+        Zyx = cdiv(csub(cmul(Ey1, Hy2), cmul(Ey2, Hy1)), det);
+        Zyy = cdiv(csub(cmul(Ey2, Hx1), cmul(Ey1, Hx2)), det);
+    } else {
+        const double2 z1 = csqrt_d(cdiv(iwmu, make_double2(st.sigma_cell[s], 0.0)));
+        Zxx = zero2(); Zxy = z1; Zyx = cneg(z1); Zyy = zero2();
+    }
+    H.Zxx = Zxx; H.Zxy = Zxy; H.Zyx = Zyx; H.Zyy = Zyy;
+    hc[i] = H;
+    zo[0] = Zxx; zo[1] = Zxy; zo[2] = Zyx; zo[3] = Zyy;
+}
+
+__global__ void k_wr(int ns, int nf, int nf_total, int f0, const double2* __restrict__ obs,
+                     const double* __restrict__ err, const double2* __restrict__ Z, double2* wr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf * ns * 4) return;
+    const int f = i / (ns * 4), s = (i / 4) % ns, c = i % 4;
+    const size_t o = ((size_t)s * nf_total + f0 + f) * 4 + c;
+    const double e = err[o];
+    double2 v = zero2();
+    if (e > 0.0) {
+        const double w = 1.0 / e;
+        const double2 d = csub(obs[o], Z[((size_t)f * ns + s) * 4 + c]);
+        v = make_double2(w * w * d.x, -(w * w * d.y));
+    }
+    wr[((size_t)f * ns + s) * 4 + c] = v;
+}
+
+// forward_solver_fv.cpp:1837-2010, one thread per frequency (stations may share edges)
+__global__ void k_adjoint_rhs(StationDev st, const double2* __restrict__ wr, const HCache* __restrict__ hcs,
+                              const double* __restrict__ omegas, int nf, VecK out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int K = out.K;
+    const double2 iwmu = make_double2(0.0, omegas[f] * kMu0);
+    for (int s = 0; s < st.ns; ++s) {
+        if (st.cell[s] < 0) continue;
+        const double2* w = wr + ((size_t)f * st.ns + s) * 4;
+        const HCache hc = hcs[(size_t)f * st.ns + s];
+        if (hypot(hc.det.x, hc.det.y) < 1e-30) continue;
+        const double2 sx1 = cdiv(csub(cmul(w[0], hc.Hy2), cmul(w[1], hc.Hx2)), hc.det);
+        const double2 sy1 = cdiv(csub(cmul(w[2], hc.Hy2), cmul(w[3], hc.Hx2)), hc.det);
+        const double2 sx2 = cdiv(cadd(cmul(cneg(w[0]), hc.Hy1), cmul(w[1], hc.Hx1)), hc.det);
+        const double2 sy2 = cdiv(cadd(cmul(cneg(w[2]), hc.Hy1), cmul(w[3], hc.Hx1)), hc.det);
+        const double2 aHx1 = cneg(cadd(cmul(hc.Zxx, sx1), cmul(hc.Zyx, sy1)));
+        const double2 aHy1 = cneg(cadd(cmul(hc.Zxy, sx1), cmul(hc.Zyy, sy1)));
+        const double2 aHx2 = cneg(cadd(cmul(hc.Zxx, sx2), cmul(hc.Zyx, sy2)));
+        const double2 aHy2 = cneg(cadd(cmul(hc.Zxy, sx2), cmul(hc.Zyy, sy2)));
+        int nxt = 0, nxb = 0, nyt = 0, nyb = 0, npx = 0, nmx = 0, npy = 0, nmy = 0;
+        for (int q = st.e_ptr[s]; q < st.e_ptr[s + 1]; ++q) {
+            const unsigned char code = st.e_code[q];
+            const int d = code & 3;
+            if (d == 0) { if (code & 4) ++nxt; else ++nxb; }
+            else if (d == 1) { if (code & 4) ++nyt; else ++nyb; }
+            else { if (code & 8) ++npx; else ++nmx; if (code & 16) ++npy; else ++nmy; }
+        }
+        double wxt = nxt > 0 ? 0.5 / nxt : 0.0, wxb = nxb > 0 ? 0.5 / nxb : 0.0;
+        double wyt = nyt > 0 ? 0.5 / nyt : 0.0, wyb = nyb > 0 ? 0.5 / nyb : 0.0;
+        if (nxt == 0) wxb = nxb > 0 ? 1.0 / nxb : 0.0;
+        if (nxb == 0) wxt = nxt > 0 ? 1.0 / nxt : 0.0;
+        if (nyt == 0) wyb = nyb > 0 ? 1.0 / nyb : 0.0;
+        if (nyb == 0) wyt = nyt > 0 ? 1.0 / nyt : 0.0;
+        const double2 icdz = cdiv(make_double2(1.0, 0.0), make_double2(iwmu.x * hc.cdz, iwmu.y * hc.cdz));
+        const double2 icdx = cdiv(make_double2(1.0, 0.0), make_double2(iwmu.x * hc.cdx, iwmu.y * hc.cdx));
+        const double2 icdy = cdiv(make_double2(1.0, 0.0), make_double2(iwmu.x * hc.cdy, iwmu.y * hc.cdy));
+        for (int q = st.e_ptr[s]; q < st.e_ptr[s + 1]; ++q) {
+            const int row = st.e_row[q];
+            const unsigned char code = st.e_code[q];
+            const int d = code & 3;
+            double2* a1 = out.p + (size_t)row * K + 2 * f;
+            double2* a2 = a1 + 1;
+            if (d == 0) {
+                const bool top = code & 4;
+                const double we = top ? wxt : wxb;
+                *a1 = cadd(*a1, cscale(sx1, we));
+                *a2 = cadd(*a2, cscale(sx2, we));
+                if (top && nxt > 0) {
+                    const double2 wh = make_double2(icdz.x / nxt, icdz.y / nxt);
+                    *a1 = cadd(*a1, cmul(aHy1, wh)); *a2 = cadd(*a2, cmul(aHy2, wh));
+                } else if (!top && nxb > 0) {
+                    const double2 wh = make_double2(-icdz.x / nxb, -icdz.y / nxb);
+                    *a1 = cadd(*a1, cmul(aHy1, wh)); *a2 = cadd(*a2, cmul(aHy2, wh));
+                }
+            } else if (d == 1) {
+                const bool top = code & 4;
+                const double we = top ? wyt : wyb;
+                *a1 = cadd(*a1, cscale(sy1, we));
+                *a2 = cadd(*a2, cscale(sy2, we));
+                if (top && nyt > 0) {
+                    const double2 wh = make_double2(-icdz.x / nyt, -icdz.y / nyt);
+                    *a1 = cadd(*a1, cmul(aHx1, wh)); *a2 = cadd(*a2, cmul(aHx2, wh));
+                } else if (!top && nyb > 0) {
+                    const double2 wh = make_double2(icdz.x / nyb, icdz.y / nyb);
+                    *a1 = cadd(*a1, cmul(aHx1, wh)); *a2 = cadd(*a2, cmul(aHx2, wh));
+                }
+            } else {
+                const bool py = code & 16;
+                if (py && npy > 0) {
+                    const double2 wh = make_double2(icdy.x / npy, icdy.y / npy);
+                    *a1 = cadd(*a1, cmul(aHx1, wh)); *a2 = cadd(*a2, cmul(aHx2, wh));
+                } else if (!py && nmy > 0) {
+                    const double2 wh = make_double2(-icdy.x / nmy, -icdy.y / nmy);
+                    *a1 = cadd(*a1, cmul(aHx1, wh)); *a2 = cadd(*a2, cmul(aHx2, wh));
+                }
+                const bool px = code & 8;
+                if (px && npx > 0) {
+                    const double2 wh = make_double2(-icdx.x / npx, -icdx.y / npx);
+                    *a1 = cadd(*a1, cmul(aHy1, wh)); *a2 = cadd(*a2, cmul(aHy2, wh));
+                } else if (!px && nmx > 0) {
+                    const double2 wh = make_double2(icdx.x / nmx, icdx.y / nmx);
+                    *a1 = cadd(*a1, cmul(aHy1, wh)); *a2 = cadd(*a2, cmul(aHy2, wh));
+                }
+            }
+        }
+    }
+}
+
+// one thread per cell, frequencies and polarisations summed in order
+__global__ void k_sensitivity(MeshDev m, const double* __restrict__ sigma, VecK E, VecK lam,
+                              const double* __restrict__ omegas, int nf, int npol, double* g) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.nc) return;
+    const double sc = sigma[c];
+    double acc = g[c];
+    for (int f = 0; f < nf; ++f) {
+        double gsum = 0.0;
+        for (int p = 0; p < npol; ++p) {
+            const int kE = npol * f + p;
+            double2 s = zero2();
+            for (int q = m.cell_ptr[c]; q < m.cell_ptr[c + 1]; ++q) {
+                const int e = m.cell_edge[q];
+                if (m.flags[e] & kFlagSensFixed) continue;
+                const int na = m.nadj[e];
+                if (na == 0) continue;
+                const double dMe = sc * m.adual[e] * m.elen[e] / na;
+                const double2 le = cmul(lam.p[(size_t)e * lam.K + kE], E.p[(size_t)e * E.K + kE]);
+                s.x += le.x * dMe;
+                s.y += le.y * dMe;
+            }
+            gsum += -omegas[f] * s.y;   // Re(i omega s)
+        }
+        acc += gsum;
+    }
+    g[c] = acc;
+}
+
+__global__ void k_pert_rhs(MeshDev m, const double* __restrict__ sigma, const double* __restrict__ dsig,
+                           VecK E, int kE, double omega, VecK out, int kout) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= m.n_pad) return;
+    double2 acc = zero2();
+    if (!(m.flags[row] & kFlagPad)) {
+        const int a0 = m.adj_ptr[row], a1 = m.adj_ptr[row + 1];
+        const double L = m.elen[row];
+        const double vol = L * L * L;
+        double si = 0.0;
+        int na = 0;
+        for (int k = a0; k < a1; ++k) {
+            const double sg = sigma[m.adj_cell[k]];
+            if (sg > 1e-30) { si += 1.0 / sg; ++na; }
+        }
+        const double sa = (na > 0 && si > 1e-30) ? na / si : 1e-8;
+        const double2 ev = E.p[(size_t)row * E.K + kE];
+        for (int k = a0; k < a1; ++k) {
+            const int c = m.adj_cell[k];
+            const double ds = dsig[c];
+            if (fabs(ds) < 1e-30) continue;
+            const double sc = sigma[c];
+            const double dMe = vol * sa * sa / (na * sc * sc);
+            const double2 t = cmul(make_double2(0.0, omega * (ds * dMe)), ev);
+            acc = csub(acc, t);
+        }
+    }
+    out.p[(size_t)row * out.K + kout] = acc;
+}
+
+__global__ void k_delta_z(StationDev st, VecK dE, int kE, const HCache* __restrict__ hcs, int pol, double2* dZ) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= st.ns) return;
+    double2* o = dZ + (size_t)s * 4;
+    o[0] = o[1] = o[2] = o[3] = zero2();
+    if (st.cell[s] < 0) return;
+    double2 dEx = zero2(), dEy = zero2();
+    int nx = 0, ny = 0;
+    for (int q = st.e_ptr[s]; q < st.e_ptr[s + 1]; ++q) {
+        const int d = st.e_code[q] & 3;
+        const double2 v = dE.p[(size_t)st.e_row[q] * dE.K + kE];
+        if (d == 0) { dEx = cadd(dEx, v); ++nx; }
+        else if (d == 1) { dEy = cadd(dEy, v); ++ny; }
+    }
+    if (nx > 0) dEx = cdivn(dEx, nx);
+    if (ny > 0) dEy = cdivn(dEy, ny);
+    const HCache hc = hcs[s];
+    if (hypot(hc.det.x, hc.det.y) < 1e-30) return;
+    const double2 id = cdiv(make_double2(1.0, 0.0), hc.det);
+    if (pol == 1) {
+        o[0] = cmul(cmul(dEx, hc.Hy2), id); o[1] = cmul(cmul(dEx, cneg(hc.Hx2)), id);
+        o[2] = cmul(cmul(dEy, hc.Hy2), id); o[3] = cmul(cmul(dEy, cneg(hc.Hx2)), id);
+    } else {
+        o[0] = cmul(cmul(dEx, cneg(hc.Hy1)), id); o[1] = cmul(cmul(dEx, hc.Hx1), id);
+        o[2] = cmul(cmul(dEy, cneg(hc.Hy1)), id); o[3] = cmul(cmul(dEy, hc.Hx1), id);
+    }
+}
+
+}  // namespace
+
+void edge_mass(const MeshDev& m, const double* sigma, double* Me, double* me_dc, cudaStream_t s) {
+    k_edge_mass<<<grid1(m.n_pad), kBlock, 0, s>>>(m, sigma, Me, me_dc);
+    ck();
+}
+
+void assemble_diag(const MeshDev& m, const double* Me, const double* omegas, int nf, double2* d,
+                   double2* dinv, float2* d32, float2* dinv32, cudaStream_t s) {
+    const long n = (long)m.n_pad * nf;
+    k_assemble_diag<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, Me, omegas, nf, d, dinv, d32, dinv32);
+    ck();
+}
+
+void primary_field(const MeshDev& m, VecK out, const RhsInfo& info, bool bc_only, cudaStream_t s) {
+    const long n = (long)m.n_pad * out.K;
+    k_primary<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, out, info, bc_only ? 1 : 0);
+    ck();
+}
+
+void lift_rhs(const MeshDev& m, VecK ebc, VecK rhs, cudaStream_t s) {
+    const long n = (long)m.n_pad * rhs.K;
+    k_lift<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, ebc, rhs);
+    ck();
+}
+
+void vsub(long n, const double2* a, const double2* b, double2* out, cudaStream_t s) {
+    k_vsub<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(n, a, b, out);
+    ck();
+}
+
+void interpolate_hanging(const MeshDev& m, VecK x, bool sequential, cudaStream_t s) {
+    if (m.nhp == 0) return;
+    if (sequential) {
+        k_hanging_seq<<<1, 32, 0, s>>>(m, x);
+    } else {
+        const long n = (long)m.nhp * x.K;
+        k_hanging<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, x);
+    }
+    ck();
+}
+
+void combine_total(const MeshDev& m, VecK epri, VecK esec, VecK ebc, VecK e, cudaStream_t s) {
+    const long n = (long)m.n_pad * e.K;
+    k_combine<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, epri, esec, ebc, e);
+    ck();
+}
+
+void to_permuted(const MeshDev& m, const double2* ref, int K, int k, VecK dst, cudaStream_t s) {
+    (void)K;
+    k_to_perm<<<grid1(m.ne), kBlock, 0, s>>>(m, ref, dst, k);
+    ck();
+}
+
+void from_permuted(const MeshDev& m, VecK src, int k, double2* ref, cudaStream_t s) {
+    k_from_perm<<<grid1(m.ne), kBlock, 0, s>>>(m, src, k, ref);
+    ck();
+}
+
+void fill_zero(VecK v, long n_pad, cudaStream_t s) {
+    cudaMemsetAsync(v.p, 0, sizeof(double2) * (size_t)n_pad * v.K, s);
+    ck();
+}
+
+void dc_build_laplacian(const MeshDev& m, const double* me_dc, DcWork w, cudaStream_t s) {
+    k_dc_lap<<<grid1(m.nn), kBlock, 0, s>>>(m, me_dc, w);
+    ck();
+}
+
+void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStream_t s) {
+    const long n = (long)m.nn * rhs.K;
+    k_dc_phi0<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, rhs, info, w);
+    ck();
+}
+
+long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
+                  double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk) {
+    const int K = E.K;
+    long long launches = 0;
+    std::vector<DcState> hs(K);
+    for (int k = 0; k < K; ++k) {
+        DcState S{};
+        S.active = active_host[k] ? 1 : 0;
+        S.done = S.active ? 0 : 1;
+        hs[k] = S;
+    }
+    cudaMemcpyAsync(w.st, hs.data(), sizeof(DcState) * K, cudaMemcpyHostToDevice, s);
+    const int gv = red.max_blocks;
+    const int cg_max = m.nn > 500 ? m.nn : 500;
+    const long nn_k = (long)m.nn * K;
+    const int ge = (int)(((long)m.n_pad * K + kBlock - 1) / kBlock);
+    for (int outer = 0; outer < max_outer; ++outer) {
+        k_dc_divj<<<gv, kBlock, 0, s>>>(m, me_dc, E, use_phi0 ? 1 : 0, w, tol, red);
+        ck(); ++launches;
+        cudaMemcpyAsync(hs.data(), w.st, sizeof(DcState) * K, cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        bool any = false;
+        for (int k = 0; k < K; ++k) any |= (hs[k].active && !hs[k].done);
+        if (!any) break;
+        k_dc_cg_init<<<gv, kBlock, 0, s>>>(m.nn, K, w, red);
+        ck(); ++launches;
+        for (int it = 0; it < cg_max;) {
+            const int n_it = (cg_max - it) < cg_chunk ? (cg_max - it) : cg_chunk;
+            for (int j = 0; j < n_it; ++j) {
+                k_dc_cg_ap<<<gv, kBlock, 0, s>>>(m, K, w, red);
+                k_dc_cg_update<<<gv, kBlock, 0, s>>>(m.nn, K, cg_max, w, red);
+                k_dc_cg_p<<<gv, kBlock, 0, s>>>(m.nn, K, w);
+                launches += 3;
+            }
+            ck();
+            it += n_it;
+            cudaMemcpyAsync(hs.data(), w.st, sizeof(DcState) * K, cudaMemcpyDeviceToHost, s);
+            cudaStreamSynchronize(s);
+            bool run = false;
+            for (int k = 0; k < K; ++k) run |= hs[k].cg_run != 0;
+            if (!run) break;
+        }
+        k_dc_grad<<<ge, kBlock, 0, s>>>(m, E, w);
+        k_dc_outer_done<<<1, 32, 0, s>>>(K, w);
+        ck(); launches += 2;
+    }
+    (void)nn_k;
+    return launches;
+}
+
+void station_impedance(const StationDev& st, VecK E, const double* omegas, int nf, HCache* hc, double2* Z,
+                       cudaStream_t s) {
+    const int n = nf * st.ns;
+    if (n == 0) return;
+    k_station_z<<<(n + 127) / 128, 128, 0, s>>>(st, E, omegas, nf, hc, Z);
+    ck();
+}
+
+void weighted_residual(int ns, int nf, int nf_total, int f0, const double2* obs, const double* err,
+                       const double2* Z, double2* wr, cudaStream_t s) {
+    const int n = nf * ns * 4;
+    if (n == 0) return;
+    k_wr<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(ns, nf, nf_total, f0, obs, err, Z, wr);
+    ck();
+}
+
+void adjoint_rhs(const StationDev& st, const MeshDev& m, const double2* wr, const HCache* hc,
+                 const double* omegas, int nf, VecK out, cudaStream_t s) {
+    (void)m;
+    k_adjoint_rhs<<<1, 32, 0, s>>>(st, wr, hc, omegas, nf, out);
+    ck();
+}
+
+void sensitivity(const MeshDev& m, const double* sigma, VecK E, VecK lam, const double* omegas, int nf,
+                 int npol, double* g, cudaStream_t s) {
+    k_sensitivity<<<grid1(m.nc), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    ck();
+}
+
+void perturbation_rhs(const MeshDev& m, const double* sigma, const double* dsigma, VecK E, int kE, double omega,
+                      VecK out, int kout, cudaStream_t s) {
+    k_pert_rhs<<<grid1(m.n_pad), kBlock, 0, s>>>(m, sigma, dsigma, E, kE, omega, out, kout);
+    ck();
+}
+
+void delta_impedance(const StationDev& st, VecK dE, int kE, const HCache* hc, int pol, double2* dZ,
+                     cudaStream_t s) {
+    if (st.ns == 0) return;
+    k_delta_z<<<(st.ns + 127) / 128, 128, 0, s>>>(st, dE, kE, hc, pol, dZ);
+    ck();
+}
+
+}  // namespace phys
+}  // namespace m3d

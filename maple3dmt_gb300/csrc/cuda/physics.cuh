@@ -1,0 +1,169 @@
+// Device data of one mesh and the non-Krylov kernels of the solve path:
+// system diagonal (assembly), primary field and boundary lift, hanging-edge
+// interpolation, divergence correction, station impedances, adjoint source,
+// sensitivity and the J.v pieces.  Each launcher cites the reference code it
+// restates.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "krylov.cuh"
+
+namespace m3d {
+
+// Row flags (permuted edge rows).
+enum : unsigned char {
+    kFlagConstrained = 1,   // identity row in A (solve BC or dead)   forward_solver_fv.cpp:214-217
+    kFlagBc = 2,            // Dirichlet edge of the solve            :166-194
+    kFlagDead = 4,          // dead coarse hanging edge               :206-208
+    kFlagDcBc = 8,          // BC edge of compute_bc_flags_           :559-569
+    kFlagSensFixed = 16,    // skipped by compute_sensitivity         :1019-1029
+    kFlagPad = 32,          // padding row of the sliced layout
+};
+
+struct MeshDev {
+    int ne, n_pad, nc, nn, n_slices;
+    int* perm;          // [n_pad] permuted row -> reference edge id (-1 padding)
+    int* iperm;         // [ne] reference edge id -> permuted row
+    unsigned char* flags;  // [n_pad]
+    signed char* dir;   // [n_pad] edge direction
+    double* ez;         // [n_pad] edge midpoint z
+    double* s_diag;     // [n_pad] S_ii
+    double* me_geom;    // [n_pad] A_dual * L
+    double* adual;      // [n_pad]
+    double* elen;       // [n_pad]
+    int* nadj;          // [n_pad] number of adjacent cells
+    int* adj_ptr;       // [n_pad + 1] adjacency of permuted rows (reference cell order)
+    int* adj_cell;
+    int* lift_ptr;      // [n_pad + 1] free row -> BC columns (reference column order)
+    int* lift_col;
+    double* lift_val;
+    int nhp;
+    int* hp;            // [nhp][3] coarse, child1, child2 (permuted rows)
+    // nodes
+    int* inc_ptr;       // [nn + 1] node -> incident edges, reference edge order
+    int* inc_edge;      // permuted edge row
+    int* inc_other;     // other node
+    double* inc_gv;     // G[e, v]
+    double* inc_gw;     // G[e, other]
+    unsigned char* node_bc;  // [nn]
+    int* e_node;        // [n_pad][2] node ids in G's column order (pads: 0)
+    double* e_g;        // [n_pad][2] G values
+    // cells
+    int* cell_ptr;      // [nc + 1] cell -> edges (StaggeredGrid::cell_edges order), permuted rows
+    int* cell_edge;
+};
+
+// Per station data, built by the host at m3d_set_stations.
+struct StationDev {
+    int ns;
+    int* cell;          // [ns] station cell (-1 none)
+    double* geom;       // [ns][6] cx cy cz cdx cdy cdz
+    int* e_ptr;         // [ns + 1]
+    int* e_row;         // permuted rows of the cell's edges, cell_edges order
+    unsigned char* e_code;  // bit0-1 direction, bit2 top (z > cz), bit3 +x (x > cx), bit4 +y (y > cy)
+    double* sigma_cell; // [ns] sigma of the station cell (1-D fallback)
+};
+
+// Cached H / Z of a station at one frequency (StationHCache, forward_solver_fv.h:216-223).
+struct HCache {
+    double2 Hx1, Hy1, Hx2, Hy2, det, Zxx, Zxy, Zyx, Zyy;
+    double cdx, cdy, cdz, pad_;
+};
+
+// Vector of K right-hand sides, [n_pad][K] complex double.
+struct VecK {
+    double2* p;
+    int K;
+};
+
+// Per right-hand side data of a batch.
+struct RhsInfo {
+    int K;
+    int f[dev::kMaxRhs];         // frequency slot of the diagonal arrays
+    int pol[dev::kMaxRhs];       // source polarisation 0 (Ex) / 1 (Ey), -1 none
+    double2 ik[dev::kMaxRhs];    // sqrt(i omega mu0 sigma_bg) (forward_solver_fv.cpp:121)
+    double omega[dev::kMaxRhs];
+};
+
+namespace phys {
+
+// build_edge_mass (operators.cpp:481-518) and me_sigma of
+// build_div_laplacian / compute_div_sigma_E (:956-973, :1030-1048).
+void edge_mass(const MeshDev& m, const double* sigma, double* Me, double* me_dc, cudaStream_t s);
+// A diagonal for each frequency: S_ii + i omega Me_i on free rows, 1 on
+// constrained / padding rows (operators.cpp:607-616, forward_solver_fv.cpp:224-234),
+// and its SSOR inverse (ssor.h:37-44). d/dinv: [nf][n_pad]; d32/dinv32 optional.
+void assemble_diag(const MeshDev& m, const double* Me, const double* omegas, int nf, double2* d,
+                   double2* dinv, float2* d32, float2* dinv32, cudaStream_t s);
+// E_primary on edges of direction pol for each rhs (forward_solver_fv.cpp:121-136, :318-323);
+void primary_field(const MeshDev& m, VecK out, const RhsInfo& info, bool bc_only, cudaStream_t s);
+// rhs_total of build_rhs (:244-255) from the BC values in `ebc`.
+void lift_rhs(const MeshDev& m, VecK ebc, VecK rhs, cudaStream_t s);
+// out = a - b (elementwise, all rhs).
+void vsub(long n, const double2* a, const double2* b, double2* out, cudaStream_t s);
+// interpolate_hanging (:258-261) on every rhs of x.
+void interpolate_hanging(const MeshDev& m, VecK x, bool sequential, cudaStream_t s);
+// E = E_pri + E_sec; E_bc on BC rows (:357-361).
+void combine_total(const MeshDev& m, VecK epri, VecK esec, VecK ebc, VecK e, cudaStream_t s);
+// gather / scatter between reference order (host layout [K][ne]) and permuted [n_pad][K]
+void to_permuted(const MeshDev& m, const double2* ref, int K, int k, VecK dst, cudaStream_t s);
+void from_permuted(const MeshDev& m, VecK src, int k, double2* ref, cudaStream_t s);
+void fill_zero(VecK v, long n_pad, cudaStream_t s);
+
+// ---- divergence correction (forward_solver_fv.cpp:623-722) ----
+struct DcState {
+    double div0, dn, rn;
+    double2 rz, alpha, beta;
+    int outer;      // outer iterations done
+    int done;       // outer loop finished for this rhs
+    int cg_run;     // PCG still iterating
+    int cg_iter;
+    int active;     // rhs takes part
+    int pad_;
+};
+struct DcWork {
+    double2 *divJ, *phi, *r, *z, *p, *Ap, *phi0;  // [nn][K]
+    double* lap_diag;   // [nn] L_vv (1 on BC nodes)
+    double* lap_off;    // [inc] off-diagonal per incidence entry (0 on BC rows / columns)
+    double* jac_diag;   // [nn] Jacobi diagonal (1 where L has no diagonal entry)
+    DcState* st;        // [K]
+};
+
+// Laplacian values for the current sigma (build_div_laplacian + Dirichlet rows/cols, :581-606).
+void dc_build_laplacian(const MeshDev& m, const double* me_dc, DcWork w, cudaStream_t s);
+// phi0 = G^T rhs / (i omega) (compute_phi0 :893-908) for every rhs.
+void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStream_t s);
+// One full divcorr_poisson_ call on every active rhs of E; phi0 optional.
+// Returns the number of kernel launches. Iteration caps: outer <= max_outer,
+// PCG <= max(500, nn) per outer (the reference's caps).
+long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w,
+                  int max_outer, double tol, const int* active_host, dev::RedScratch red,
+                  cudaStream_t s, int cg_chunk);
+
+// ---- stations (forward_solver_fv.cpp:1490-1727, :1804-2065) ----
+// Z and H cache per (frequency f, station); E1 = rhs 2f, E2 = rhs 2f+1 of E.
+void station_impedance(const StationDev& st, VecK E, const double* omegas, int nf, HCache* hc,
+                       double2* Z, cudaStream_t s);
+// weighted residual wr = w^2 conj(obs - pred), w = 1/err (inversion_fv.cpp:258-271);
+// obs/err layout [ns][nf_total][4] with frequency offset f0.
+void weighted_residual(int ns, int nf, int nf_total, int f0, const double2* obs, const double* err,
+                       const double2* Z, double2* wr, cudaStream_t s);
+// adjoint source for every frequency: rhs 2f <- pol1, 2f+1 <- pol2 (must be zeroed first).
+void adjoint_rhs(const StationDev& st, const MeshDev& m, const double2* wr, const HCache* hc,
+                 const double* omegas, int nf, VecK out, cudaStream_t s);
+// g[c] (+)= sum_f Re(i omega_f sum_e lambda_e E_e dMe) over both polarisations
+// (compute_sensitivity :989-1059 summed as in inversion_fv.cpp:282-288).
+// E rhs 2f+p pairs with lambda rhs 2f+p; npol = 1 uses rhs f only.
+void sensitivity(const MeshDev& m, const double* sigma, VecK E, VecK lam, const double* omegas,
+                 int nf, int npol, double* g, cudaStream_t s);
+// build_perturbation_rhs (:945-984) for one rhs.
+void perturbation_rhs(const MeshDev& m, const double* sigma, const double* dsigma, VecK E, int kE,
+                      double omega, VecK out, int kout, cudaStream_t s);
+// extract_delta_impedance_complex (:2018-2065).
+void delta_impedance(const StationDev& st, VecK dE, int kE, const HCache* hc, int pol, double2* dZ,
+                     cudaStream_t s);
+
+}  // namespace phys
+}  // namespace m3d

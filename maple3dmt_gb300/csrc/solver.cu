@@ -1,0 +1,901 @@
+// GpuSolver implementation: see solver.hpp.
+#include "solver.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <stdexcept>
+
+namespace m3d {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kMu0 = 4.0e-7 * kPi;
+
+void cuda_ok(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+T* dalloc(size_t n) {
+    T* p = nullptr;
+    if (n == 0) n = 1;
+    const cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) throw std::bad_alloc();
+    return p;
+}
+
+template <class T>
+T* dupload(const std::vector<T>& v, cudaStream_t s) {
+    T* p = dalloc<T>(v.size());
+    if (!v.empty()) cuda_ok(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "upload");
+    return p;
+}
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+int pow2_at_least(int k) {
+    int K = 2;
+    while (K < k) K *= 2;
+    return K;
+}
+
+__global__ void k_zero_col(double2* x, int K, int k, int n_pad) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n_pad) x[(size_t)r * K + k] = make_double2(0.0, 0.0);
+}
+
+
+}  // namespace
+
+GpuSolver::GpuSolver(int dev_) : device(dev_) {
+    m3d_params_default(&P);
+    std::memset(&stats, 0, sizeof(stats));
+}
+
+GpuSolver::~GpuSolver() { free_all(); }
+
+void GpuSolver::free_all() {
+    if (stream) cudaStreamSynchronize(stream);
+    dfree(md.perm); dfree(md.iperm); dfree(md.flags); dfree(md.dir); dfree(md.ez); dfree(md.s_diag);
+    dfree(md.me_geom); dfree(md.adual); dfree(md.elen); dfree(md.nadj); dfree(md.adj_ptr); dfree(md.adj_cell);
+    dfree(md.lift_ptr); dfree(md.lift_col); dfree(md.lift_val); dfree(md.hp);
+    dfree(md.inc_ptr); dfree(md.inc_edge); dfree(md.inc_other); dfree(md.inc_gv); dfree(md.inc_gw);
+    dfree(md.node_bc); dfree(md.e_node); dfree(md.e_g); dfree(md.cell_ptr); dfree(md.cell_edge);
+    dfree(d_slice_off); dfree(d_slice_wl); dfree(d_slice_wu); dfree(d_col); dfree(d_val); dfree(d_val32);
+    dfree(d_sigma); dfree(d_Me); dfree(d_me_dc);
+    dfree(d_diag); dfree(d_dinv); dfree(d_diag32); dfree(d_dinv32); dfree(d_omegas);
+    dfree(red.partial); dfree(red.final_); dfree(red.counter);
+    dfree(kv.x); dfree(kv.b); dfree(kv.r); dfree(kv.r0); dfree(kv.p); dfree(kv.v); dfree(kv.s); dfree(kv.t);
+    dfree(kv.ph); dfree(kv.sh); dfree(kv.y);
+    dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
+    dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
+    dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_diag); dfree(dc.st);
+    dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
+    dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
+    dfree(d_host_stage); dfree(d_stage_real); dfree(d_states); dfree(d_states2);
+    if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
+    kv_K = 0; fwd_cap = 0; dc_K = 0; hc_cap = 0; obs_cap = 0; diag_cap = 0;
+    ready = false; have_sigma = false; lap_built = false; stations_set = false;
+}
+
+void GpuSolver::sync() { cuda_ok(cudaStreamSynchronize(stream), "stream sync"); }
+
+// ---------------------------------------------------------------------------
+// setup: layout, boundary sets, colouring, sliced-ELL permutation, upload
+// ---------------------------------------------------------------------------
+
+void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
+    free_all();
+    if (params) P = *params;
+    cuda_ok(cudaSetDevice(device), "cudaSetDevice");
+    cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+
+    LeafInput in;
+    for (int i = 0; i < 6; ++i) in.domain[i] = lv->domain[i];
+    in.min_level = lv->min_level; in.max_level = lv->max_level; in.nc = lv->n_cells;
+    in.level = lv->level; in.cx = lv->cx; in.cy = lv->cy; in.cz = lv->cz; in.type = lv->cell_type;
+    build_layout(in, L);
+    const int ne = L.ne;
+    const double* dm = L.domain;
+
+    // Boundary sets (forward_solver_fv.cpp:117, :166-217; :556-569; :1012-1029)
+    flags_ref.assign(ne, 0);
+    const double bt = L.cell_size0 * 0.1;
+    const double air = P.air_z_threshold;
+    for (int e = 0; e < ne; ++e) {
+        const double x = L.ex[e], y = L.ey[e], z = L.ez[e];
+        const bool onb = x <= dm[0] + bt || x >= dm[1] - bt || y <= dm[2] + bt || y >= dm[3] - bt ||
+                         z <= dm[4] + bt || z >= dm[5] - bt;
+        const bool is_bc = onb || z > air;
+        const bool dead = L.dead[e] != 0;
+        const bool on1 = x <= dm[0] + 1.0 || x >= dm[1] - 1.0 || y <= dm[2] + 1.0 || y >= dm[3] - 1.0 ||
+                         z <= dm[4] + 1.0 || z >= dm[5] - 1.0 || z > air;
+        unsigned char f = 0;
+        if (is_bc) f |= kFlagBc;
+        if (dead) f |= kFlagDead;
+        if (is_bc || dead) f |= kFlagConstrained;
+        if (!dead && on1) f |= kFlagDcBc;
+        if (dead || on1) f |= kFlagSensFixed;
+        flags_ref[e] = f;
+    }
+    auto free_row = [&](int e) { return !(flags_ref[e] & kFlagConstrained); };
+
+    // Greedy colouring of the free-free coupling graph in reference order.
+    std::vector<int> colour(ne, 0);
+    {
+        std::vector<int> mark(64, -1);
+        for (int i = 0; i < ne; ++i) {
+            if (!free_row(i)) { colour[i] = 0; continue; }
+            for (int k = L.s_ptr[i]; k < L.s_ptr[i + 1]; ++k) {
+                const int j = L.s_idx[k];
+                if (j >= i || !free_row(j)) continue;
+                const int c = colour[j];
+                if (c >= (int)mark.size()) mark.resize(c + 1, -1);
+                mark[c] = i;
+            }
+            int c = 0;
+            while (c < (int)mark.size() && mark[c] == i) ++c;
+            colour[i] = c;
+        }
+    }
+    // later neighbours are coloured afterwards; greedy above only looked at
+    // j < i, which is exactly the constraint set of sequential greedy.
+    const int n_col = *std::max_element(colour.begin(), colour.end()) + 1;
+
+    // Permutation: colour-major, reference order inside a colour, each colour
+    // padded to whole slices.
+    perm.clear();
+    colour_slices.assign(1, 0);
+    {
+        std::vector<std::vector<int>> byc(n_col);
+        for (int e = 0; e < ne; ++e) byc[colour[e]].push_back(e);
+        for (int c = 0; c < n_col; ++c) {
+            for (int e : byc[c]) perm.push_back(e);
+            while (perm.size() % dev::kSlice) perm.push_back(-1);
+            colour_slices.push_back((int)(perm.size() / dev::kSlice));
+        }
+    }
+    n_pad = (int)perm.size();
+    n_slices = n_pad / dev::kSlice;
+    iperm.assign(ne, -1);
+    for (int r = 0; r < n_pad; ++r) if (perm[r] >= 0) iperm[perm[r]] = r;
+
+    // Sliced ELL of the free-free off-diagonal part; lower (earlier colour)
+    // entries first, then upper, each in reference column order.
+    std::vector<int> slice_off(n_slices), slice_wl(n_slices), slice_wu(n_slices);
+    std::vector<int> ecol;
+    std::vector<double> eval;
+    {
+        long total = 0;
+        std::vector<int> nl(dev::kSlice), nu(dev::kSlice);
+        for (int s = 0; s < n_slices; ++s) {
+            int wl = 0, wu = 0;
+            for (int l = 0; l < dev::kSlice; ++l) {
+                const int e = perm[s * dev::kSlice + l];
+                int a = 0, b = 0;
+                if (e >= 0 && free_row(e))
+                    for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
+                        const int j = L.s_idx[k];
+                        if (j == e || !free_row(j)) continue;
+                        if (colour[j] < colour[e]) ++a; else ++b;
+                    }
+                wl = std::max(wl, a); wu = std::max(wu, b);
+            }
+            slice_off[s] = (int)total;
+            slice_wl[s] = wl; slice_wu[s] = wu;
+            total += (long)(wl + wu) * dev::kSlice;
+            if (total > 2000000000L) throw std::runtime_error("mesh too large for 32-bit ELL offsets");
+        }
+        ecol.assign(total, 0);
+        eval.assign(total, 0.0);
+        for (int s = 0; s < n_slices; ++s) {
+            const int off = slice_off[s], wl = slice_wl[s], wu = slice_wu[s];
+            for (int l = 0; l < dev::kSlice; ++l) {
+                const int r = s * dev::kSlice + l;
+                const int e = perm[r];
+                int a = 0, b = 0;
+                for (int k = 0; k < wl + wu; ++k) { ecol[off + k * dev::kSlice + l] = r; eval[off + k * dev::kSlice + l] = 0.0; }
+                if (e < 0 || !free_row(e)) continue;
+                for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
+                    const int j = L.s_idx[k];
+                    if (j == e || !free_row(j)) continue;
+                    const int slot = (colour[j] < colour[e]) ? a++ : wl + b++;
+                    ecol[off + slot * dev::kSlice + l] = iperm[j];
+                    eval[off + slot * dev::kSlice + l] = L.s_val[k];
+                }
+            }
+        }
+    }
+
+    // Per permuted row data.
+    std::vector<unsigned char> flags(n_pad, kFlagPad);
+    std::vector<signed char> dir(n_pad, 0);
+    std::vector<double> ez(n_pad, 0.0), sdiag(n_pad, 1.0), megeom(n_pad, 0.0), adual(n_pad, 0.0), elen(n_pad, 1.0);
+    std::vector<int> nadj(n_pad, 0), adj_ptr(n_pad + 1, 0), adj_cell;
+    std::vector<int> lift_ptr(n_pad + 1, 0), lift_col;
+    std::vector<double> lift_val;
+    for (int r = 0; r < n_pad; ++r) {
+        const int e = perm[r];
+        if (e >= 0) {
+            flags[r] = flags_ref[e];
+            dir[r] = (signed char)L.edir[e];
+            ez[r] = L.ez[e];
+            for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) if (L.s_idx[k] == e) sdiag[r] = L.s_val[k];
+            megeom[r] = L.adual[e] * L.elen[e];
+            adual[r] = L.adual[e];
+            elen[r] = L.elen[e];
+            nadj[r] = L.adj_ptr[e + 1] - L.adj_ptr[e];
+            for (int k = L.adj_ptr[e]; k < L.adj_ptr[e + 1]; ++k) adj_cell.push_back(L.adj[k]);
+            if (free_row(e))
+                for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
+                    const int j = L.s_idx[k];
+                    if (j != e && (flags_ref[j] & kFlagBc)) { lift_col.push_back(iperm[j]); lift_val.push_back(L.s_val[k]); }
+                }
+        }
+        adj_ptr[r + 1] = (int)adj_cell.size();
+        lift_ptr[r + 1] = (int)lift_col.size();
+    }
+    std::vector<int> hp(3 * L.hp.size());
+    {
+        std::vector<char> coarse(ne, 0);
+        for (const auto& h : L.hp) coarse[h[0]] = 1;
+        hp_sequential = false;
+        for (size_t i = 0; i < L.hp.size(); ++i) {
+            for (int k = 0; k < 3; ++k) hp[3 * i + k] = iperm[L.hp[i][k]];
+            if (coarse[L.hp[i][1]] || coarse[L.hp[i][2]]) hp_sequential = true;
+        }
+    }
+    // node incidence in reference edge order; G[e, n1] = -1/L, G[e, n2] = +1/L
+    const int nn = L.nn;
+    std::vector<int> inc_ptr(nn + 1, 0), inc_edge(2 * ne), inc_other(2 * ne);
+    std::vector<double> inc_gv(2 * ne), inc_gw(2 * ne);
+    std::vector<unsigned char> node_bc(nn, 0);
+    std::vector<int> e_node(2 * n_pad, 0);
+    std::vector<double> e_g(2 * n_pad, 0.0);
+    for (int e = 0; e < ne; ++e) { inc_ptr[L.n1[e] + 1]++; inc_ptr[L.n2[e] + 1]++; }
+    for (int v = 0; v < nn; ++v) inc_ptr[v + 1] += inc_ptr[v];
+    {
+        std::vector<int> pos(inc_ptr.begin(), inc_ptr.end() - 1);
+        for (int e = 0; e < ne; ++e) {
+            const double inv = 1.0 / L.elen[e];
+            const int a = L.n1[e], b = L.n2[e];
+            int q = pos[a]++;
+            inc_edge[q] = iperm[e]; inc_other[q] = b; inc_gv[q] = -inv; inc_gw[q] = +inv;
+            q = pos[b]++;
+            inc_edge[q] = iperm[e]; inc_other[q] = a; inc_gv[q] = +inv; inc_gw[q] = -inv;
+            if (flags_ref[e] & kFlagDcBc) { node_bc[a] = 1; node_bc[b] = 1; }
+            const int r = iperm[e];
+            if (a < b) { e_node[2 * r] = a; e_g[2 * r] = -inv; e_node[2 * r + 1] = b; e_g[2 * r + 1] = +inv; }
+            else { e_node[2 * r] = b; e_g[2 * r] = +inv; e_node[2 * r + 1] = a; e_g[2 * r + 1] = -inv; }
+        }
+    }
+    std::vector<int> cell_edge(L.cell_edge.size());
+    for (size_t q = 0; q < cell_edge.size(); ++q) cell_edge[q] = iperm[L.cell_edge[q]];
+
+    // upload
+    md.ne = ne; md.n_pad = n_pad; md.nc = L.nc; md.nn = nn; md.n_slices = n_slices;
+    md.perm = dupload(perm, stream); md.iperm = dupload(iperm, stream);
+    md.flags = dupload(flags, stream); md.dir = dupload(dir, stream); md.ez = dupload(ez, stream);
+    md.s_diag = dupload(sdiag, stream); md.me_geom = dupload(megeom, stream);
+    md.adual = dupload(adual, stream); md.elen = dupload(elen, stream); md.nadj = dupload(nadj, stream);
+    md.adj_ptr = dupload(adj_ptr, stream); md.adj_cell = dupload(adj_cell, stream);
+    md.lift_ptr = dupload(lift_ptr, stream); md.lift_col = dupload(lift_col, stream);
+    md.lift_val = dupload(lift_val, stream);
+    md.nhp = (int)L.hp.size(); md.hp = dupload(hp, stream);
+    md.inc_ptr = dupload(inc_ptr, stream); md.inc_edge = dupload(inc_edge, stream);
+    md.inc_other = dupload(inc_other, stream); md.inc_gv = dupload(inc_gv, stream);
+    md.inc_gw = dupload(inc_gw, stream); md.node_bc = dupload(node_bc, stream);
+    md.e_node = dupload(e_node, stream); md.e_g = dupload(e_g, stream);
+    md.cell_ptr = dupload(L.cell_ptr, stream); md.cell_edge = dupload(cell_edge, stream);
+    d_slice_off = dupload(slice_off, stream); d_slice_wl = dupload(slice_wl, stream);
+    d_slice_wu = dupload(slice_wu, stream); d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
+    {
+        std::vector<float> ev32(eval.begin(), eval.end());
+        d_val32 = dupload(ev32, stream);
+    }
+    // reduction scratch: enough blocks for two waves on every SM
+    int sms = 0;
+    cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "sm count");
+    red.max_blocks = std::max(2, 2 * sms);
+    red.max_blocks += red.max_blocks & 1;
+    red.partial = dalloc<double2>((size_t)red.max_blocks * dev::kMaxQ * dev::kMaxRhs);
+    red.final_ = dalloc<double2>(dev::kMaxQ * dev::kMaxRhs);
+    red.counter = dalloc<unsigned int>(1);
+    cuda_ok(cudaMemsetAsync(red.counter, 0, sizeof(unsigned int), stream), "memset");
+    d_sigma = dalloc<double>(L.nc);
+    d_Me = dalloc<double>(n_pad);
+    d_me_dc = dalloc<double>(n_pad);
+    d_host_stage = dalloc<double2>(std::max(ne, 1));
+    d_stage_real = dalloc<double>(std::max(ne, L.nc));
+    d_grad = dalloc<double>(L.nc);
+    d_states = dalloc<BicgState>(dev::kMaxRhs);
+    d_states2 = dalloc<BicgState>(dev::kMaxRhs);
+    sigma_h.assign(L.nc, 0.0);
+    sync();
+    ready = true;
+}
+
+void GpuSolver::set_sigma(const double* sigma, int n) {
+    if (n != L.nc) throw std::invalid_argument("sigma size != number of cells");
+    sigma_h.assign(sigma, sigma + n);
+    cuda_ok(cudaMemcpyAsync(d_sigma, sigma, sizeof(double) * n, cudaMemcpyHostToDevice, stream), "sigma");
+    phys::edge_mass(md, d_sigma, d_Me, d_me_dc, stream);
+    ++launches;
+    have_sigma = true;
+    lap_built = false;
+    if (stations_set) {
+        std::vector<double> sc(st_cell.size(), 0.0);
+        for (size_t s = 0; s < st_cell.size(); ++s) if (st_cell[s] >= 0) sc[s] = sigma_h[st_cell[s]];
+        cuda_ok(cudaMemcpyAsync(sd.sigma_cell, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, stream), "sc");
+    }
+    sync();
+}
+
+// find_stations_ (forward_solver_fv.cpp:1393-1485) on the leaf geometry
+void GpuSolver::set_stations(const double* xyz, int n) {
+    const double* dm = L.domain;
+    const double DX = dm[1] - dm[0], DY = dm[3] - dm[2], DZ = dm[5] - dm[4];
+    st_cell.assign(n, -1);
+    for (int si = 0; si < n; ++si) {
+        const double sx = xyz[3 * si], sy = xyz[3 * si + 1], sz = 0.0;
+        int best = -1, fb = -1;
+        double bcz = 1e30, fbd = 1e30;
+        for (int c = 0; c < L.nc; ++c) {
+            if (L.ctype[c] == 1) continue;
+            const double cx = L.ccx[c], cy = L.ccy[c], cz = L.ccz[c];
+            const double h = 1.0 / (1 << L.clevel[c]);
+            const double hdx = h * DX, hdy = h * DY;
+            const bool inx = (sx >= cx - hdx / 2 - 1.0) && (sx <= cx + hdx / 2 + 1.0);
+            const bool iny = (sy >= cy - hdy / 2 - 1.0) && (sy <= cy + hdy / 2 + 1.0);
+            if (inx && iny && cz < 0 && std::abs(cz) < bcz) { bcz = std::abs(cz); best = c; }
+            const double d = std::sqrt((cx - sx) * (cx - sx) + (cy - sy) * (cy - sy) + (cz - sz) * (cz - sz));
+            if (d < fbd) { fbd = d; fb = c; }
+        }
+        if (best < 0) best = fb;
+        st_cell[si] = best;
+    }
+    std::vector<double> geom(6 * (size_t)n, 0.0), sc(n, 0.0);
+    std::vector<int> eptr(n + 1, 0), erow;
+    std::vector<unsigned char> ecode;
+    for (int s = 0; s < n; ++s) {
+        const int c = st_cell[s];
+        if (c >= 0) {
+            const double h = 1.0 / (1 << L.clevel[c]);
+            const double cx = L.ccx[c], cy = L.ccy[c], cz = L.ccz[c];
+            geom[6 * s] = cx; geom[6 * s + 1] = cy; geom[6 * s + 2] = cz;
+            geom[6 * s + 3] = h * DX; geom[6 * s + 4] = h * DY; geom[6 * s + 5] = h * DZ;
+            sc[s] = have_sigma ? sigma_h[c] : 0.0;
+            for (int q = L.cell_ptr[c]; q < L.cell_ptr[c + 1]; ++q) {
+                const int e = L.cell_edge[q];
+                unsigned char code = (unsigned char)L.edir[e];
+                if (L.ez[e] > cz) code |= 4;
+                if (L.ex[e] > cx) code |= 8;
+                if (L.ey[e] > cy) code |= 16;
+                erow.push_back(iperm[e]);
+                ecode.push_back(code);
+            }
+        }
+        eptr[s + 1] = (int)erow.size();
+    }
+    dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
+    sd.ns = n;
+    sd.cell = dupload(st_cell, stream);
+    sd.geom = dupload(geom, stream);
+    sd.e_ptr = dupload(eptr, stream);
+    sd.e_row = dupload(erow, stream);
+    sd.e_code = dupload(ecode, stream);
+    sd.sigma_cell = dupload(sc, stream);
+    stations_set = true;
+    hc_cap = 0;
+    dfree(d_hc); dfree(d_Z); dfree(d_wr);
+    sync();
+}
+
+// ---------------------------------------------------------------------------
+// buffers
+// ---------------------------------------------------------------------------
+
+void GpuSolver::ensure_vecs(int K) {
+    if (kv_K >= K) return;
+    dfree(kv.x); dfree(kv.b); dfree(kv.r); dfree(kv.r0); dfree(kv.p); dfree(kv.v); dfree(kv.s); dfree(kv.t);
+    dfree(kv.ph); dfree(kv.sh); dfree(kv.y);
+    const size_t n = (size_t)n_pad * K;
+    kv.x = dalloc<double2>(n); kv.b = dalloc<double2>(n); kv.r = dalloc<double2>(n); kv.r0 = dalloc<double2>(n);
+    kv.p = dalloc<double2>(n); kv.v = dalloc<double2>(n); kv.s = dalloc<double2>(n); kv.t = dalloc<double2>(n);
+    kv.ph = dalloc<double2>(n); kv.sh = dalloc<double2>(n); kv.y = dalloc<double2>(n);
+    kv_K = K;
+}
+
+void GpuSolver::ensure_fields(int K) {
+    if (fwd_cap >= K) return;
+    dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
+    const size_t n = (size_t)n_pad * K;
+    d_E = dalloc<double2>(n); d_Epri = dalloc<double2>(n); d_Ebc = dalloc<double2>(n);
+    d_rhs = dalloc<double2>(n); d_tmp = dalloc<double2>(n); d_lam = dalloc<double2>(n); d_adj = dalloc<double2>(n);
+    fwd_cap = K;
+}
+
+void GpuSolver::ensure_dc(int K) {
+    if (!dc.lap_diag) {
+        dc.lap_diag = dalloc<double>(L.nn);
+        dc.jac_diag = dalloc<double>(L.nn);
+        dc.lap_off = dalloc<double>(2 * (size_t)L.ne);
+        dc.st = dalloc<phys::DcState>(dev::kMaxRhs);
+    }
+    if (dc_K >= K) return;
+    dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
+    const size_t n = (size_t)L.nn * K;
+    dc.divJ = dalloc<double2>(n); dc.phi = dalloc<double2>(n); dc.r = dalloc<double2>(n);
+    dc.z = dalloc<double2>(n); dc.p = dalloc<double2>(n); dc.Ap = dalloc<double2>(n); dc.phi0 = dalloc<double2>(n);
+    dc_K = K;
+}
+
+void GpuSolver::ensure_hc(int nf) {
+    if (hc_cap >= nf) return;
+    dfree(d_hc); dfree(d_Z); dfree(d_wr);
+    const size_t n = (size_t)std::max(1, sd.ns) * nf;
+    d_hc = dalloc<HCache>(n);
+    d_Z = dalloc<double2>(4 * n);
+    d_wr = dalloc<double2>(4 * n);
+    hc_cap = nf;
+}
+
+void GpuSolver::ensure_sigma_device() {
+    if (!have_sigma) throw std::logic_error("conductivity not set (m3d_set_sigma)");
+    if (P.div_correction && !lap_built) {
+        ensure_dc(2);
+        phys::dc_build_laplacian(md, d_me_dc, dc, stream);
+        ++launches;
+        lap_built = true;
+    }
+}
+
+KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
+    KrylovCtx<double> c;
+    c.A = EllView<double>{d_slice_off, d_slice_wl, d_slice_wu, d_col, d_val, n_slices};
+    c.D = DiagView<double>{d_diag, d_dinv, n_pad};
+    c.B.K = K;
+    for (int k = 0; k < dev::kMaxRhs; ++k) c.B.fmap[k] = (k < K) ? fmap[k] : 0;
+    c.colour_slices = colour_slices;
+    c.n_pad = n_pad;
+    c.grid_vec = red.max_blocks;
+    c.grid_spmv = red.max_blocks;
+    c.red = red;
+    c.stream = stream;
+    c.launches = const_cast<long long*>(&launches);
+    return c;
+}
+
+RhsInfo GpuSolver::rhs_info(int K, const std::vector<int>& f, const std::vector<int>& pol,
+                            const std::vector<double>& freqs) const {
+    RhsInfo info;
+    std::memset(&info, 0, sizeof(info));
+    info.K = K;
+    for (int k = 0; k < K; ++k) {
+        info.f[k] = f[k];
+        info.pol[k] = pol[k];
+        const double om = 2.0 * kPi * freqs[f[k]];
+        info.omega[k] = om;
+        const std::complex<double> ik = std::sqrt(std::complex<double>(0.0, om * kMu0 * P.sigma_bg));
+        info.ik[k] = make_double2(ik.real(), ik.imag());
+    }
+    return info;
+}
+
+// ---------------------------------------------------------------------------
+// factorisation (assembly of the per-frequency diagonals)
+// ---------------------------------------------------------------------------
+
+void GpuSolver::factorize(const std::vector<double>& freqs) {
+    ensure_sigma_device();
+    const int nf = (int)freqs.size();
+    if (diag_cap < nf) {
+        dfree(d_diag); dfree(d_dinv); dfree(d_diag32); dfree(d_dinv32); dfree(d_omegas);
+        d_diag = dalloc<double2>((size_t)n_pad * nf);
+        d_dinv = dalloc<double2>((size_t)n_pad * nf);
+        d_diag32 = dalloc<float2>((size_t)n_pad * nf);
+        d_dinv32 = dalloc<float2>((size_t)n_pad * nf);
+        d_omegas = dalloc<double>(nf);
+        diag_cap = nf;
+    }
+    std::vector<double> om(nf);
+    for (int f = 0; f < nf; ++f) om[f] = 2.0 * kPi * freqs[f];
+    cuda_ok(cudaMemcpyAsync(d_omegas, om.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, stream), "omegas");
+    phys::assemble_diag(md, d_Me, d_omegas, nf, d_diag, d_dinv, d_diag32, d_dinv32, stream);
+    ++launches;
+    fz_freqs = freqs;
+    current_omega = om.back();
+}
+
+// ---------------------------------------------------------------------------
+// batched BiCGStab (device-resident scalars, host polls every chunk)
+// ---------------------------------------------------------------------------
+
+BatchResult GpuSolver::solve_batch(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                                   double tol, int maxiter) {
+    ensure_vecs(K);
+    KrylovCtx<double> c = kctx(K, fmap);
+    KrylovVecs<double> v = kv;
+    v.b = b;
+    v.x = x;
+    BatchResult R;
+    R.K = K;
+    R.iters.assign(K, 0); R.status.assign(K, kInactive); R.res.assign(K, 0.0); R.true_res.assign(K, 0.0);
+    std::vector<BicgState> hs(K);
+    std::vector<int> run_set = active;
+    const int chunk = 10;
+    // pass 0 is the solve; passes 1.. restart from x (r = b - A x recomputed
+    // in FP64) for right-hand sides whose recursive residual met tol while
+    // the true residual did not.
+    const int passes = 1 + (P.true_residual_check ? std::max(0, P.max_refinements) : 0);
+    for (int pass = 0; pass < passes; ++pass) {
+        bool any = false;
+        for (int k = 0; k < K; ++k) any |= run_set[k] != 0;
+        if (!any) break;
+        for (int k = 0; k < K; ++k) {
+            std::memset(&hs[k], 0, sizeof(BicgState));
+            hs[k].tol = tol;
+            hs[k].maxiter = std::max(1, maxiter - R.iters[k]);
+            hs[k].status = run_set[k] ? kRunning : kInactive;
+        }
+        cuda_ok(cudaMemcpyAsync(d_states, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "states");
+        bicg_init(c, v, d_states);
+        int it = 0;
+        for (;;) {
+            cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
+            sync();
+            bool run = false;
+            for (int k = 0; k < K; ++k) run |= hs[k].status == kRunning;
+            if (!run || it >= maxiter) break;
+            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c, v, d_states);
+        }
+        for (int k = 0; k < K; ++k) {
+            if (!run_set[k]) continue;
+            R.iters[k] += hs[k].iter;
+            R.status[k] = hs[k].status;
+            R.res[k] = hs[k].res;
+        }
+        // FP64 true residual || b - A x || / || b || of every active rhs
+        for (int k = 0; k < K; ++k) {
+            std::memset(&hs[k], 0, sizeof(BicgState));
+            hs[k].status = active[k] ? kConverged : kInactive;
+        }
+        cuda_ok(cudaMemcpyAsync(d_states, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "states");
+        spmv(c, kSpmvTrueRes, x, kv.y, b, nullptr, d_states);
+        cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
+        sync();
+        for (int k = 0; k < K; ++k) {
+            if (active[k]) R.true_res[k] = hs[k].true_res;
+            const bool again = run_set[k] && R.status[k] == kConverged && R.true_res[k] > tol &&
+                               R.iters[k] < maxiter;
+            run_set[k] = again ? 1 : 0;
+            if (again && pass + 1 < passes) ++stats.refinements;
+        }
+    }
+    return R;
+}
+
+// ---------------------------------------------------------------------------
+// forward: solve_frequency (forward_solver_fv.cpp:84-531) for nf frequencies
+// ---------------------------------------------------------------------------
+
+void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
+    if (!stations_set) throw std::logic_error("stations not set (m3d_set_stations)");
+    const int nf = (int)freqs.size();
+    const int Kreal = 2 * nf;
+    if (Kreal > dev::kMaxRhs) throw std::invalid_argument("at most 8 frequencies per forward group");
+    const int K = pow2_at_least(Kreal);
+    const auto t0 = std::chrono::steady_clock::now();
+    factorize(freqs);
+    ensure_vecs(K);
+    ensure_fields(K);
+    ensure_hc(nf);
+    std::vector<int> fmap(K, 0), pol(K, -1), active(K, 0);
+    for (int k = 0; k < Kreal; ++k) { fmap[k] = k / 2; pol[k] = k % 2; active[k] = 1; }
+    const RhsInfo info = rhs_info(K, fmap, pol, freqs);
+    const KrylovCtx<double> c = kctx(K, fmap.data());
+    const VecK Ebc{d_Ebc, K}, Epri{d_Epri, K}, rhs{d_rhs, K}, tmp{d_tmp, K}, E{d_E, K}, X{kv.x, K};
+    phys::primary_field(md, Ebc, info, true, stream);
+    phys::lift_rhs(md, Ebc, rhs, stream);
+    phys::primary_field(md, Epri, info, false, stream);
+    spmv(c, kSpmvPlain, d_Epri, d_tmp, nullptr, nullptr, nullptr);
+    phys::vsub((long)n_pad * K, d_rhs, d_tmp, kv.b, stream);
+    cuda_ok(cudaMemsetAsync(kv.x, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    launches += 5;
+    BatchResult R = solve_batch(K, fmap.data(), kv.b, kv.x, active, P.bicgstab_tol, P.bicgstab_maxiter);
+    phys::interpolate_hanging(md, X, hp_sequential, stream);
+    phys::combine_total(md, Epri, X, Ebc, E, stream);
+    launches += 2;
+    if (P.div_correction) {
+        ensure_dc(K);
+        launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
+                                  red, stream, 25);
+    }
+    phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
+    ++launches;
+    if (Z_out)
+        cuda_ok(cudaMemcpyAsync(Z_out, d_Z, sizeof(double2) * 4 * (size_t)sd.ns * nf, cudaMemcpyDeviceToHost, stream), "Z");
+    sync();
+    E_K = K;
+    E_nf = nf;
+    stats.n_rhs = Kreal;
+    stats.total_iterations = 0;
+    for (int k = 0; k < Kreal && k < 64; ++k) {
+        stats.iterations[k] = R.iters[k];
+        stats.status[k] = R.status[k];
+        stats.true_residual[k] = R.true_res[k];
+        stats.total_iterations += R.iters[k];
+    }
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats.kernel_launches = launches;
+}
+
+void GpuSolver::compute_single_frequency(double freq, double* Z_out) {
+    run_forward(std::vector<double>{freq}, Z_out);
+}
+
+void GpuSolver::background_E(int pol, double* out) {
+    if (!d_E || E_nf < 1) throw std::logic_error("no forward solution");
+    const int k = 2 * (E_nf - 1) + pol;
+    phys::from_permuted(md, VecK{d_E, E_K}, k, d_host_stage, stream);
+    cuda_ok(cudaMemcpyAsync(out, d_host_stage, sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "E");
+    sync();
+}
+
+void GpuSolver::set_background(const double* E1, const double* E2) {
+    ensure_fields(2);
+    cuda_ok(cudaMemsetAsync(d_E, 0, sizeof(double2) * (size_t)n_pad * 2, stream), "memset");
+    for (int p = 0; p < 2; ++p) {
+        cuda_ok(cudaMemcpyAsync(d_host_stage, p == 0 ? E1 : E2, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "E");
+        phys::to_permuted(md, d_host_stage, 2, p, VecK{d_E, 2}, stream);
+    }
+    E_K = 2;
+    E_nf = 1;
+    sync();
+}
+
+void GpuSolver::build_adjoint_rhs(const double* wr, double* rhs1, double* rhs2) {
+    if (E_nf != 1 || !d_hc) throw std::logic_error("adjoint source needs a solved single frequency");
+    ensure_fields(2);
+    cuda_ok(cudaMemcpyAsync(d_wr, wr, sizeof(double2) * 4 * (size_t)sd.ns, cudaMemcpyHostToDevice, stream), "wr");
+    cuda_ok(cudaMemsetAsync(d_adj, 0, sizeof(double2) * (size_t)n_pad * 2, stream), "memset");
+    phys::adjoint_rhs(sd, md, d_wr, d_hc, d_omegas + (fz_freqs.size() - 1), 1, VecK{d_adj, 2}, stream);
+    for (int p = 0; p < 2; ++p) {
+        phys::from_permuted(md, VecK{d_adj, 2}, p, d_host_stage, stream);
+        cuda_ok(cudaMemcpyAsync(p == 0 ? rhs1 : rhs2, d_host_stage, sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "rhs");
+        sync();
+    }
+}
+
+// solve_with_divcorr_ (forward_solver_fv.cpp:778-888) / solve_system_ (:727-759)
+void GpuSolver::run_adjoint(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
+                            const std::vector<int>& active) {
+    const double tol = tol_override > 0 ? tol_override : P.bicgstab_tol;
+    const KrylovCtx<double> c = kctx(K, fmap);
+    cuda_ok(cudaMemsetAsync(x, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    stats.n_rhs = 0;
+    stats.total_iterations = 0;
+    std::vector<int> iters(K, 0), status(K, 0);
+    std::vector<double> tres(K, 0.0);
+    if (P.div_correction && current_omega > 0) {
+        ensure_dc(K);
+        phys::dc_phi0(md, VecK{rhs, K}, info, dc, stream);
+        ++launches;
+        launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
+                                  active.data(), red, stream, 25);
+        std::vector<int> done(K, 0);
+        std::vector<double> prev(K, 1e30);
+        for (int k = 0; k < K; ++k) done[k] = !active[k];
+        for (int outer = 0; outer < P.divcorr_outer_max; ++outer) {
+            std::vector<int> act(K, 0);
+            bool any = false;
+            for (int k = 0; k < K; ++k) { act[k] = !done[k]; any |= act[k] != 0; }
+            if (!any) break;
+            BatchResult R = solve_batch(K, fmap, rhs, x, act, tol, P.divcorr_iter_per_dc);
+            std::vector<int> dca(K, 0);
+            for (int k = 0; k < K; ++k) {
+                if (!act[k]) continue;
+                iters[k] += R.iters[k];
+                tres[k] = R.true_res[k];
+                status[k] = R.status[k];
+                if (R.res[k] > 1.0) {
+                    k_zero_col<<<(n_pad + 255) / 256, 256, 0, stream>>>(x, K, k, n_pad);
+                    ++launches;
+                    status[k] = M3D_SOLVE_DIVERGED;
+                    done[k] = 1;
+                } else if (R.status[k] == kConverged) {
+                    done[k] = 1;
+                } else {
+                    dca[k] = 1;
+                }
+            }
+            bool anyd = false;
+            for (int k = 0; k < K; ++k) anyd |= dca[k] != 0;
+            if (!anyd) break;
+            launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
+                                      dca.data(), red, stream, 25);
+            // true residual after the correction
+            std::vector<BicgState> hs(K);
+            for (int k = 0; k < K; ++k) {
+                std::memset(&hs[k], 0, sizeof(BicgState));
+                hs[k].status = dca[k] ? kConverged : kInactive;
+            }
+            BicgState* d_tr = d_states2;
+            cuda_ok(cudaMemcpyAsync(d_tr, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "st");
+            ensure_vecs(K);
+            spmv(c, kSpmvTrueRes, x, kv.y, rhs, nullptr, d_tr);
+            cuda_ok(cudaMemcpyAsync(hs.data(), d_tr, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "st");
+            sync();
+            for (int k = 0; k < K; ++k) {
+                if (!dca[k]) continue;
+                const double rel = hs[k].true_res;
+                tres[k] = rel;
+                if (rel < tol) { done[k] = 1; status[k] = M3D_SOLVE_CONVERGED; }
+                else if (outer > 0 && rel > 0.95 * prev[k]) { done[k] = 1; status[k] = M3D_SOLVE_STAGNATED; }
+                prev[k] = rel;
+            }
+        }
+    } else {
+        BatchResult R = solve_batch(K, fmap, rhs, x, active, tol, P.bicgstab_maxiter);
+        for (int k = 0; k < K; ++k) {
+            if (!active[k]) continue;
+            iters[k] = R.iters[k]; status[k] = R.status[k]; tres[k] = R.true_res[k];
+            if (R.status[k] != kConverged && R.res[k] > 1.0) {
+                k_zero_col<<<(n_pad + 255) / 256, 256, 0, stream>>>(x, K, k, n_pad);
+                ++launches;
+                status[k] = M3D_SOLVE_DIVERGED;
+            }
+        }
+    }
+    sync();
+    int nr = 0;
+    for (int k = 0; k < K; ++k) {
+        if (!active[k]) continue;
+        if (nr < 64) { stats.iterations[nr] = iters[k]; stats.status[nr] = status[k]; stats.true_residual[nr] = tres[k]; }
+        stats.total_iterations += iters[k];
+        ++nr;
+    }
+    stats.n_rhs = nr;
+    stats.kernel_launches = launches;
+}
+
+void GpuSolver::adjoint_solve(const double* rhs_h, double* out, bool perturbation) {
+    (void)perturbation;
+    if (fz_freqs.empty()) throw std::logic_error("no factorised frequency");
+    const auto t0 = std::chrono::steady_clock::now();
+    ensure_fields(2);
+    ensure_vecs(2);
+    const int K = 2;
+    // use the last factorised frequency (diag slot)
+    const int fslot = (int)fz_freqs.size() - 1;
+    std::vector<int> fmap(K, fslot), pol(K, -1), active{1, 0};
+    RhsInfo info = rhs_info(K, fmap, pol, fz_freqs);
+    cuda_ok(cudaMemsetAsync(d_adj, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    cuda_ok(cudaMemcpyAsync(d_host_stage, rhs_h, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "rhs");
+    phys::to_permuted(md, d_host_stage, K, 0, VecK{d_adj, K}, stream);
+    run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
+    phys::from_permuted(md, VecK{d_lam, K}, 0, d_host_stage, stream);
+    cuda_ok(cudaMemcpyAsync(out, d_host_stage, sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "lam");
+    sync();
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void GpuSolver::sensitivity(const double* E_h, const double* lam_h, double* g) {
+    ensure_fields(2);
+    cuda_ok(cudaMemsetAsync(d_tmp, 0, sizeof(double2) * (size_t)n_pad * 2, stream), "memset");
+    cuda_ok(cudaMemcpyAsync(d_host_stage, E_h, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "E");
+    phys::to_permuted(md, d_host_stage, 2, 0, VecK{d_tmp, 2}, stream);
+    cuda_ok(cudaMemcpyAsync(d_host_stage, lam_h, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "lam");
+    phys::to_permuted(md, d_host_stage, 2, 1, VecK{d_tmp, 2}, stream);
+    // lambda sits in column 1: view it through a shifted pointer with the same stride
+    cuda_ok(cudaMemsetAsync(d_grad, 0, sizeof(double) * L.nc, stream), "memset");
+    double om = current_omega;
+    cuda_ok(cudaMemcpyAsync(d_stage_real, &om, sizeof(double), cudaMemcpyHostToDevice, stream), "om");
+    phys::sensitivity(md, d_sigma, VecK{d_tmp, 2}, VecK{d_tmp + 1, 2}, d_stage_real, 1, 1, d_grad, stream);
+    cuda_ok(cudaMemcpyAsync(g, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "g");
+    sync();
+}
+
+void GpuSolver::perturbation_rhs(int pol, const double* dsig, double* out) {
+    if (E_nf < 1) throw std::logic_error("no background field");
+    ensure_fields(2);
+    cuda_ok(cudaMemcpyAsync(d_stage_real, dsig, sizeof(double) * L.nc, cudaMemcpyHostToDevice, stream), "dsig");
+    const int kE = 2 * (E_nf - 1) + (pol == 1 ? 0 : 1);
+    phys::perturbation_rhs(md, d_sigma, d_stage_real, VecK{d_E, E_K}, kE, current_omega, VecK{d_tmp, 2}, 0, stream);
+    phys::from_permuted(md, VecK{d_tmp, 2}, 0, d_host_stage, stream);
+    cuda_ok(cudaMemcpyAsync(out, d_host_stage, sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "out");
+    sync();
+}
+
+void GpuSolver::delta_impedance(const double* dE, int pol, double* dZ) {
+    if (E_nf != 1 || !d_hc) throw std::logic_error("delta impedance needs a solved single frequency");
+    ensure_fields(2);
+    cuda_ok(cudaMemsetAsync(d_tmp, 0, sizeof(double2) * (size_t)n_pad * 2, stream), "memset");
+    cuda_ok(cudaMemcpyAsync(d_host_stage, dE, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "dE");
+    phys::to_permuted(md, d_host_stage, 2, 0, VecK{d_tmp, 2}, stream);
+    phys::delta_impedance(sd, VecK{d_tmp, 2}, 0, d_hc, pol, d_wr, stream);
+    cuda_ok(cudaMemcpyAsync(dZ, d_wr, sizeof(double2) * 4 * (size_t)sd.ns, cudaMemcpyDeviceToHost, stream), "dZ");
+    sync();
+}
+
+void GpuSolver::release() {
+    fz_freqs.clear();
+    E_nf = 0;
+}
+
+// ---------------------------------------------------------------------------
+// batched entry points
+// ---------------------------------------------------------------------------
+
+void GpuSolver::forward_batch(const double* freqs, int nf, double* Z_out, double* E_out) {
+    if (nf < 1) throw std::invalid_argument("no frequencies");
+    const auto t0 = std::chrono::steady_clock::now();
+    long long it_total = 0;
+    for (int f0 = 0; f0 < nf; f0 += 8) {
+        const int g = std::min(8, nf - f0);
+        std::vector<double> fr(freqs + f0, freqs + f0 + g);
+        run_forward(fr, Z_out ? Z_out + (size_t)f0 * sd.ns * 8 : nullptr);
+        it_total += stats.total_iterations;
+        if (E_out) {
+            for (int k = 0; k < 2 * g; ++k) {
+                phys::from_permuted(md, VecK{d_E, E_K}, k, d_host_stage, stream);
+                cuda_ok(cudaMemcpyAsync(E_out + ((size_t)(f0 * 2 + k)) * L.ne * 2, d_host_stage,
+                                        sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "E");
+            }
+            sync();
+        }
+    }
+    stats.total_iterations = (int)it_total;
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,
+                               double* grad) {
+    if (nf < 1) throw std::invalid_argument("no frequencies");
+    const auto t0 = std::chrono::steady_clock::now();
+    const int ns = sd.ns;
+    if (obs_cap < nf) {
+        dfree(d_obs); dfree(d_err);
+        d_obs = dalloc<double2>((size_t)ns * nf * 4 + 1);
+        d_err = dalloc<double>((size_t)ns * nf * 4 + 1);
+        obs_cap = nf;
+    }
+    cuda_ok(cudaMemcpyAsync(d_obs, obs, sizeof(double2) * (size_t)ns * nf * 4, cudaMemcpyHostToDevice, stream), "obs");
+    cuda_ok(cudaMemcpyAsync(d_err, err, sizeof(double) * (size_t)ns * nf * 4, cudaMemcpyHostToDevice, stream), "err");
+    cuda_ok(cudaMemsetAsync(d_grad, 0, sizeof(double) * L.nc, stream), "memset");
+    long long it_total = 0;
+    for (int f0 = 0; f0 < nf; f0 += 8) {
+        const int g = std::min(8, nf - f0);
+        std::vector<double> fr(freqs + f0, freqs + f0 + g);
+        run_forward(fr, Z_out ? Z_out + (size_t)f0 * ns * 8 : nullptr);
+        it_total += stats.total_iterations;
+        const int K = E_K;
+        phys::weighted_residual(ns, g, nf, f0, d_obs, d_err, d_Z, d_wr, stream);
+        cuda_ok(cudaMemsetAsync(d_adj, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+        phys::adjoint_rhs(sd, md, d_wr, d_hc, d_omegas, g, VecK{d_adj, K}, stream);
+        launches += 2;
+        std::vector<int> fmap(K, 0), pol(K, -1), active(K, 0);
+        for (int k = 0; k < 2 * g; ++k) { fmap[k] = k / 2; active[k] = 1; }
+        RhsInfo info = rhs_info(K, fmap, pol, fr);
+        current_omega = 2.0 * kPi * fr[0];
+        run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
+        it_total += stats.total_iterations;
+        phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, g, 2, d_grad, stream);
+        ++launches;
+    }
+    cuda_ok(cudaMemcpyAsync(grad, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "grad");
+    sync();
+    stats.total_iterations = (int)it_total;
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats.kernel_launches = launches;
+}
+
+}  // namespace m3d

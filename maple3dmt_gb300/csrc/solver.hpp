@@ -1,0 +1,144 @@
+// GpuSolver: host orchestration of the GB300 forward + adjoint solve behind
+// the C ABI of include/m3d_gb300.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "m3d_gb300.h"
+#include "host/layout.hpp"
+#include "cuda/krylov.cuh"
+#include "cuda/physics.cuh"
+
+namespace m3d {
+
+struct BatchResult {
+    int K = 0;
+    std::vector<int> iters, status;
+    std::vector<double> res, true_res;
+};
+
+class GpuSolver {
+public:
+    explicit GpuSolver(int device);
+    ~GpuSolver();
+
+    int device;
+    std::string err;
+    m3d_params P;
+    bool ready = false;
+
+    // ---- setup ----
+    void setup(const m3d_leaves* leaves, const m3d_params* params);
+    void set_sigma(const double* sigma, int n);
+    void set_stations(const double* xyz, int n);
+
+    // ---- per-frequency interface (IForwardSolver) ----
+    void factorize(const std::vector<double>& freqs);
+    void compute_single_frequency(double freq, double* Z_out);
+    void background_E(int pol, double* out);
+    void set_background(const double* E1, const double* E2);
+    void build_adjoint_rhs(const double* wr, double* rhs1, double* rhs2);
+    void adjoint_solve(const double* rhs, double* lam, bool perturbation);
+    void sensitivity(const double* E, const double* lam, double* g);
+    void perturbation_rhs(int pol, const double* dsig, double* out);
+    void delta_impedance(const double* dE, int pol, double* dZ);
+    void release();
+
+    // ---- batched ----
+    void forward_batch(const double* freqs, int nf, double* Z_out, double* E_out);
+    void gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,
+                        double* grad);
+
+    m3d_stats stats{};
+    double tol_override = 0.0;
+    double current_omega = 0.0;
+
+    int n_edges() const { return L.ne; }
+    int n_cells() const { return L.nc; }
+    int n_nodes() const { return L.nn; }
+    int n_colours() const { return (int)colour_slices.size() - 1; }
+
+private:
+    HostLayout L;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+
+    // host-side structure
+    std::vector<int> perm, iperm, colour_slices;
+    std::vector<unsigned char> flags_ref;  // reference order
+    int n_pad = 0, n_slices = 0;
+    bool hp_sequential = false;
+
+    // device mesh
+    MeshDev md{};
+    int *d_slice_off = nullptr, *d_slice_wl = nullptr, *d_slice_wu = nullptr, *d_col = nullptr;
+    double* d_val = nullptr;
+    float* d_val32 = nullptr;
+
+    // sigma
+    std::vector<double> sigma_h;
+    double *d_sigma = nullptr, *d_Me = nullptr, *d_me_dc = nullptr;
+    bool have_sigma = false, lap_built = false;
+
+    // factorised frequencies (diagonals)
+    std::vector<double> fz_freqs;
+    int diag_cap = 0;
+    double2 *d_diag = nullptr, *d_dinv = nullptr;
+    float2 *d_diag32 = nullptr, *d_dinv32 = nullptr;
+    double* d_omegas = nullptr;
+
+    // reductions
+    dev::RedScratch red{};
+
+    // Krylov work vectors for batches of up to 16 right-hand sides
+    KrylovVecs<double> kv{};
+    int kv_K = 0;
+    // fields of the last forward solve: [n_pad][Kf], rhs 2f+p
+    double2* d_E = nullptr;
+    int E_K = 0, E_nf = 0;
+    double2 *d_Epri = nullptr, *d_Ebc = nullptr, *d_rhs = nullptr, *d_tmp = nullptr;
+    double2* d_lam = nullptr;     // adjoint solutions
+    double2* d_adj = nullptr;     // adjoint sources
+    int fwd_cap = 0;
+
+    // divergence correction
+    phys::DcWork dc{};
+    int dc_K = 0;
+
+    // stations
+    StationDev sd{};
+    std::vector<int> st_cell;
+    bool stations_set = false;
+    HCache* d_hc = nullptr;
+    double2 *d_Z = nullptr, *d_wr = nullptr, *d_obs = nullptr;
+    double* d_err = nullptr;
+    int hc_cap = 0, obs_cap = 0;
+    double* d_grad = nullptr;
+    double2* d_host_stage = nullptr;   // [ne] staging of host vectors
+    double* d_stage_real = nullptr;    // [max(nc, ne)]
+    BicgState* d_states = nullptr;     // [16] Krylov scalars of the running batch
+    BicgState* d_states2 = nullptr;    // [16] true-residual checks of the outer loop
+
+    // helpers
+    void free_all();
+    void upload_mesh();
+    void ensure_sigma_device();
+    void ensure_vecs(int K);
+    void ensure_fields(int K);
+    void ensure_dc(int K);
+    void ensure_hc(int nf);
+    KrylovCtx<double> kctx(int K, const int* fmap) const;
+    RhsInfo rhs_info(int K, const std::vector<int>& f, const std::vector<int>& pol,
+                     const std::vector<double>& freqs) const;
+    BatchResult solve_batch(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                            double tol, int maxiter);
+    void run_forward(const std::vector<double>& freqs, double* Z_out);
+    void run_adjoint(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
+                     const std::vector<int>& active);
+    void sync();
+};
+
+}  // namespace m3d

@@ -196,3 +196,53 @@ def small_survey(*, min_level=2, max_level=4, n_side=2, spacing=4000.0, freqs=(0
         return s
     sig = assign_sigma(lv, earth)
     return Survey("small", lv, sig, sigma0, st, fr, {})
+
+
+def leaves_struct(lv: Leaves):
+    """ctypes m3d_leaves over the arrays of `lv` (keep `lv` alive while it is used)."""
+    s = _abi.Leaves()
+    for i in range(6):
+        s.domain[i] = float(lv.domain[i])
+    s.min_level = int(lv.min_level)
+    s.max_level = int(lv.max_level)
+    s.n_cells = int(lv.n_cells)
+    for name in ("level", "cell_type"):
+        a = getattr(lv, name)
+        assert a.dtype == np.int32 and a.flags.c_contiguous
+        setattr(s, name, a.ctypes.data_as(_abi.c_int_p))
+    for name in ("cx", "cy", "cz"):
+        a = getattr(lv, name)
+        assert a.dtype == np.float64 and a.flags.c_contiguous
+        setattr(s, name, a.ctypes.data_as(_abi.c_double_p))
+    return s
+
+
+def host_layout(lv: Leaves, lib=None) -> dict:
+    """The solver's host layout (edges, stiffness S, hanging pairs) as numpy arrays."""
+    lib = lib or _loader.load()
+    st = leaves_struct(lv)
+    h = C.c_void_p()
+    rc = lib.m3d_layout_build(C.byref(st), C.byref(h))
+    if rc != 0:
+        raise RuntimeError(f"m3d_layout_build failed with code {rc}")
+    try:
+        ne, nf, nc, nn, nnz, nh = (C.c_int() for _ in range(6))
+        lib.m3d_layout_sizes(h, C.byref(ne), C.byref(nf), C.byref(nc), C.byref(nn), C.byref(nnz),
+                             C.byref(nh))
+        ne, nf, nc, nn, nnz, nh = (v.value for v in (ne, nf, nc, nn, nnz, nh))
+        xyz = np.zeros((ne, 3)); ln = np.zeros(ne); d = np.zeros(ne, np.int32)
+        ad = np.zeros(ne); dead = np.zeros(ne, np.int32)
+        n1 = np.zeros(ne, np.int32); n2 = np.zeros(ne, np.int32)
+        ip = lambda a: a.ctypes.data_as(_abi.c_int_p)  # noqa: E731
+        dp = lambda a: a.ctypes.data_as(_abi.c_double_p)  # noqa: E731
+        lib.m3d_layout_edges(h, dp(xyz), dp(ln), ip(d), dp(ad), ip(dead), ip(n1), ip(n2))
+        ptr = np.zeros(ne + 1, np.int32); idx = np.zeros(nnz, np.int32); val = np.zeros(nnz)
+        lib.m3d_layout_stiffness(h, ip(ptr), ip(idx), dp(val))
+        hp = np.zeros((nh, 3), np.int32)
+        if nh:
+            lib.m3d_layout_hanging(h, ip(hp))
+    finally:
+        lib.m3d_layout_destroy(h)
+    return dict(n_edges=ne, n_faces=nf, n_cells=nc, n_nodes=nn, xyz=xyz, length=ln, direction=d,
+                dual_area=ad, dead=dead, node1=n1, node2=n2, s_ptr=ptr, s_idx=idx, s_val=val,
+                hanging=hp)

@@ -1,0 +1,200 @@
+"""Python face of the GB300 solver, shaped like the reference's IForwardSolver.
+
+Method names follow maple3dmt::forward::IForwardSolver
+(include/maple3dmt/forward/iforward_solver.h:31-115) and ForwardSolverFV
+(include/maple3dmt/forward/forward_solver_fv.h:77-187); each call goes
+straight through the C ABI of include/m3d_gb300.h to the CUDA path.  There is
+no CPU fallback: without a CUDA device, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _loader, mesh
+from ._abi import c_double_p, c_int_p
+from ._abi_solver import Params, Stats
+
+ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "OOM", 5: "NO_DEVICE", 6: "TOO_LARGE", 7: "NUMERIC"}
+
+
+class SolverError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"M3D_ERR_{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def default_params(**overrides) -> Params:
+    lib = _loader.load()
+    p = Params()
+    lib.m3d_params_default(C.byref(p))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def _c(a):
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    return a, a.ctypes.data_as(c_double_p)
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(c_double_p)
+
+
+class ForwardSolverFV:
+    """GPU forward + adjoint octree-FV solver (one CUDA device)."""
+
+    def __init__(self, device: int = 0, lib=None):
+        self.lib = lib or _loader.load()
+        h = C.c_void_p()
+        rc = self.lib.m3d_solver_create(int(device), C.byref(h))
+        if rc != 0:
+            raise SolverError(rc, "m3d_solver_create failed")
+        self.h = h
+        self.ne = self.nc = self.nn = self.n_colours = 0
+        self.ns = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.m3d_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise SolverError(rc, self.lib.m3d_last_error(self.h).decode(errors="replace"))
+
+    # -- setup ------------------------------------------------------------
+    def setup(self, leaves: mesh.Leaves, params: Params | None = None, **kw):
+        p = params or default_params(**kw)
+        self._leaves = leaves
+        st = mesh.leaves_struct(leaves)
+        self._ck(self.lib.m3d_solver_setup(self.h, C.byref(st), C.byref(p)))
+        ne, nc, nn, ncol = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.lib.m3d_solver_sizes(self.h, C.byref(ne), C.byref(nc), C.byref(nn), C.byref(ncol)))
+        self.ne, self.nc, self.nn, self.n_colours = ne.value, nc.value, nn.value, ncol.value
+        return self
+
+    def set_sigma(self, sigma):
+        s, p = _d(sigma)
+        self._ck(self.lib.m3d_set_sigma(self.h, p, int(s.shape[0])))
+
+    def set_stations(self, xyz):
+        a, p = _d(np.asarray(xyz).reshape(-1, 3))
+        self.ns = a.shape[0]
+        self._ck(self.lib.m3d_set_stations(self.h, p, self.ns))
+
+    def set_solver_tolerance_override(self, tol):
+        self._ck(self.lib.m3d_set_tolerance_override(self.h, float(tol)))
+
+    def current_omega(self) -> float:
+        o = C.c_double()
+        self._ck(self.lib.m3d_current_omega(self.h, C.byref(o)))
+        return o.value
+
+    # -- per frequency ----------------------------------------------------
+    def compute_single_frequency(self, freq):
+        Z = np.zeros((self.ns, 4), np.complex128)
+        self._ck(self.lib.m3d_compute_single_frequency(self.h, float(freq), Z.ctypes.data_as(c_double_p)))
+        return Z
+
+    def factorize_frequency(self, freq):
+        self._ck(self.lib.m3d_factorize_frequency(self.h, float(freq)))
+
+    def release_factorization(self):
+        self._ck(self.lib.m3d_release_factorization(self.h))
+
+    def background_E(self, pol):
+        E = np.zeros(self.ne, np.complex128)
+        self._ck(self.lib.m3d_background_E(self.h, int(pol), E.ctypes.data_as(c_double_p)))
+        return E
+
+    def set_background_fields_complex(self, E1, E2):
+        a, pa = _c(E1)
+        b, pb = _c(E2)
+        self._ck(self.lib.m3d_set_background_fields(self.h, pa, pb))
+
+    def build_adjoint_rhs_from_residual(self, wr):
+        w, pw = _c(np.asarray(wr).reshape(self.ns, 4))
+        r1 = np.zeros(self.ne, np.complex128)
+        r2 = np.zeros(self.ne, np.complex128)
+        self._ck(self.lib.m3d_build_adjoint_rhs(self.h, pw, r1.ctypes.data_as(c_double_p),
+                                                r2.ctypes.data_as(c_double_p)))
+        return r1, r2
+
+    def adjoint_solve_complex(self, rhs):
+        r, pr = _c(rhs)
+        lam = np.zeros(self.ne, np.complex128)
+        self._ck(self.lib.m3d_adjoint_solve(self.h, pr, lam.ctypes.data_as(c_double_p)))
+        return lam
+
+    def solve_rhs_complex(self, rhs):
+        r, pr = _c(rhs)
+        x = np.zeros(self.ne, np.complex128)
+        self._ck(self.lib.m3d_solve_rhs(self.h, pr, x.ctypes.data_as(c_double_p)))
+        return x
+
+    def compute_sensitivity_complex(self, E, lam):
+        e, pe = _c(E)
+        l, pl = _c(lam)
+        g = np.zeros(self.nc)
+        self._ck(self.lib.m3d_compute_sensitivity(self.h, pe, pl, g.ctypes.data_as(c_double_p)))
+        return g
+
+    def build_perturbation_rhs_complex(self, pol, delta_sigma):
+        d, pd = _d(delta_sigma)
+        out = np.zeros(self.ne, np.complex128)
+        self._ck(self.lib.m3d_build_perturbation_rhs(self.h, int(pol), pd, out.ctypes.data_as(c_double_p)))
+        return out
+
+    def extract_delta_impedance_complex(self, dE, pol):
+        e, pe = _c(dE)
+        dZ = np.zeros((self.ns, 4), np.complex128)
+        self._ck(self.lib.m3d_extract_delta_impedance(self.h, pe, int(pol), dZ.ctypes.data_as(c_double_p)))
+        return dZ
+
+    # -- batched ----------------------------------------------------------
+    def forward_batch(self, freqs, with_fields=False):
+        f, pf = _d(freqs)
+        Z = np.zeros((f.shape[0], self.ns, 4), np.complex128)
+        E = np.zeros((f.shape[0], 2, self.ne), np.complex128) if with_fields else None
+        self._ck(self.lib.m3d_forward_batch(self.h, pf, int(f.shape[0]), Z.ctypes.data_as(c_double_p),
+                                            E.ctypes.data_as(c_double_p) if with_fields else None))
+        return (Z, E) if with_fields else Z
+
+    def gradient_batch(self, freqs, obs_Z, obs_err):
+        f, pf = _d(freqs)
+        oz, poz = _c(obs_Z)
+        oe, poe = _d(obs_err)
+        Z = np.zeros((f.shape[0], self.ns, 4), np.complex128)
+        g = np.zeros(self.nc)
+        self._ck(self.lib.m3d_gradient_batch(self.h, pf, int(f.shape[0]), poz, poe,
+                                             Z.ctypes.data_as(c_double_p), g.ctypes.data_as(c_double_p)))
+        return Z, g
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._ck(self.lib.m3d_get_stats(self.h, C.byref(s)))
+        n = min(s.n_rhs, 64)
+        return dict(n_rhs=s.n_rhs, iterations=list(s.iterations[:n]), status=list(s.status[:n]),
+                    true_residual=list(s.true_residual[:n]), total_iterations=s.total_iterations,
+                    refinements=s.refinements, seconds=s.seconds, kernel_launches=s.kernel_launches)
+
+
+def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:
+    s = ForwardSolverFV(device)
+    params.setdefault("sigma_bg", sv.sigma_bg)
+    s.setup(sv.leaves, **params)
+    s.set_sigma(sv.sigma)
+    s.set_stations(sv.stations)
+    return s
