@@ -106,6 +106,9 @@ typedef struct m3d_params {
     int true_residual_check;  /* 1: confirm ||b - A x|| / ||b|| <= tol in FP64 and refine until met */
     int max_refinements;      /* FP64 refinement steps allowed on top of the Krylov solve */
     int print_level;
+    int forward_interleaved;  /* 0: forward as the reference (full BiCGStab, then divergence
+                                 correction, forward_solver_fv.cpp:346-367); 1: forward solved
+                                 with interleaved divergence correction like the adjoint (:778-888) */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -186,6 +189,27 @@ int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const do
                        const double* obs_err, double* Z_out, double* grad);
 
 int m3d_get_stats(const m3d_solver* s, m3d_stats* out);
+
+/* ---------------------------------------------------------------------- */
+/* Measurement (no counterpart in the reference, which times with wall     */
+/* clocks in its drivers): CUDA events on the solver's own stream.         */
+/* ---------------------------------------------------------------------- */
+
+/* Record a start / stop event; stop synchronises and returns elapsed ms. */
+int m3d_timer_start(m3d_solver* s);
+int m3d_timer_stop(m3d_solver* s, double* ms);
+
+/* Kernel classes: 0 SpMV, 1 SSOR apply (all colour sweeps), 2 Krylov vector
+ * updates, 3 divergence correction, 4 other.  bytes = algorithmic bytes
+ * (matrix entries, diagonals and vector streams each counted once). */
+typedef struct m3d_kernel_times {
+    long long launches[5];
+    double ms[5];
+    double bytes[5];
+} m3d_kernel_times;
+
+int m3d_set_kernel_timing(m3d_solver* s, int on);   /* also resets the totals */
+int m3d_get_kernel_times(m3d_solver* s, m3d_kernel_times* out);
 
 #ifdef __cplusplus
 }

@@ -23,6 +23,7 @@ class Params(C.Structure):
         ("true_residual_check", C.c_int),
         ("max_refinements", C.c_int),
         ("print_level", C.c_int),
+        ("forward_interleaved", C.c_int),
     ]
 
 
@@ -40,6 +41,17 @@ class Stats(C.Structure):
     ]
 
 
+class KernelTimes(C.Structure):
+    """struct m3d_kernel_times."""
+    _fields_ = [
+        ("launches", C.c_longlong * 5),
+        ("ms", C.c_double * 5),
+        ("bytes", C.c_double * 5),
+    ]
+
+
+KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "other")
+
 SOLVER_SYMBOLS = [
     "m3d_params_default", "m3d_solver_create", "m3d_solver_destroy", "m3d_last_error",
     "m3d_solver_setup", "m3d_solver_sizes", "m3d_set_sigma", "m3d_set_stations",
@@ -48,6 +60,7 @@ SOLVER_SYMBOLS = [
     "m3d_set_background_fields", "m3d_build_adjoint_rhs", "m3d_adjoint_solve", "m3d_solve_rhs",
     "m3d_compute_sensitivity", "m3d_build_perturbation_rhs", "m3d_extract_delta_impedance",
     "m3d_forward_batch", "m3d_gradient_batch", "m3d_get_stats",
+    "m3d_timer_start", "m3d_timer_stop", "m3d_set_kernel_timing", "m3d_get_kernel_times",
 ]
 
 
@@ -78,3 +91,7 @@ def declare(lib) -> None:
     _fn(lib, "m3d_gradient_batch", C.c_int,
         [vp, c_double_p, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_get_stats", C.c_int, [vp, C.POINTER(Stats)])
+    _fn(lib, "m3d_timer_start", C.c_int, [vp])
+    _fn(lib, "m3d_timer_stop", C.c_int, [vp, c_double_p])
+    _fn(lib, "m3d_set_kernel_timing", C.c_int, [vp, C.c_int])
+    _fn(lib, "m3d_get_kernel_times", C.c_int, [vp, C.POINTER(KernelTimes)])

@@ -70,6 +70,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->true_residual_check = 1;
     p->max_refinements = 3;
     p->print_level = 0;
+    p->forward_interleaved = 0;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -225,4 +226,33 @@ extern "C" int m3d_get_stats(const m3d_solver* h, m3d_stats* out) {
     if (!h || !h->s || !out) return M3D_ERR_ARG;
     *out = h->s->stats;
     return M3D_OK;
+}
+
+extern "C" int m3d_timer_start(m3d_solver* h) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.timer_start(); });
+}
+
+extern "C" int m3d_timer_stop(m3d_solver* h, double* ms) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!ms) return fail(h, M3D_ERR_ARG, "null output");
+    return guarded(h, [&](m3d::GpuSolver& s) { *ms = s.timer_stop(); });
+}
+
+extern "C" int m3d_set_kernel_timing(m3d_solver* h, int on) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.timer.reset(); s.timer.on = on != 0; });
+}
+
+extern "C" int m3d_get_kernel_times(m3d_solver* h, m3d_kernel_times* out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!out) return fail(h, M3D_ERR_ARG, "null output");
+    return guarded(h, [&](m3d::GpuSolver& s) {
+        s.timer.collect();
+        for (int i = 0; i < 5; ++i) {
+            out->launches[i] = s.timer.launches[i];
+            out->ms[i] = s.timer.ms[i];
+            out->bytes[i] = s.timer.bytes[i];
+        }
+    });
 }

@@ -113,12 +113,79 @@ __device__ bool grid_reduce(const double2 (&acc)[KT][NQ], int rhs0, RedScratch r
     __syncthreads();
     if (!am_last) return false;
     __threadfence();
-    if (threadIdx.x < NQ * K) {
+    // Last block: for each of the NQ*K totals, thread t sums blocks t, t+256, ...
+    // then a fixed-shape tree over the 256 threads; deterministic and short.
+    __shared__ double2 red[kBlock];
+    for (int qk = 0; qk < NQ * K; ++qk) {
         double2 s = make_double2(0.0, 0.0);
-        for (int b = 0; b < (int)gridDim.x; ++b)
-            s = cadd(s, __ldcg(&rs.partial[(size_t)b * (NQ * K) + threadIdx.x]));
-        out[threadIdx.x] = s;
-        rs.final_[threadIdx.x] = s;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+            s = cadd(s, __ldcg(&rs.partial[(size_t)b * (NQ * K) + qk]));
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + w]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            out[qk] = red[0];
+            rs.final_[qk] = red[0];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *rs.counter = 0u;
+    __syncthreads();
+    return true;
+}
+
+// Grid reduction for kernels whose lane l always works on right-hand side
+// l % K (K a power of two <= 32, blockDim a multiple of 32): a shuffle tree
+// over the lanes that share a right-hand side, warps combined in warp order,
+// blocks in block order by the last block to arrive (each of the NQ*K totals
+// summed by a fixed set of threads, then in a fixed order).  Deterministic
+// for a fixed launch shape.  Returns true in the last block, where
+// out[q * K + k] (shared, NQ*K entries) holds the totals.
+template <int NQ, int K>
+__device__ bool grid_reduce_lanes(double2 (&acc)[NQ], RedScratch rs, double2* out) {
+    static_assert(K >= 1 && K <= 32 && (K & (K - 1)) == 0, "K must be a power of two <= 32");
+    constexpr int PK = NQ * K;
+    __shared__ double2 sm[kWarpsPerBlock][PK];
+    __shared__ double2 chunk[kBlock];
+    __shared__ bool am_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= K; off >>= 1)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = cadd(acc[q], shfl_xor(acc[q], off));
+    if (lane < K)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) sm[warp][q * K + lane] = acc[q];
+    __syncthreads();
+    if (threadIdx.x < PK) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < kWarpsPerBlock; ++w) s = cadd(s, sm[w][threadIdx.x]);
+        __stcg(&rs.partial[(size_t)blockIdx.x * PK + threadIdx.x], s);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned t = atomicAdd(rs.counter, 1u);
+        am_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!am_last) return false;
+    __threadfence();
+    constexpr int CH = kBlock / PK > 0 ? kBlock / PK : 1;   // threads per total
+    const int p = threadIdx.x % PK, j = threadIdx.x / PK;
+    double2 s = make_double2(0.0, 0.0);
+    if (j < CH)
+        for (int b = j; b < (int)gridDim.x; b += CH) s = cadd(s, __ldcg(&rs.partial[(size_t)b * PK + p]));
+    chunk[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < PK) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int jj = 0; jj < CH; ++jj) t = cadd(t, chunk[jj * PK + threadIdx.x]);
+        out[threadIdx.x] = t;
+        rs.final_[threadIdx.x] = t;
     }
     if (threadIdx.x == 0) *rs.counter = 0u;
     __syncthreads();

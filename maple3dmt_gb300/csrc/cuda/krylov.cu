@@ -7,12 +7,61 @@ namespace m3d {
 
 using namespace dev;
 
+cudaEvent_t KernelTimer::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) throw std::runtime_error("cudaEventCreate failed");
+    return e;
+}
+
+int KernelTimer::begin(int cls, double algorithmic_bytes) {
+    if (!on) return -1;
+    Pair p{cls, get(), get(), algorithmic_bytes};
+    cudaEventRecord(p.a, stream);
+    open.push_back(p);
+    return (int)open.size() - 1;
+}
+
+void KernelTimer::end(int h) {
+    if (h < 0) return;
+    cudaEventRecord(open[h].b, stream);
+}
+
+void KernelTimer::collect() {
+    if (open.empty()) return;
+    cudaStreamSynchronize(stream);
+    for (const Pair& p : open) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+            ms[p.cls] += t;
+            bytes[p.cls] += p.bytes;
+            launches[p.cls] += 1;
+        }
+        pool.push_back(p.a);
+        pool.push_back(p.b);
+    }
+    open.clear();
+    cudaGetLastError();
+}
+
+void KernelTimer::reset() {
+    collect();
+    for (int i = 0; i < kNumCls; ++i) { launches[i] = 0; ms[i] = 0; bytes[i] = 0; }
+}
+
+KernelTimer::~KernelTimer() {
+    for (auto& p : open) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+}
+
 namespace {
 
-// Right-hand sides handled by one thread in the SpMV / SSOR kernels: the
-// gathers of x[col][rhs0 .. rhs0+KT) are 32 contiguous bytes or more.
-template <class R, int K> struct KtOf { static constexpr int v = (K < 2 ? K : 2); };
-template <int K> struct KtOf<float, K> { static constexpr int v = (K < 4 ? K : 4); };
+// Rows per warp when lane l works on rhs l % K.
+template <int K> struct Rpw { static constexpr int v = 32 / K; };
 
 // ---------------------------------------------------------------------------
 // Scalar recurrences of BiCGStabSolver::solve (src/forward/bicgstab.cpp),
@@ -94,95 +143,102 @@ __device__ void ep_trueres(BicgState& S, const double2* out, int k, int K) {
     if (S.status == kInactive) return;
     double bn = sqrt(out[1 * K + k].x);
     if (bn < 1e-30) bn = 1.0;
-    S.true_res = sqrt(out[0 * K + k].x) / bn;
+    S.rnorm = sqrt(out[0 * K + k].x);
+    S.bnorm = bn;
+    S.true_res = S.rnorm / bn;
 }
 
 // ---------------------------------------------------------------------------
-// Sliced-ELL SpMV with fused reductions.  Warp task = (slice, subgroup g);
-// lane = row within the slice; the thread handles right-hand sides
-// g*KT .. g*KT+KT-1.  The warp stride of the grid is a multiple of G, so a
-// warp keeps the same subgroup across its tasks.
+// Row products: entries [k0, k1) of one row against one right-hand side
+// (this lane's), unrolled four deep so four independent gathers are in
+// flight per lane; the K lanes of the row read the same entry (broadcast)
+// and neighbouring complex values of the same vector row (coalesced).
+// ---------------------------------------------------------------------------
+template <class R, int K>
+__device__ __forceinline__ cplx<R> row_dot(const OpView<R>& A, int k0, int k1, const cplx<R>* v, int rhs) {
+    using C = cplx<R>;
+    C s = cm<R>(0, 0);
+    int k = k0;
+    for (; k + 4 <= k1; k += 4) {
+        int c[4];
+        R a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { c[u] = __ldg(&A.col[k + u]); a[u] = __ldg(&A.val[k + u]); }
+        C xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xv[u] = v[(size_t)c[u] * K + rhs];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a[u] * xv[u].x; s.y += a[u] * xv[u].y; }
+    }
+    for (; k < k1; ++k) {
+        const int c = __ldg(&A.col[k]);
+        const R a = __ldg(&A.val[k]);
+        const C xv = v[(size_t)c * K + rhs];
+        s.x += a * xv.x;
+        s.y += a * xv.y;
+    }
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// SpMV y = A x with fused reductions; warp task = Rpw<K> consecutive rows.
 // ---------------------------------------------------------------------------
 template <class R, int K, int MODE>
-__global__ void __launch_bounds__(kBlock) k_spmv(EllView<R> A, DiagView<R> D, BatchView B,
+__global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, BatchView B,
                                                  const cplx<R>* __restrict__ x, cplx<R>* __restrict__ y,
                                                  const cplx<R>* __restrict__ aux,
                                                  cplx<R>* __restrict__ aux_out, BicgState* st,
                                                  RedScratch rs) {
     using C = cplx<R>;
-    constexpr int KT = KtOf<R, K>::v;
-    constexpr int G = K / KT;
+    constexpr int RPW = Rpw<K>::v;
     constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kSpmvAs || MODE == kSpmvTrueRes) ? 2 : 3;
     constexpr bool REDUCE = MODE != kSpmvPlain;
     const int lane = threadIdx.x & 31;
+    const int rhs = lane % K, sub = lane / K;
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
-    const int g = (int)(wg % G);
-    const int rhs0 = g * KT;
-    double2 acc[KT][NQ];
+    const int f = B.fmap[rhs];
+    double2 acc[NQ];
 #pragma unroll
-    for (int kt = 0; kt < KT; ++kt)
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) acc[kt][q] = make_double2(0.0, 0.0);
-
-    const long tasks = (long)A.n_slices * G;
-    for (long t = wg; t < tasks; t += W) {
-        const int s = (int)(t / G);
-        const int row = s * kSlice + lane;
-        const int off = A.slice_off[s];
-        const int w = A.slice_wl[s] + A.slice_wu[s];
-        C sum[KT];
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
-        for (int k = 0; k < w; ++k) {
-            const int c = __ldg(&A.col[off + k * kSlice + lane]);
-            const R v = __ldg(&A.val[off + k * kSlice + lane]);
-            const C* xp = x + (size_t)c * K + rhs0;
-#pragma unroll
-            for (int kt = 0; kt < KT; ++kt) {
-                const C xv = xp[kt];
-                sum[kt].x += v * xv.x;
-                sum[kt].y += v * xv.y;
-            }
-        }
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const int rhs = rhs0 + kt;
-            const size_t i = (size_t)row * K + rhs;
-            const C d = D.d[(size_t)B.fmap[rhs] * D.n_pad + row];
-            const C yv = cadd(sum[kt], cmul(d, x[i]));
-            if (MODE == kSpmvPlain) {
-                y[i] = yv;
-            } else if (MODE == kSpmvAp) {
-                y[i] = yv;
-                acc[kt][0] = cadd(acc[kt][0], cjmul(to_d(aux[i]), to_d(yv)));
-            } else if (MODE == kSpmvAs) {
-                y[i] = yv;
-                const double2 tv = to_d(yv);
-                acc[kt][0].x += tv.x * tv.x + tv.y * tv.y;
-                acc[kt][1] = cadd(acc[kt][1], cjmul(tv, to_d(aux[i])));
-            } else if (MODE == kSpmvInit) {
-                const C bv = aux[i];
-                const C rv = csub(bv, yv);
-                y[i] = rv;
-                aux_out[i] = rv;
-                const double2 bd = to_d(bv), rd = to_d(rv);
-                acc[kt][0].x += bd.x * bd.x + bd.y * bd.y;
-                acc[kt][1].x += rd.x * rd.x + rd.y * rd.y;
-                acc[kt][2] = cadd(acc[kt][2], cjmul(rd, rd));
-            } else {  // kSpmvTrueRes
-                const C bv = aux[i];
-                const C rv = csub(bv, yv);
-                y[i] = rv;
-                const double2 bd = to_d(bv), rd = to_d(rv);
-                acc[kt][0].x += rd.x * rd.x + rd.y * rd.y;
-                acc[kt][1].x += bd.x * bd.x + bd.y * bd.y;
-            }
+    for (int q = 0; q < NQ; ++q) acc[q] = make_double2(0.0, 0.0);
+    const long groups = A.n_pad / RPW;
+    for (long t = wg; t < groups; t += W) {
+        const int row = (int)(t * RPW) + sub;
+        const C s = row_dot<R, K>(A, A.rp[row], A.rp[row + 1], x, rhs);
+        const size_t i = (size_t)row * K + rhs;
+        const C d = D.d[(size_t)row * D.nf + f];
+        const C yv = cadd(s, cmul(d, x[i]));
+        if (MODE == kSpmvPlain) {
+            y[i] = yv;
+        } else if (MODE == kSpmvAp) {
+            y[i] = yv;
+            acc[0] = cadd(acc[0], cjmul(to_d(aux[i]), to_d(yv)));
+        } else if (MODE == kSpmvAs) {
+            y[i] = yv;
+            const double2 tv = to_d(yv);
+            acc[0].x += tv.x * tv.x + tv.y * tv.y;
+            acc[1] = cadd(acc[1], cjmul(tv, to_d(aux[i])));
+        } else if (MODE == kSpmvInit) {
+            const C bv = aux[i];
+            const C rv = csub(bv, yv);
+            y[i] = rv;
+            aux_out[i] = rv;
+            const double2 bd = to_d(bv), rd = to_d(rv);
+            acc[0].x += bd.x * bd.x + bd.y * bd.y;
+            acc[1].x += rd.x * rd.x + rd.y * rd.y;
+            acc[2] = cadd(acc[2], cjmul(rd, rd));
+        } else {  // kSpmvTrueRes
+            const C bv = aux[i];
+            const C rv = csub(bv, yv);
+            y[i] = rv;
+            const double2 bd = to_d(bv), rd = to_d(rv);
+            acc[0].x += rd.x * rd.x + rd.y * rd.y;
+            acc[1].x += bd.x * bd.x + bd.y * bd.y;
         }
     }
     if (!REDUCE) return;
     __shared__ double2 out[NQ * K];
-    if (grid_reduce<NQ, K, KT>(acc, rhs0, rs, out)) {
+    if (grid_reduce_lanes<NQ, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             BicgState S = st[threadIdx.x];
             if (MODE == kSpmvAp) ep_r0v(S, out, threadIdx.x, K);
@@ -194,89 +250,50 @@ __global__ void __launch_bounds__(kBlock) k_spmv(EllView<R> A, DiagView<R> D, Ba
     }
 }
 
-// SSOR forward sweep over the slices of one colour:
+// SSOR forward sweep over the 32-row slices of one colour (list[0..count)):
 //   y_i = (in_i - sum_{j in earlier colours} a_ij y_j) / d_i      (ssor.h:58-66)
+// Gathered rows belong to other colours, which this launch does not write.
 template <class R, int K>
-__global__ void __launch_bounds__(kBlock) k_ssor_fwd(EllView<R> A, DiagView<R> D, BatchView B,
-                                                     int s_begin, int s_end,
+__global__ void __launch_bounds__(kBlock) k_ssor_fwd(OpView<R> A, DiagView<R> D, BatchView B,
+                                                     const int* __restrict__ list, int count,
                                                      const cplx<R>* __restrict__ in, cplx<R>* y) {
     using C = cplx<R>;
-    constexpr int KT = KtOf<R, K>::v;
-    constexpr int G = K / KT;
+    constexpr int RPW = Rpw<K>::v;
+    constexpr int GPS = kSlice / RPW;   // row groups per slice
     const int lane = threadIdx.x & 31;
+    const int rhs = lane % K, sub = lane / K;
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
-    const long tasks = (long)(s_end - s_begin) * G;
+    const long tasks = (long)count * GPS;
+    const int f = B.fmap[rhs];
     for (long t = wg; t < tasks; t += W) {
-        const int s = s_begin + (int)(t / G);
-        const int rhs0 = (int)(t % G) * KT;
-        const int row = s * kSlice + lane;
-        const int off = A.slice_off[s];
-        const int wl = A.slice_wl[s];
-        C sum[KT];
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
-        for (int k = 0; k < wl; ++k) {
-            const int c = __ldg(&A.col[off + k * kSlice + lane]);
-            const R v = __ldg(&A.val[off + k * kSlice + lane]);
-            const C* yp = y + (size_t)c * K + rhs0;
-#pragma unroll
-            for (int kt = 0; kt < KT; ++kt) {
-                const C yv = yp[kt];
-                sum[kt].x += v * yv.x;
-                sum[kt].y += v * yv.y;
-            }
-        }
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const int rhs = rhs0 + kt;
-            const size_t i = (size_t)row * K + rhs;
-            const C di = D.dinv[(size_t)B.fmap[rhs] * D.n_pad + row];
-            y[i] = cmul(csub(in[i], sum[kt]), di);
-        }
+        const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
+        const C s = row_dot<R, K>(A, A.rp[row], A.rs[row], y, rhs);
+        const size_t i = (size_t)row * K + rhs;
+        y[i] = cmul(csub(in[i], s), D.dinv[(size_t)row * D.nf + f]);
     }
 }
 
 // SSOR backward sweep over the slices of one colour:
 //   out_i = y_i - (sum_{j in later colours} a_ij out_j) / d_i      (ssor.h:69-78)
 template <class R, int K>
-__global__ void __launch_bounds__(kBlock) k_ssor_bwd(EllView<R> A, DiagView<R> D, BatchView B,
-                                                     int s_begin, int s_end,
+__global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D, BatchView B,
+                                                     const int* __restrict__ list, int count,
                                                      const cplx<R>* __restrict__ y, cplx<R>* out) {
     using C = cplx<R>;
-    constexpr int KT = KtOf<R, K>::v;
-    constexpr int G = K / KT;
+    constexpr int RPW = Rpw<K>::v;
+    constexpr int GPS = kSlice / RPW;
     const int lane = threadIdx.x & 31;
+    const int rhs = lane % K, sub = lane / K;
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
-    const long tasks = (long)(s_end - s_begin) * G;
+    const long tasks = (long)count * GPS;
+    const int f = B.fmap[rhs];
     for (long t = wg; t < tasks; t += W) {
-        const int s = s_begin + (int)(t / G);
-        const int rhs0 = (int)(t % G) * KT;
-        const int row = s * kSlice + lane;
-        const int off = A.slice_off[s];
-        const int wl = A.slice_wl[s], wu = A.slice_wu[s];
-        C sum[KT];
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) sum[kt] = cm<R>(0, 0);
-        for (int k = wl; k < wl + wu; ++k) {
-            const int c = __ldg(&A.col[off + k * kSlice + lane]);
-            const R v = __ldg(&A.val[off + k * kSlice + lane]);
-            const C* op = out + (size_t)c * K + rhs0;
-#pragma unroll
-            for (int kt = 0; kt < KT; ++kt) {
-                const C ov = op[kt];
-                sum[kt].x += v * ov.x;
-                sum[kt].y += v * ov.y;
-            }
-        }
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const int rhs = rhs0 + kt;
-            const size_t i = (size_t)row * K + rhs;
-            const C di = D.dinv[(size_t)B.fmap[rhs] * D.n_pad + row];
-            out[i] = csub(y[i], cmul(sum[kt], di));
-        }
+        const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
+        const C s = row_dot<R, K>(A, A.rs[row], A.rp[row + 1], out, rhs);
+        const size_t i = (size_t)row * K + rhs;
+        out[i] = csub(y[i], cmul(s, D.dinv[(size_t)row * D.nf + f]));
     }
 }
 
@@ -317,16 +334,16 @@ __global__ void __launch_bounds__(kBlock) k_update_s(long n, const cplx<R>* __re
     const BicgState S = st[rhs];
     const bool run = S.status == kRunning;
     const C al = from_d<C>(S.alpha);
-    double2 acc[1][1] = {{make_double2(0.0, 0.0)}};
+    double2 acc[1] = {make_double2(0.0, 0.0)};
     for (long i = i0; i < n; i += stride) {
         if (!run) { s[i] = cm<R>(0, 0); continue; }
         const C sv = csub(r[i], cmul(al, v[i]));
         s[i] = sv;
         const double2 d = to_d(sv);
-        acc[0][0].x += d.x * d.x + d.y * d.y;
+        acc[0].x += d.x * d.x + d.y * d.y;
     }
     __shared__ double2 out[K];
-    if (grid_reduce<1, K, 1>(acc, rhs, rs, out)) {
+    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             BicgState T = st[threadIdx.x];
             ep_s(T, out, threadIdx.x, K);
@@ -354,7 +371,7 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
     const bool run = S.status == kRunning;
     const bool pend = S.pend_x != 0;
     const C al = from_d<C>(S.alpha), om = from_d<C>(S.omega);
-    double2 acc[1][2] = {{make_double2(0.0, 0.0), make_double2(0.0, 0.0)}};
+    double2 acc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
     for (long i = i0; i < n; i += stride) {
         if (pend) { x[i] = cadd(x[i], cmul(al, ph[i])); continue; }
         if (!run) continue;
@@ -362,11 +379,11 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
         const C rv = csub(s[i], cmul(om, t[i]));
         r[i] = rv;
         const double2 d = to_d(rv);
-        acc[0][0].x += d.x * d.x + d.y * d.y;
-        acc[0][1] = cadd(acc[0][1], cjmul(to_d(r0[i]), d));
+        acc[0].x += d.x * d.x + d.y * d.y;
+        acc[1] = cadd(acc[1], cjmul(to_d(r0[i]), d));
     }
     __shared__ double2 out[2 * K];
-    if (grid_reduce<2, K, 1>(acc, rhs, rs, out)) {
+    if (grid_reduce_lanes<2, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             BicgState T = st[threadIdx.x];
             ep_xr(T, out, threadIdx.x, K);
@@ -388,17 +405,26 @@ inline int blocks_for(long work, int per_block, int cap) {
     return (int)b;
 }
 
+// Algorithmic bytes: matrix entries (value + column) once, the diagonals in
+// use, and each vector stream of the kernel once (gathers counted once).
+template <class R>
+double matrix_bytes(const KrylovCtx<R>& c) {
+    return (double)c.nnz * (sizeof(R) + 4) + (double)c.n_rows * c.n_freq * sizeof(cplx<R>);
+}
+
 template <class R, int K>
 void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
             cplx<R>* aux_out, BicgState* st) {
-    constexpr int G = K / KtOf<R, K>::v;
-    const long warps = (long)c.A.n_slices * G;
+    const long warps = (long)c.A.n_pad / Rpw<K>::v;
     int grid;
     if (mode == kSpmvPlain) {
         grid = blocks_for(warps, kWarpsPerBlock, 1 << 20);
     } else {
-        grid = c.grid_spmv;  // multiple of 2, so the warp stride is a multiple of G
+        grid = c.grid_spmv;
     }
+    const int streams = 2 + (aux ? 1 : 0) + (aux_out ? 1 : 0);
+    const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
+                                            (double)c.n_rows * K * sizeof(cplx<R>) * streams) : -1;
     switch (mode) {
         case kSpmvPlain:
             k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
@@ -417,42 +443,56 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
             break;
     }
     check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
 }
 
 template <class R, int K>
 void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
-    constexpr int G = K / KtOf<R, K>::v;
-    const int nc = (int)c.colour_slices.size() - 1;
+    constexpr int G = kSlice / Rpw<K>::v;   // row-group tasks per slice
+    const int nc = (int)c.colour_ptr.size() - 1;
+    // whole apply: matrix once (lower forward, upper backward), the inverse
+    // diagonal twice, vectors in, y (written, read back), out
+    const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) +
+                                            (double)c.n_rows * c.n_freq * sizeof(cplx<R>) +
+                                            (double)c.n_rows * K * sizeof(cplx<R>) * 4) : -1;
     for (int col = 0; col < nc; ++col) {
-        const int s0 = c.colour_slices[col], s1 = c.colour_slices[col + 1];
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
         const int grid = blocks_for((long)(s1 - s0) * G, kWarpsPerBlock, 1 << 20);
-        k_ssor_fwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, s0, s1, in, y);
+        k_ssor_fwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, c.colour_list + s0, s1 - s0, in, y);
         check_launch(c.launches);
     }
     for (int col = nc - 1; col >= 0; --col) {
-        const int s0 = c.colour_slices[col], s1 = c.colour_slices[col + 1];
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
         const int grid = blocks_for((long)(s1 - s0) * G, kWarpsPerBlock, 1 << 20);
-        k_ssor_bwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, s0, s1, y, out);
+        k_ssor_bwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, c.colour_list + s0, s1 - s0, y, out);
         check_launch(c.launches);
     }
+    if (c.timer) c.timer->end(th);
 }
 
 template <class R, int K>
 void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     const long n = (long)c.n_pad * K;
     const int gv = c.grid_vec;
+    const double vb = (double)c.n_rows * K * sizeof(cplx<R>);
+    int th = c.timer ? c.timer->begin(kClsVec, 4 * vb) : -1;
     k_update_p<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.p, v.v, st);
     check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.p, v.y, v.ph);
     spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
+    th = c.timer ? c.timer->begin(kClsVec, 3 * vb) : -1;
     k_update_s<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.s, v.y, v.sh);
     spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
+    th = c.timer ? c.timer->begin(kClsVec, 8 * vb) : -1;
     k_update_xr<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
     check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
 }
 
 }  // namespace

@@ -1,15 +1,19 @@
 // Batched multi-right-hand-side SSOR-preconditioned BiCGStab on the edge
-// system, and the sliced-ELL operator it runs on.
+// system, and the split-CSR operator it runs on.
 //
 // Restates BiCGStabSolver::solve (src/forward/bicgstab.cpp:15-166; Hermitian
 // dots include/maple3dmt/forward/bicgstab.h:68-73) and
 // SSORPreconditioner::apply (include/maple3dmt/forward/ssor.h:53-78, omega = 1)
 // for K right-hand sides at once.  Differences from the reference, by design:
 //  * Gauss-Seidel order is colour by colour (a graph colouring of A), so each
-//    sweep is K parallel launches instead of a serial loop; within a colour
-//    the original edge order is kept.  This is SSOR on the colour-permuted
-//    matrix, a different (equally valid) preconditioner, so iterates differ
-//    while converged solutions agree.
+//    sweep is one parallel launch per colour instead of a serial loop; within
+//    a colour the original edge order is kept.  This is SSOR on the colour-
+//    permuted matrix, a different (equally valid) preconditioner, so iterates
+//    differ while converged solutions agree.
+//  * Lanes run over right-hand sides: lane l of a warp works on rhs l % K of
+//    row (warp row base + l / K), so each neighbour gather of K complex values
+//    is one contiguous, coalesced segment and each matrix entry is a
+//    broadcast load shared by the K lanes of its row.
 //  * A's off-diagonal part is real and shared by every frequency; each right-
 //    hand side r carries its own complex diagonal d_f(r) (frequency f(r)).
 //  * Scalars (rho, alpha, omega, norms) stay on the device; every reduction is
@@ -37,23 +41,24 @@ struct BicgState {
 
 enum : int { kRunning = 0, kConverged = 1, kBreakdown = 2, kMaxIter = 3, kInactive = 9 };
 
-// Sliced ELL storage of the off-diagonal part, rows in colour order, each row
-// holding its "lower" entries (earlier colours) then its "upper" entries.
+// Off-diagonal part in "split CSR": rows in the solver's permuted order, each
+// row holding its lower entries (columns in earlier colours) in
+// [rp[i], rs[i]) and its upper entries in [rs[i], rp[i+1]).
 template <class R>
-struct EllView {
-    const int* slice_off;
-    const int* slice_wl;
-    const int* slice_wu;
+struct OpView {
+    const int* rp;     // [n_pad + 1]
+    const int* rs;     // [n_pad]
     const int* col;
     const R* val;
-    int n_slices;
+    int n_pad;
 };
 
+// Complex diagonal of A and its inverse, [n_pad][nf] (frequency fastest).
 template <class R>
 struct DiagView {
-    const dev::cplx<R>* d;     // [n_freq][n_pad] diagonal of A
-    const dev::cplx<R>* dinv;  // [n_freq][n_pad] 1 / diagonal (ssor.h:37-44)
-    int n_pad;
+    const dev::cplx<R>* d;
+    const dev::cplx<R>* dinv;
+    int nf;
 };
 
 // Frequency index of each right-hand side of the batch.
@@ -62,19 +67,43 @@ struct BatchView {
     int fmap[dev::kMaxRhs];
 };
 
+// Optional CUDA-event timing of kernel classes on the solver's stream.
+enum KernelClass : int { kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsOther = 4, kNumCls = 5 };
+struct KernelTimer {
+    bool on = false;
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> pool;
+    struct Pair { int cls; cudaEvent_t a, b; double bytes; };
+    std::vector<Pair> open;
+    long long launches[kNumCls] = {0, 0, 0, 0, 0};
+    double ms[kNumCls] = {0, 0, 0, 0, 0};
+    double bytes[kNumCls] = {0, 0, 0, 0, 0};
+    cudaEvent_t get();
+    int begin(int cls, double algorithmic_bytes);   // returns handle or -1
+    void end(int handle);
+    void collect();   // synchronises and folds finished pairs into the totals
+    void reset();
+    ~KernelTimer();
+};
+
 // Everything one launch of the batched solver needs.
 template <class R>
 struct KrylovCtx {
-    EllView<R> A;
+    OpView<R> A;
     DiagView<R> D;
     BatchView B;
-    std::vector<int> colour_slices;  // [n_colours + 1] slice ranges per colour
+    std::vector<int> colour_ptr;     // [n_colours + 1] ranges of colour_list per colour
+    const int* colour_list;          // device: 32-row slice ids grouped by colour, memory order inside
     int n_pad;
     int grid_vec;     // blocks for vector kernels with reductions
     int grid_spmv;    // blocks for SpMV kernels with reductions
     dev::RedScratch red;
     cudaStream_t stream;
     long long* launches;   // host counter of kernel launches
+    KernelTimer* timer;    // may be null
+    long nnz;              // true off-diagonal entries (algorithmic bytes)
+    int n_rows;            // real edge rows
+    int n_freq;            // distinct diagonals in use
 };
 
 // Work vectors of one batched solve, each [n_pad][K] complex of type R.

@@ -69,7 +69,7 @@ __global__ void k_assemble_diag(MeshDev m, const double* __restrict__ Me, const 
                                 int nf, double2* d, double2* dinv, float2* d32, float2* dinv32) {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)m.n_pad * nf) return;
-    const int f = (int)(i / m.n_pad), row = (int)(i % m.n_pad);
+    const int row = (int)(i / nf), f = (int)(i % nf);   // layout [row][nf]
     double2 dv, di;
     if (m.flags[row] & (kFlagConstrained | kFlagPad)) {
         dv = make_double2(1.0, 0.0);

@@ -94,7 +94,7 @@ namespace phys {
 void edge_mass(const MeshDev& m, const double* sigma, double* Me, double* me_dc, cudaStream_t s);
 // A diagonal for each frequency: S_ii + i omega Me_i on free rows, 1 on
 // constrained / padding rows (operators.cpp:607-616, forward_solver_fv.cpp:224-234),
-// and its SSOR inverse (ssor.h:37-44). d/dinv: [nf][n_pad]; d32/dinv32 optional.
+// and its SSOR inverse (ssor.h:37-44). d/dinv: [n_pad][nf]; d32/dinv32 optional.
 void assemble_diag(const MeshDev& m, const double* Me, const double* omegas, int nf, double2* d,
                    double2* dinv, float2* d32, float2* dinv32, cudaStream_t s);
 // E_primary on edges of direction pol for each rhs (forward_solver_fv.cpp:121-136, :318-323);

@@ -52,6 +52,31 @@ __global__ void k_zero_col(double2* x, int K, int k, int n_pad) {
     if (r < n_pad) x[(size_t)r * K + k] = make_double2(0.0, 0.0);
 }
 
+// b32 = y64 / scale[k] (scale 0: column left at zero)
+__global__ void k_to_f32_scaled(const double2* __restrict__ y, float2* __restrict__ b,
+                                const double* __restrict__ scale, int K, long n) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double s = scale[i % K];
+    const double inv = s > 0.0 ? 1.0 / s : 0.0;
+    const double2 v = y[i];
+    b[i] = make_float2((float)(v.x * inv), (float)(v.y * inv));
+}
+
+// x64 += d32 * scale[k]
+__global__ void k_add_f32_scaled(double2* __restrict__ x, const float2* __restrict__ d,
+                                 const double* __restrict__ scale, int K, long n) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double s = scale[i % K];
+    if (s == 0.0) return;
+    const float2 v = d[i];
+    double2 xv = x[i];
+    xv.x += (double)v.x * s;
+    xv.y += (double)v.y * s;
+    x[i] = xv;
+}
+
 
 }  // namespace
 
@@ -60,7 +85,11 @@ GpuSolver::GpuSolver(int dev_) : device(dev_) {
     std::memset(&stats, 0, sizeof(stats));
 }
 
-GpuSolver::~GpuSolver() { free_all(); }
+GpuSolver::~GpuSolver() {
+    free_all();
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+}
 
 void GpuSolver::free_all() {
     if (stream) cudaStreamSynchronize(stream);
@@ -69,12 +98,16 @@ void GpuSolver::free_all() {
     dfree(md.lift_ptr); dfree(md.lift_col); dfree(md.lift_val); dfree(md.hp);
     dfree(md.inc_ptr); dfree(md.inc_edge); dfree(md.inc_other); dfree(md.inc_gv); dfree(md.inc_gw);
     dfree(md.node_bc); dfree(md.e_node); dfree(md.e_g); dfree(md.cell_ptr); dfree(md.cell_edge);
-    dfree(d_slice_off); dfree(d_slice_wl); dfree(d_slice_wu); dfree(d_col); dfree(d_val); dfree(d_val32);
+    dfree(d_op_rp); dfree(d_op_rs); dfree(d_col); dfree(d_val); dfree(d_val32);
+    dfree(d_colour_list);
     dfree(d_sigma); dfree(d_Me); dfree(d_me_dc);
     dfree(d_diag); dfree(d_dinv); dfree(d_diag32); dfree(d_dinv32); dfree(d_omegas);
     dfree(red.partial); dfree(red.final_); dfree(red.counter);
     dfree(kv.x); dfree(kv.b); dfree(kv.r); dfree(kv.r0); dfree(kv.p); dfree(kv.v); dfree(kv.s); dfree(kv.t);
     dfree(kv.ph); dfree(kv.sh); dfree(kv.y);
+    dfree(kv32.x); dfree(kv32.b); dfree(kv32.r); dfree(kv32.r0); dfree(kv32.p); dfree(kv32.v); dfree(kv32.s);
+    dfree(kv32.t); dfree(kv32.ph); dfree(kv32.sh); dfree(kv32.y); dfree(d_scale);
+    kv32_K = 0;
     dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
     dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_diag); dfree(dc.st);
@@ -97,6 +130,8 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     if (params) P = *params;
     cuda_ok(cudaSetDevice(device), "cudaSetDevice");
     cuda_ok(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+    timer.stream = stream;
+    if (!ev_start) { cuda_ok(cudaEventCreate(&ev_start), "event"); cuda_ok(cudaEventCreate(&ev_stop), "event"); }
 
     LeafInput in;
     for (int i = 0; i < 6; ++i) in.domain[i] = lv->domain[i];
@@ -150,69 +185,67 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     // j < i, which is exactly the constraint set of sequential greedy.
     const int n_col = *std::max_element(colour.begin(), colour.end()) + 1;
 
-    // Permutation: colour-major, reference order inside a colour, each colour
-    // padded to whole slices.
+    // Permutation: the reference order (cell by cell along the Morton curve)
+    // is cut into blocks of kRowBlock edges; inside a block rows are grouped by
+    // colour (reference order kept within a group) and each group is padded to
+    // whole slices.  A row's neighbours then sit in the same block or the next
+    // one, so gathers stay inside a small, cache-resident window, while each
+    // SSOR colour sweep walks its slice list across all blocks.
+    constexpr int kRowBlock = 16384;
     perm.clear();
-    colour_slices.assign(1, 0);
+    std::vector<std::vector<int>> slices_of(n_col);
     {
         std::vector<std::vector<int>> byc(n_col);
-        for (int e = 0; e < ne; ++e) byc[colour[e]].push_back(e);
-        for (int c = 0; c < n_col; ++c) {
-            for (int e : byc[c]) perm.push_back(e);
-            while (perm.size() % dev::kSlice) perm.push_back(-1);
-            colour_slices.push_back((int)(perm.size() / dev::kSlice));
+        for (int b0 = 0; b0 < ne; b0 += kRowBlock) {
+            for (auto& v : byc) v.clear();
+            for (int e = b0; e < std::min(ne, b0 + kRowBlock); ++e) byc[colour[e]].push_back(e);
+            for (int c = 0; c < n_col; ++c) {
+                if (byc[c].empty()) continue;
+                const int s0 = (int)(perm.size() / dev::kSlice);
+                for (int e : byc[c]) perm.push_back(e);
+                while (perm.size() % dev::kSlice) perm.push_back(-1);
+                const int s1 = (int)(perm.size() / dev::kSlice);
+                for (int s = s0; s < s1; ++s) slices_of[c].push_back(s);
+            }
         }
+    }
+    colour_ptr.assign(1, 0);
+    colour_list.clear();
+    for (int c = 0; c < n_col; ++c) {
+        colour_list.insert(colour_list.end(), slices_of[c].begin(), slices_of[c].end());
+        colour_ptr.push_back((int)colour_list.size());
     }
     n_pad = (int)perm.size();
     n_slices = n_pad / dev::kSlice;
     iperm.assign(ne, -1);
     for (int r = 0; r < n_pad; ++r) if (perm[r] >= 0) iperm[perm[r]] = r;
 
-    // Sliced ELL of the free-free off-diagonal part; lower (earlier colour)
-    // entries first, then upper, each in reference column order.
-    std::vector<int> slice_off(n_slices), slice_wl(n_slices), slice_wu(n_slices);
-    std::vector<int> ecol;
+    // Split CSR of the free-free off-diagonal part in permuted row order:
+    // lower (earlier colour) entries, then upper, each in reference column order.
+    std::vector<int> op_rp(n_pad + 1, 0), op_rs(n_pad, 0), ecol;
     std::vector<double> eval;
     {
-        long total = 0;
-        std::vector<int> nl(dev::kSlice), nu(dev::kSlice);
-        for (int s = 0; s < n_slices; ++s) {
-            int wl = 0, wu = 0;
-            for (int l = 0; l < dev::kSlice; ++l) {
-                const int e = perm[s * dev::kSlice + l];
-                int a = 0, b = 0;
-                if (e >= 0 && free_row(e))
-                    for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
-                        const int j = L.s_idx[k];
-                        if (j == e || !free_row(j)) continue;
-                        if (colour[j] < colour[e]) ++a; else ++b;
-                    }
-                wl = std::max(wl, a); wu = std::max(wu, b);
-            }
-            slice_off[s] = (int)total;
-            slice_wl[s] = wl; slice_wu[s] = wu;
-            total += (long)(wl + wu) * dev::kSlice;
-            if (total > 2000000000L) throw std::runtime_error("mesh too large for 32-bit ELL offsets");
-        }
-        ecol.assign(total, 0);
-        eval.assign(total, 0.0);
-        for (int s = 0; s < n_slices; ++s) {
-            const int off = slice_off[s], wl = slice_wl[s], wu = slice_wu[s];
-            for (int l = 0; l < dev::kSlice; ++l) {
-                const int r = s * dev::kSlice + l;
-                const int e = perm[r];
-                int a = 0, b = 0;
-                for (int k = 0; k < wl + wu; ++k) { ecol[off + k * dev::kSlice + l] = r; eval[off + k * dev::kSlice + l] = 0.0; }
-                if (e < 0 || !free_row(e)) continue;
+        ecol.reserve((size_t)L.s_idx.size());
+        eval.reserve((size_t)L.s_idx.size());
+        std::vector<int> up_c;
+        std::vector<double> up_v;
+        for (int r = 0; r < n_pad; ++r) {
+            const int e = perm[r];
+            up_c.clear(); up_v.clear();
+            if (e >= 0 && free_row(e))
                 for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
                     const int j = L.s_idx[k];
                     if (j == e || !free_row(j)) continue;
-                    const int slot = (colour[j] < colour[e]) ? a++ : wl + b++;
-                    ecol[off + slot * dev::kSlice + l] = iperm[j];
-                    eval[off + slot * dev::kSlice + l] = L.s_val[k];
+                    if (colour[j] < colour[e]) { ecol.push_back(iperm[j]); eval.push_back(L.s_val[k]); }
+                    else { up_c.push_back(iperm[j]); up_v.push_back(L.s_val[k]); }
                 }
-            }
+            op_rs[r] = (int)ecol.size();
+            ecol.insert(ecol.end(), up_c.begin(), up_c.end());
+            eval.insert(eval.end(), up_v.begin(), up_v.end());
+            op_rp[r + 1] = (int)ecol.size();
+            if (ecol.size() > 2000000000UL) throw std::runtime_error("mesh too large for 32-bit row pointers");
         }
+        nnz_off = (long)ecol.size();
     }
 
     // Per permuted row data.
@@ -295,8 +328,9 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     md.inc_gw = dupload(inc_gw, stream); md.node_bc = dupload(node_bc, stream);
     md.e_node = dupload(e_node, stream); md.e_g = dupload(e_g, stream);
     md.cell_ptr = dupload(L.cell_ptr, stream); md.cell_edge = dupload(cell_edge, stream);
-    d_slice_off = dupload(slice_off, stream); d_slice_wl = dupload(slice_wl, stream);
-    d_slice_wu = dupload(slice_wu, stream); d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
+    d_op_rp = dupload(op_rp, stream); d_op_rs = dupload(op_rs, stream);
+    d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
+    d_colour_list = dupload(colour_list, stream);
     {
         std::vector<float> ev32(eval.begin(), eval.end());
         d_val32 = dupload(ev32, stream);
@@ -304,7 +338,7 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     // reduction scratch: enough blocks for two waves on every SM
     int sms = 0;
     cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "sm count");
-    red.max_blocks = std::max(2, 2 * sms);
+    red.max_blocks = std::max(2, 8 * sms);
     red.max_blocks += red.max_blocks & 1;
     red.partial = dalloc<double2>((size_t)red.max_blocks * dev::kMaxQ * dev::kMaxRhs);
     red.final_ = dalloc<double2>(dev::kMaxQ * dev::kMaxRhs);
@@ -460,17 +494,24 @@ void GpuSolver::ensure_sigma_device() {
 
 KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
     KrylovCtx<double> c;
-    c.A = EllView<double>{d_slice_off, d_slice_wl, d_slice_wu, d_col, d_val, n_slices};
-    c.D = DiagView<double>{d_diag, d_dinv, n_pad};
+    c.A = OpView<double>{d_op_rp, d_op_rs, d_col, d_val, n_pad};
+    c.D = DiagView<double>{d_diag, d_dinv, diag_nf};
     c.B.K = K;
     for (int k = 0; k < dev::kMaxRhs; ++k) c.B.fmap[k] = (k < K) ? fmap[k] : 0;
-    c.colour_slices = colour_slices;
+    c.colour_ptr = colour_ptr;
+    c.colour_list = d_colour_list;
     c.n_pad = n_pad;
     c.grid_vec = red.max_blocks;
-    c.grid_spmv = red.max_blocks;
+    c.grid_spmv = std::max(2, red.max_blocks / 2);
     c.red = red;
     c.stream = stream;
     c.launches = const_cast<long long*>(&launches);
+    c.timer = timer.on ? const_cast<KernelTimer*>(&timer) : nullptr;
+    c.nnz = nnz_off;
+    c.n_rows = L.ne;
+    std::vector<int> fs(fmap, fmap + K);
+    std::sort(fs.begin(), fs.end());
+    c.n_freq = (int)(std::unique(fs.begin(), fs.end()) - fs.begin());
     return c;
 }
 
@@ -510,6 +551,7 @@ void GpuSolver::factorize(const std::vector<double>& freqs) {
     for (int f = 0; f < nf; ++f) om[f] = 2.0 * kPi * freqs[f];
     cuda_ok(cudaMemcpyAsync(d_omegas, om.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, stream), "omegas");
     phys::assemble_diag(md, d_Me, d_omegas, nf, d_diag, d_dinv, d_diag32, d_dinv32, stream);
+    diag_nf = nf;
     ++launches;
     fz_freqs = freqs;
     current_omega = om.back();
@@ -580,7 +622,142 @@ BatchResult GpuSolver::solve_batch(int K, const int* fmap, double2* b, double2* 
             if (again && pass + 1 < passes) ++stats.refinements;
         }
     }
+    timer.collect();
     return R;
+}
+
+void GpuSolver::ensure_vecs32(int K) {
+    if (kv32_K >= K) return;
+    dfree(kv32.x); dfree(kv32.b); dfree(kv32.r); dfree(kv32.r0); dfree(kv32.p); dfree(kv32.v); dfree(kv32.s);
+    dfree(kv32.t); dfree(kv32.ph); dfree(kv32.sh); dfree(kv32.y);
+    const size_t n = (size_t)n_pad * K;
+    kv32.x = dalloc<float2>(n); kv32.b = dalloc<float2>(n); kv32.r = dalloc<float2>(n); kv32.r0 = dalloc<float2>(n);
+    kv32.p = dalloc<float2>(n); kv32.v = dalloc<float2>(n); kv32.s = dalloc<float2>(n); kv32.t = dalloc<float2>(n);
+    kv32.ph = dalloc<float2>(n); kv32.sh = dalloc<float2>(n); kv32.y = dalloc<float2>(n);
+    if (!d_scale) d_scale = dalloc<double>(dev::kMaxRhs);
+    kv32_K = K;
+}
+
+KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
+    const KrylovCtx<double> c = kctx(K, fmap);
+    KrylovCtx<float> f;
+    f.A = OpView<float>{d_op_rp, d_op_rs, d_col, d_val32, n_pad};
+    f.D = DiagView<float>{d_diag32, d_dinv32, diag_nf};
+    f.B = c.B;
+    f.colour_ptr = c.colour_ptr;
+    f.colour_list = c.colour_list;
+    f.n_pad = c.n_pad;
+    f.grid_vec = c.grid_vec;
+    f.grid_spmv = c.grid_spmv;
+    f.red = c.red;
+    f.stream = c.stream;
+    f.launches = c.launches;
+    f.timer = c.timer;
+    f.nnz = c.nnz;
+    f.n_rows = c.n_rows;
+    f.n_freq = c.n_freq;
+    return f;
+}
+
+BatchResult GpuSolver::solve_any(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                                 double tol, int maxiter) {
+    if (P.precision == 1) return solve_batch_mixed(K, fmap, b, x, active, tol, maxiter);
+    return solve_batch(K, fmap, b, x, active, tol, maxiter);
+}
+
+// Mixed precision: each step computes r = b - A x in FP64, solves A d = r
+// with the complex-FP32 batched BiCGStab (scaled to unit norm, relative
+// tolerance max(tol / ||r||_rel, 1e-5)), and adds d to x in FP64.  Steps repeat
+// until the FP64 true residual meets tol, the iteration budget is spent or a
+// step fails to reduce the residual by 10 %.
+BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, double2* x,
+                                         const std::vector<int>& active, double tol, int maxiter) {
+    ensure_vecs(K);
+    ensure_vecs32(K);
+    const KrylovCtx<double> c64 = kctx(K, fmap);
+    const KrylovCtx<float> c32 = kctx32(K, fmap);
+    KrylovVecs<float> v = kv32;
+    BatchResult R;
+    R.K = K;
+    R.iters.assign(K, 0); R.status.assign(K, kInactive); R.res.assign(K, 0.0); R.true_res.assign(K, 0.0);
+    std::vector<int> run = active;
+    std::vector<double> prev(K, 1e300), scale(K, 0.0);
+    std::vector<BicgState> hs(K);
+    const long n = (long)n_pad * K;
+    const int chunk = 10;
+    const int max_steps = 2 + std::max(0, P.max_refinements) * 4;
+    for (int step = 0; step <= max_steps; ++step) {
+        // FP64 true residual y = b - A x
+        for (int k = 0; k < K; ++k) {
+            std::memset(&hs[k], 0, sizeof(BicgState));
+            hs[k].status = active[k] ? kConverged : kInactive;
+        }
+        cuda_ok(cudaMemcpyAsync(d_states, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "states");
+        spmv(c64, kSpmvTrueRes, x, kv.y, b, nullptr, d_states);
+        cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
+        sync();
+        bool any = false;
+        for (int k = 0; k < K; ++k) {
+            if (!active[k]) continue;
+            const double rel = hs[k].true_res;
+            R.true_res[k] = rel;
+            R.res[k] = rel;
+            if (!run[k]) continue;
+            if (rel <= tol) { run[k] = 0; R.status[k] = kConverged; continue; }
+            if (!std::isfinite(rel) || rel > 0.9 * prev[k] || R.iters[k] >= maxiter || step == max_steps) {
+                run[k] = 0;
+                if (R.status[k] == kInactive || R.status[k] == kConverged) R.status[k] = kMaxIter;
+                continue;
+            }
+            prev[k] = rel;
+            scale[k] = hs[k].rnorm;
+            any = true;
+        }
+        if (!any) break;
+        std::vector<double> sc(K, 0.0);
+        for (int k = 0; k < K; ++k) sc[k] = run[k] ? scale[k] : 0.0;
+        cuda_ok(cudaMemcpyAsync(d_scale, sc.data(), sizeof(double) * K, cudaMemcpyHostToDevice, stream), "scale");
+        k_to_f32_scaled<<<(int)((n + 255) / 256), 256, 0, stream>>>(kv.y, kv32.b, d_scale, K, n);
+        cuda_ok(cudaMemsetAsync(kv32.x, 0, sizeof(float2) * (size_t)n, stream), "memset");
+        launches += 2;
+        for (int k = 0; k < K; ++k) {
+            std::memset(&hs[k], 0, sizeof(BicgState));
+            hs[k].tol = std::min(0.5, std::max(tol / R.true_res[k], 1e-5));
+            hs[k].maxiter = std::max(1, maxiter - R.iters[k]);
+            hs[k].status = run[k] ? kRunning : kInactive;
+        }
+        cuda_ok(cudaMemcpyAsync(d_states, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "states");
+        bicg_init(c32, v, d_states);
+        int it = 0;
+        for (;;) {
+            cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
+            sync();
+            bool r = false;
+            for (int k = 0; k < K; ++k) r |= hs[k].status == kRunning;
+            if (!r || it >= maxiter) break;
+            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c32, v, d_states);
+        }
+        for (int k = 0; k < K; ++k) {
+            if (!run[k]) continue;
+            R.iters[k] += hs[k].iter;
+            if (hs[k].status == kBreakdown) R.status[k] = kBreakdown;
+        }
+        k_add_f32_scaled<<<(int)((n + 255) / 256), 256, 0, stream>>>(x, kv32.x, d_scale, K, n);
+        ++launches;
+        if (step > 0) ++stats.refinements;
+    }
+    timer.collect();
+    return R;
+}
+
+void GpuSolver::timer_start() { cuda_ok(cudaEventRecord(ev_start, stream), "event"); }
+
+double GpuSolver::timer_stop() {
+    cuda_ok(cudaEventRecord(ev_stop, stream), "event");
+    cuda_ok(cudaEventSynchronize(ev_stop), "event");
+    float ms = 0.f;
+    cuda_ok(cudaEventElapsedTime(&ms, ev_start, ev_stop), "event");
+    return ms;
 }
 
 // ---------------------------------------------------------------------------
@@ -610,14 +787,26 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
     phys::vsub((long)n_pad * K, d_rhs, d_tmp, kv.b, stream);
     cuda_ok(cudaMemsetAsync(kv.x, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
     launches += 5;
-    BatchResult R = solve_batch(K, fmap.data(), kv.b, kv.x, active, P.bicgstab_tol, P.bicgstab_maxiter);
+    BatchResult R;
+    if (P.forward_interleaved && P.div_correction) {
+        // the forward system solved like the adjoint one (ModEM-style bursts
+        // with divergence correction, source divergence G^T rhs_sec / (i omega))
+        R.K = K;
+        R.iters.assign(K, 0); R.status.assign(K, 0); R.res.assign(K, 0.0); R.true_res.assign(K, 0.0);
+        solve_divcorr(K, fmap.data(), info, kv.b, kv.x, active, P.bicgstab_tol, R.iters, R.status, R.true_res);
+        for (int k = 0; k < K; ++k) if (R.status[k] == M3D_SOLVE_CONVERGED) R.status[k] = kConverged;
+    } else {
+        R = solve_any(K, fmap.data(), kv.b, kv.x, active, P.bicgstab_tol, P.bicgstab_maxiter);
+    }
     phys::interpolate_hanging(md, X, hp_sequential, stream);
     phys::combine_total(md, Epri, X, Ebc, E, stream);
     launches += 2;
     if (P.div_correction) {
         ensure_dc(K);
+        const int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
         launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
                                   red, stream, 25);
+        timer.end(th);
     }
     phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
     ++launches;
@@ -675,76 +864,91 @@ void GpuSolver::build_adjoint_rhs(const double* wr, double* rhs1, double* rhs2) 
     }
 }
 
-// solve_with_divcorr_ (forward_solver_fv.cpp:778-888) / solve_system_ (:727-759)
+// solve_with_divcorr_ (forward_solver_fv.cpp:778-888) for every active rhs:
+// initial correction with phi0 = G^T rhs / (i omega), then bursts of at most
+// divcorr_iter_per_dc BiCGStab iterations, each followed by a correction and
+// an FP64 true-residual test, with the reference's divergence (res > 1 ->
+// zero) and stagnation (> 0.95 of the previous residual) exits.
+void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
+                              const std::vector<int>& active, double tol, std::vector<int>& iters,
+                              std::vector<int>& status, std::vector<double>& tres) {
+    const KrylovCtx<double> c = kctx(K, fmap);
+    ensure_dc(K);
+    ensure_vecs(K);
+    phys::dc_phi0(md, VecK{rhs, K}, info, dc, stream);
+    ++launches;
+    int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
+    launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
+                              active.data(), red, stream, 25);
+    timer.end(th);
+    std::vector<int> done(K, 0);
+    std::vector<double> prev(K, 1e30);
+    for (int k = 0; k < K; ++k) done[k] = !active[k];
+    for (int outer = 0; outer < P.divcorr_outer_max; ++outer) {
+        std::vector<int> act(K, 0);
+        bool any = false;
+        for (int k = 0; k < K; ++k) { act[k] = !done[k]; any |= act[k] != 0; }
+        if (!any) break;
+        BatchResult R = solve_any(K, fmap, rhs, x, act, tol, P.divcorr_iter_per_dc);
+        std::vector<int> dca(K, 0);
+        for (int k = 0; k < K; ++k) {
+            if (!act[k]) continue;
+            iters[k] += R.iters[k];
+            tres[k] = R.true_res[k];
+            status[k] = R.status[k];
+            if (R.res[k] > 1.0) {
+                k_zero_col<<<(n_pad + 255) / 256, 256, 0, stream>>>(x, K, k, n_pad);
+                ++launches;
+                status[k] = M3D_SOLVE_DIVERGED;
+                done[k] = 1;
+            } else if (R.status[k] == kConverged) {
+                done[k] = 1;
+            } else {
+                dca[k] = 1;
+            }
+        }
+        bool anyd = false;
+        for (int k = 0; k < K; ++k) anyd |= dca[k] != 0;
+        if (!anyd) break;
+        th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
+        launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
+                                  dca.data(), red, stream, 25);
+        timer.end(th);
+        std::vector<BicgState> hs(K);
+        for (int k = 0; k < K; ++k) {
+            std::memset(&hs[k], 0, sizeof(BicgState));
+            hs[k].status = dca[k] ? kConverged : kInactive;
+        }
+        cuda_ok(cudaMemcpyAsync(d_states2, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "st");
+        spmv(c, kSpmvTrueRes, x, kv.y, rhs, nullptr, d_states2);
+        cuda_ok(cudaMemcpyAsync(hs.data(), d_states2, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "st");
+        sync();
+        for (int k = 0; k < K; ++k) {
+            if (!dca[k]) continue;
+            const double rel = hs[k].true_res;
+            tres[k] = rel;
+            if (rel < tol) { done[k] = 1; status[k] = M3D_SOLVE_CONVERGED; }
+            else if (outer > 0 && rel > 0.95 * prev[k]) { done[k] = 1; status[k] = M3D_SOLVE_STAGNATED; }
+            prev[k] = rel;
+        }
+    }
+    timer.collect();
+}
+
+// adjoint_solve / solve_rhs (forward_solver_fv.cpp:914-940): solve_with_divcorr_
+// when divergence correction is on, else solve_system_ (:727-759)
 void GpuSolver::run_adjoint(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
                             const std::vector<int>& active) {
     const double tol = tol_override > 0 ? tol_override : P.bicgstab_tol;
-    const KrylovCtx<double> c = kctx(K, fmap);
     cuda_ok(cudaMemsetAsync(x, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
     stats.n_rhs = 0;
     stats.total_iterations = 0;
     std::vector<int> iters(K, 0), status(K, 0);
     std::vector<double> tres(K, 0.0);
     if (P.div_correction && current_omega > 0) {
-        ensure_dc(K);
-        phys::dc_phi0(md, VecK{rhs, K}, info, dc, stream);
-        ++launches;
-        launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                                  active.data(), red, stream, 25);
-        std::vector<int> done(K, 0);
-        std::vector<double> prev(K, 1e30);
-        for (int k = 0; k < K; ++k) done[k] = !active[k];
-        for (int outer = 0; outer < P.divcorr_outer_max; ++outer) {
-            std::vector<int> act(K, 0);
-            bool any = false;
-            for (int k = 0; k < K; ++k) { act[k] = !done[k]; any |= act[k] != 0; }
-            if (!any) break;
-            BatchResult R = solve_batch(K, fmap, rhs, x, act, tol, P.divcorr_iter_per_dc);
-            std::vector<int> dca(K, 0);
-            for (int k = 0; k < K; ++k) {
-                if (!act[k]) continue;
-                iters[k] += R.iters[k];
-                tres[k] = R.true_res[k];
-                status[k] = R.status[k];
-                if (R.res[k] > 1.0) {
-                    k_zero_col<<<(n_pad + 255) / 256, 256, 0, stream>>>(x, K, k, n_pad);
-                    ++launches;
-                    status[k] = M3D_SOLVE_DIVERGED;
-                    done[k] = 1;
-                } else if (R.status[k] == kConverged) {
-                    done[k] = 1;
-                } else {
-                    dca[k] = 1;
-                }
-            }
-            bool anyd = false;
-            for (int k = 0; k < K; ++k) anyd |= dca[k] != 0;
-            if (!anyd) break;
-            launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                                      dca.data(), red, stream, 25);
-            // true residual after the correction
-            std::vector<BicgState> hs(K);
-            for (int k = 0; k < K; ++k) {
-                std::memset(&hs[k], 0, sizeof(BicgState));
-                hs[k].status = dca[k] ? kConverged : kInactive;
-            }
-            BicgState* d_tr = d_states2;
-            cuda_ok(cudaMemcpyAsync(d_tr, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "st");
-            ensure_vecs(K);
-            spmv(c, kSpmvTrueRes, x, kv.y, rhs, nullptr, d_tr);
-            cuda_ok(cudaMemcpyAsync(hs.data(), d_tr, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "st");
-            sync();
-            for (int k = 0; k < K; ++k) {
-                if (!dca[k]) continue;
-                const double rel = hs[k].true_res;
-                tres[k] = rel;
-                if (rel < tol) { done[k] = 1; status[k] = M3D_SOLVE_CONVERGED; }
-                else if (outer > 0 && rel > 0.95 * prev[k]) { done[k] = 1; status[k] = M3D_SOLVE_STAGNATED; }
-                prev[k] = rel;
-            }
-        }
+        solve_divcorr(K, fmap, info, rhs, x, active, tol, iters, status, tres);
     } else {
-        BatchResult R = solve_batch(K, fmap, rhs, x, active, tol, P.bicgstab_maxiter);
+        BatchResult R = solve_any(K, fmap, rhs, x, active, tol, P.bicgstab_maxiter);
         for (int k = 0; k < K; ++k) {
             if (!active[k]) continue;
             iters[k] = R.iters[k]; status[k] = R.status[k]; tres[k] = R.true_res[k];

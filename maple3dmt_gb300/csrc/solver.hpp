@@ -53,13 +53,17 @@ public:
                         double* grad);
 
     m3d_stats stats{};
+    KernelTimer timer;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    void timer_start();
+    double timer_stop();
     double tol_override = 0.0;
     double current_omega = 0.0;
 
     int n_edges() const { return L.ne; }
     int n_cells() const { return L.nc; }
     int n_nodes() const { return L.nn; }
-    int n_colours() const { return (int)colour_slices.size() - 1; }
+    int n_colours() const { return (int)colour_ptr.size() - 1; }
 
 private:
     HostLayout L;
@@ -67,14 +71,15 @@ private:
     long long launches = 0;
 
     // host-side structure
-    std::vector<int> perm, iperm, colour_slices;
+    std::vector<int> perm, iperm, colour_ptr, colour_list;
+    int* d_colour_list = nullptr;
     std::vector<unsigned char> flags_ref;  // reference order
     int n_pad = 0, n_slices = 0;
     bool hp_sequential = false;
 
     // device mesh
     MeshDev md{};
-    int *d_slice_off = nullptr, *d_slice_wl = nullptr, *d_slice_wu = nullptr, *d_col = nullptr;
+    int *d_op_rp = nullptr, *d_op_rs = nullptr, *d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
 
@@ -85,7 +90,7 @@ private:
 
     // factorised frequencies (diagonals)
     std::vector<double> fz_freqs;
-    int diag_cap = 0;
+    int diag_cap = 0, diag_nf = 1;
     double2 *d_diag = nullptr, *d_dinv = nullptr;
     float2 *d_diag32 = nullptr, *d_dinv32 = nullptr;
     double* d_omegas = nullptr;
@@ -96,6 +101,9 @@ private:
     // Krylov work vectors for batches of up to 16 right-hand sides
     KrylovVecs<double> kv{};
     int kv_K = 0;
+    KrylovVecs<float> kv32{};     // complex-FP32 inner solve of the mixed-precision path
+    int kv32_K = 0;
+    double* d_scale = nullptr;    // [16] per-rhs residual norms of the refinement step
     // fields of the last forward solve: [n_pad][Kf], rhs 2f+p
     double2* d_E = nullptr;
     int E_K = 0, E_nf = 0;
@@ -131,6 +139,14 @@ private:
     void ensure_dc(int K);
     void ensure_hc(int nf);
     KrylovCtx<double> kctx(int K, const int* fmap) const;
+    KrylovCtx<float> kctx32(int K, const int* fmap) const;
+    void ensure_vecs32(int K);
+    // FP32 BiCGStab on the residual equation inside FP64 refinement
+    BatchResult solve_batch_mixed(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                                  double tol, int maxiter);
+    // dispatch on P.precision
+    BatchResult solve_any(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                          double tol, int maxiter);
     RhsInfo rhs_info(int K, const std::vector<int>& f, const std::vector<int>& pol,
                      const std::vector<double>& freqs) const;
     BatchResult solve_batch(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
@@ -138,6 +154,12 @@ private:
     void run_forward(const std::vector<double>& freqs, double* Z_out);
     void run_adjoint(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
                      const std::vector<int>& active);
+    // solve_with_divcorr_ (forward_solver_fv.cpp:778-888) on a batch; fills
+    // per-rhs iterations / status / true residual
+    void solve_divcorr(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
+                       const std::vector<int>& active, double tol, std::vector<int>& iters,
+                       std::vector<int>& status, std::vector<double>& tres);
+    long nnz_off = 0;
     void sync();
 };
 

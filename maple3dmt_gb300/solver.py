@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _loader, mesh
 from ._abi import c_double_p, c_int_p
-from ._abi_solver import Params, Stats
+from ._abi_solver import KERNEL_CLASSES, KernelTimes, Params, Stats
 
 ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "OOM", 5: "NO_DEVICE", 6: "TOO_LARGE", 7: "NUMERIC"}
 
@@ -181,6 +181,23 @@ class ForwardSolverFV:
         self._ck(self.lib.m3d_gradient_batch(self.h, pf, int(f.shape[0]), poz, poe,
                                              Z.ctypes.data_as(c_double_p), g.ctypes.data_as(c_double_p)))
         return Z, g
+
+    def timer_start(self):
+        self._ck(self.lib.m3d_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        self._ck(self.lib.m3d_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def set_kernel_timing(self, on: bool):
+        self._ck(self.lib.m3d_set_kernel_timing(self.h, 1 if on else 0))
+
+    def kernel_times(self) -> dict:
+        t = KernelTimes()
+        self._ck(self.lib.m3d_get_kernel_times(self.h, C.byref(t)))
+        return {name: dict(launches=t.launches[i], ms=t.ms[i], bytes=t.bytes[i])
+                for i, name in enumerate(KERNEL_CLASSES)}
 
     def stats(self) -> dict:
         s = Stats()

@@ -195,6 +195,7 @@ def load_oracle():
             "m3d_oracle_get_matrix": (C.c_int, [vp, ip, ip, dp]),
             "m3d_oracle_get_edges": (C.c_int, [vp, dp, dp, ip, dp, ip, ip, ip]),
             "m3d_oracle_gradient": (C.c_int, [vp, dp, C.c_int, dp, dp, dp, dp]),
+            "m3d_oracle_time_iterations": (C.c_double, [vp, C.c_double, C.c_int, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -310,6 +311,12 @@ class Oracle:
         self.lib.m3d_oracle_get_edges(self.h, _p(xyz), _p(ln), _p(d, ip), _p(ad), _p(dead, ip),
                                       _p(n1, ip), _p(n2, ip))
         return dict(xyz=xyz, len=ln, dir=d, adual=ad, dead=dead, node1=n1, node2=n2)
+
+    def time_iterations(self, freq, n_iter):
+        """(seconds in n_iter reference BiCGStab+SSOR iterations, setup seconds)."""
+        setup = C.c_double()
+        t = self.lib.m3d_oracle_time_iterations(self.h, float(freq), int(n_iter), C.byref(setup))
+        return t, setup.value
 
     def gradient(self, freqs, obs_Z, obs_err):
         fr = np.ascontiguousarray(freqs, np.float64)

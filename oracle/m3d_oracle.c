@@ -1829,3 +1829,63 @@ int m3d_oracle_gradient(m3d_oracle* S, const double* freqs, int nf, const double
     free(Z); free(wr); free(a1); free(a2); free(l1); free(l2); free(g1); free(g2);
     return 0;
 }
+
+#include <time.h>
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* CPU-baseline sample: assemble frequency `freq` with the reference's BC
+ * elimination (solve_frequency :84-241), take the pol-1 scattered-field
+ * right-hand side and run exactly `n_iter` iterations of the reference's
+ * SSOR-BiCGStab (tolerance 0).  Returns seconds spent in the iterations and,
+ * through setup_s, seconds spent on assembly + BC elimination + SSOR setup. */
+double m3d_oracle_time_iterations(m3d_oracle* S, double freq, int n_iter, double* setup_s) {
+    const double t0 = now_s();
+    factorize(S, freq);
+    const int ne = S->ne;
+    const mesh_t* m = &S->m;
+    const double bt = cell_size_min(m, 0) * 0.1;
+    const cplx ik = csqrt(CMPLX(0.0, S->omega * M3D_MU0 * S->sigma_bg));
+    char* is_bc = (char*)xcalloc((size_t)ne, 1);
+    char* isc = (char*)xcalloc((size_t)ne, 1);
+    cplx* bc1 = (cplx*)xcalloc((size_t)ne, sizeof(cplx));
+    for (int e = 0; e < ne; ++e) {
+        double x = S->G.ex[e], y = S->G.ey[e], z = S->G.ez[e];
+        int onb = (x <= m->xmin + bt || x >= m->xmax - bt || y <= m->ymin + bt || y >= m->ymax - bt ||
+                   z <= m->zmin + bt || z >= m->zmax - bt);
+        if (onb || z > S->air_z) { is_bc[e] = 1; if (S->G.edir[e] == 0) bc1[e] = e_primary(ik, z); }
+    }
+    for (int h = 0; h < S->O.nhp; ++h) isc[S->O.hp[3 * h]] = 1;
+    for (int i = 0; i < ne; ++i) isc[i] = is_bc[i] || isc[i];
+    csrc_t* A = &S->A;
+    cplx* rhs = (cplx*)xcalloc((size_t)ne, sizeof(cplx));
+    for (int i = 0; i < ne; ++i)
+        for (int k = A->ptr[i]; k < A->ptr[i + 1]; ++k) {
+            int j = A->idx[k];
+            if (isc[i] || isc[j]) {
+                if (!isc[i] && is_bc[j]) rhs[i] -= A->val[k] * bc1[j];
+                if (isc[i]) A->val[k] = (j == i) ? (cplx)1.0 : (cplx)0.0;
+                else A->val[k] = 0;
+            }
+        }
+    for (int i = 0; i < ne; ++i) if (is_bc[i]) rhs[i] = bc1[i];
+    ssor_t M;
+    ssor_setup(&M, A);
+    cplx* Ep = (cplx*)xcalloc((size_t)ne, sizeof(cplx));
+    cplx* AEp = (cplx*)xcalloc((size_t)ne, sizeof(cplx));
+    for (int i = 0; i < ne; ++i) Ep[i] = (S->G.edir[i] == 0) ? e_primary(ik, S->G.ez[i]) : 0;
+    csrc_matvec(A, Ep, AEp);
+    for (int i = 0; i < ne; ++i) rhs[i] -= AEp[i];
+    cplx* x = (cplx*)xcalloc((size_t)ne, sizeof(cplx));
+    const double t1 = now_s();
+    bicgstab(A, &M, rhs, x, 0.0, n_iter);
+    const double t2 = now_s();
+    if (setup_s) *setup_s = t1 - t0;
+    ssor_free(&M);
+    free(is_bc); free(isc); free(bc1); free(rhs); free(Ep); free(AEp); free(x);
+    return t2 - t1;
+}

@@ -37,6 +37,9 @@ int m3d_oracle_get_edges(const m3d_oracle* S, double* xyz, double* len, int* dir
                          int* dead, int* node1, int* node2);
 int m3d_oracle_gradient(m3d_oracle* S, const double* freqs, int nf, const double* obs_Z,
                         const double* obs_err, double* Z_out, double* grad);
+/* CPU-baseline sample: seconds for exactly n_iter SSOR-BiCGStab iterations on
+ * the assembled, BC-eliminated system of `freq` (setup time in *setup_s). */
+double m3d_oracle_time_iterations(m3d_oracle* S, double freq, int n_iter, double* setup_s);
 
 #ifdef __cplusplus
 }
