@@ -258,6 +258,8 @@ def run_ours(args, rank, world, local_rank):
         e2e_s += time.perf_counter() - t0
         st = s.stats()
         iters.append(st["total_iterations"])
+        solver_stats = {k: st[k] for k in ("forward_iterations", "adjoint_iterations", "refinements",
+                                           "divcorr_calls", "divcorr_outer", "divcorr_cg_iterations")}
     launches = s.stats()["kernel_launches"] - launches0
     kt = s.kernel_times()
     s.set_kernel_timing(False)
@@ -305,6 +307,7 @@ def run_ours(args, rank, world, local_rank):
                                "GB/s": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None}
                            for k, v in kt.items()},
         "krylov_iterations_per_step": statistics.mean(iters),
+        "solver_stats_last_step": solver_stats,
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cb,

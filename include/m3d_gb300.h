@@ -123,6 +123,11 @@ typedef struct m3d_stats {
     int refinements;
     double seconds;
     long long kernel_launches;
+    int divcorr_calls;         /* divcorr_poisson_ calls (forward_solver_fv.cpp:623-722) */
+    int divcorr_outer;         /* Poisson rounds inside them */
+    long long divcorr_cg_iterations;  /* Jacobi-PCG iterations, summed over rhs */
+    long long forward_iterations;     /* Krylov iterations of the forward phase, summed over rhs */
+    long long adjoint_iterations;     /* ... of the adjoint phase */
 } m3d_stats;
 
 void m3d_params_default(m3d_params* p);

@@ -38,6 +38,11 @@ class Stats(C.Structure):
         ("refinements", C.c_int),
         ("seconds", C.c_double),
         ("kernel_launches", C.c_longlong),
+        ("divcorr_calls", C.c_int),
+        ("divcorr_outer", C.c_int),
+        ("divcorr_cg_iterations", C.c_longlong),
+        ("forward_iterations", C.c_longlong),
+        ("adjoint_iterations", C.c_longlong),
     ]
 
 

@@ -1,6 +1,7 @@
 // Batched SSOR-BiCGStab kernels.  See krylov.cuh for what they restate.
 #include "krylov.cuh"
 
+#include <algorithm>
 #include <stdexcept>
 
 namespace m3d {
@@ -62,6 +63,19 @@ namespace {
 
 // Rows per warp when lane l works on rhs l % K.
 template <int K> struct Rpw { static constexpr int v = 32 / K; };
+
+template <class R>
+__device__ __forceinline__ cplx<R> diag_of(const DiagView<R>& D, int row, R om) {
+    const cplx<R> a = D.sm[row];
+    return cm<R>(a.x, om * a.y);
+}
+// 1 / d: Smith's division in FP64 (as the assembly of the reference system),
+// conj(d) / |d|^2 in FP32
+__device__ __forceinline__ double2 inv_c(double2 d) { return cdiv(make_double2(1.0, 0.0), d); }
+__device__ __forceinline__ float2 inv_c(float2 d) {
+    const float n = d.x * d.x + d.y * d.y;
+    return make_float2(d.x / n, -d.y / n);
+}
 
 // ---------------------------------------------------------------------------
 // Scalar recurrences of BiCGStabSolver::solve (src/forward/bicgstab.cpp),
@@ -197,46 +211,46 @@ __global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, Bat
     const int rhs = lane % K, sub = lane / K;
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
-    const int f = B.fmap[rhs];
-    double2 acc[NQ];
+    const R om = (R)B.omega[rhs];
+    C accR[NQ];   // per-thread partial sums in the working precision
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) acc[q] = make_double2(0.0, 0.0);
+    for (int q = 0; q < NQ; ++q) accR[q] = cm<R>(0, 0);
     const long groups = A.n_pad / RPW;
     for (long t = wg; t < groups; t += W) {
         const int row = (int)(t * RPW) + sub;
         const C s = row_dot<R, K>(A, A.rp[row], A.rp[row + 1], x, rhs);
         const size_t i = (size_t)row * K + rhs;
-        const C d = D.d[(size_t)row * D.nf + f];
+        const C d = diag_of(D, row, om);
         const C yv = cadd(s, cmul(d, x[i]));
         if (MODE == kSpmvPlain) {
             y[i] = yv;
         } else if (MODE == kSpmvAp) {
             y[i] = yv;
-            acc[0] = cadd(acc[0], cjmul(to_d(aux[i]), to_d(yv)));
+            accR[0] = cadd(accR[0], cjmul(aux[i], yv));
         } else if (MODE == kSpmvAs) {
             y[i] = yv;
-            const double2 tv = to_d(yv);
-            acc[0].x += tv.x * tv.x + tv.y * tv.y;
-            acc[1] = cadd(acc[1], cjmul(tv, to_d(aux[i])));
+            accR[0].x += yv.x * yv.x + yv.y * yv.y;
+            accR[1] = cadd(accR[1], cjmul(yv, aux[i]));
         } else if (MODE == kSpmvInit) {
             const C bv = aux[i];
             const C rv = csub(bv, yv);
             y[i] = rv;
             aux_out[i] = rv;
-            const double2 bd = to_d(bv), rd = to_d(rv);
-            acc[0].x += bd.x * bd.x + bd.y * bd.y;
-            acc[1].x += rd.x * rd.x + rd.y * rd.y;
-            acc[2] = cadd(acc[2], cjmul(rd, rd));
+            accR[0].x += bv.x * bv.x + bv.y * bv.y;
+            accR[1].x += rv.x * rv.x + rv.y * rv.y;
+            accR[2] = cadd(accR[2], cjmul(rv, rv));
         } else {  // kSpmvTrueRes
             const C bv = aux[i];
             const C rv = csub(bv, yv);
             y[i] = rv;
-            const double2 bd = to_d(bv), rd = to_d(rv);
-            acc[0].x += rd.x * rd.x + rd.y * rd.y;
-            acc[1].x += bd.x * bd.x + bd.y * bd.y;
+            accR[0].x += rv.x * rv.x + rv.y * rv.y;
+            accR[1].x += bv.x * bv.x + bv.y * bv.y;
         }
     }
     if (!REDUCE) return;
+    double2 acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = to_d(accR[q]);
     __shared__ double2 out[NQ * K];
     if (grid_reduce_lanes<NQ, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
@@ -265,12 +279,12 @@ __global__ void __launch_bounds__(kBlock) k_ssor_fwd(OpView<R> A, DiagView<R> D,
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
     const long tasks = (long)count * GPS;
-    const int f = B.fmap[rhs];
+    const R om = (R)B.omega[rhs];
     for (long t = wg; t < tasks; t += W) {
         const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
         const C s = row_dot<R, K>(A, A.rp[row], A.rs[row], y, rhs);
         const size_t i = (size_t)row * K + rhs;
-        y[i] = cmul(csub(in[i], s), D.dinv[(size_t)row * D.nf + f]);
+        y[i] = cmul(csub(in[i], s), inv_c(diag_of(D, row, om)));
     }
 }
 
@@ -288,12 +302,12 @@ __global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D,
     const long wg = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long W = ((long)gridDim.x * blockDim.x) >> 5;
     const long tasks = (long)count * GPS;
-    const int f = B.fmap[rhs];
+    const R om = (R)B.omega[rhs];
     for (long t = wg; t < tasks; t += W) {
         const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
         const C s = row_dot<R, K>(A, A.rs[row], A.rp[row + 1], out, rhs);
         const size_t i = (size_t)row * K + rhs;
-        out[i] = csub(y[i], cmul(s, D.dinv[(size_t)row * D.nf + f]));
+        out[i] = csub(y[i], cmul(s, inv_c(diag_of(D, row, om))));
     }
 }
 
@@ -334,14 +348,14 @@ __global__ void __launch_bounds__(kBlock) k_update_s(long n, const cplx<R>* __re
     const BicgState S = st[rhs];
     const bool run = S.status == kRunning;
     const C al = from_d<C>(S.alpha);
-    double2 acc[1] = {make_double2(0.0, 0.0)};
+    R ss = 0;
     for (long i = i0; i < n; i += stride) {
         if (!run) { s[i] = cm<R>(0, 0); continue; }
         const C sv = csub(r[i], cmul(al, v[i]));
         s[i] = sv;
-        const double2 d = to_d(sv);
-        acc[0].x += d.x * d.x + d.y * d.y;
+        ss += sv.x * sv.x + sv.y * sv.y;
     }
+    double2 acc[1] = {make_double2((double)ss, 0.0)};
     __shared__ double2 out[K];
     if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
@@ -371,17 +385,18 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
     const bool run = S.status == kRunning;
     const bool pend = S.pend_x != 0;
     const C al = from_d<C>(S.alpha), om = from_d<C>(S.omega);
-    double2 acc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    R rr = 0;
+    C r0r = cm<R>(0, 0);
     for (long i = i0; i < n; i += stride) {
         if (pend) { x[i] = cadd(x[i], cmul(al, ph[i])); continue; }
         if (!run) continue;
         x[i] = cadd(x[i], cadd(cmul(al, ph[i]), cmul(om, sh[i])));
         const C rv = csub(s[i], cmul(om, t[i]));
         r[i] = rv;
-        const double2 d = to_d(rv);
-        acc[0].x += d.x * d.x + d.y * d.y;
-        acc[1] = cadd(acc[1], cjmul(to_d(r0[i]), d));
+        rr += rv.x * rv.x + rv.y * rv.y;
+        r0r = cadd(r0r, cjmul(r0[i], rv));
     }
+    double2 acc[2] = {make_double2((double)rr, 0.0), to_d(r0r)};
     __shared__ double2 out[2 * K];
     if (grid_reduce_lanes<2, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
@@ -396,6 +411,21 @@ inline void check_launch(long long* counter) {
     if (counter) ++*counter;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
+}
+
+// One resident wave of `kernel` (blocks per SM from the occupancy API x SMs),
+// capped by the reduction scratch; cached per kernel instantiation.
+template <class KernelT>
+int wave_grid(KernelT kernel, int cap) {
+    static int g = 0;
+    if (g == 0) {
+        int dev = 0, sms = 0, nb = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0);
+        g = std::max(1, nb) * std::max(1, sms);
+    }
+    return std::min(g, cap);
 }
 
 inline int blocks_for(long work, int per_block, int cap) {
@@ -425,22 +455,31 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
     const int streams = 2 + (aux ? 1 : 0) + (aux_out ? 1 : 0);
     const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * streams) : -1;
+    const int cap = c.red.max_blocks;
     switch (mode) {
         case kSpmvPlain:
             k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
-        case kSpmvAp:
-            k_spmv<R, K, kSpmvAp><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+        case kSpmvAp: {
+            auto kf = k_spmv<R, K, kSpmvAp>;
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
-        case kSpmvAs:
-            k_spmv<R, K, kSpmvAs><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+        }
+        case kSpmvAs: {
+            auto kf = k_spmv<R, K, kSpmvAs>;
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
-        case kSpmvInit:
-            k_spmv<R, K, kSpmvInit><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+        }
+        case kSpmvInit: {
+            auto kf = k_spmv<R, K, kSpmvInit>;
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
-        default:
-            k_spmv<R, K, kSpmvTrueRes><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+        }
+        default: {
+            auto kf = k_spmv<R, K, kSpmvTrueRes>;
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
+        }
     }
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
@@ -484,13 +523,13 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     ssor_k<R, K>(c, v.p, v.y, v.ph);
     spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 3 * vb) : -1;
-    k_update_s<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
+    k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.s, v.y, v.sh);
     spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb) : -1;
-    k_update_xr<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
+    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
 }

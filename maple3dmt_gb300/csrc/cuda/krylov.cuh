@@ -53,18 +53,20 @@ struct OpView {
     int n_pad;
 };
 
-// Complex diagonal of A and its inverse, [n_pad][nf] (frequency fastest).
+// Diagonal of A for every frequency from one frequency-independent pair per
+// row: sm[row] = (S_ii, Me_i) on free rows and (1, 0) on constrained or padding
+// rows, so d_f = S_ii + i omega_f Me_i (operators.cpp:607-616) and the SSOR
+// inverse (ssor.h:37-44) are formed in registers.
 template <class R>
 struct DiagView {
-    const dev::cplx<R>* d;
-    const dev::cplx<R>* dinv;
-    int nf;
+    const dev::cplx<R>* sm;
 };
 
 // Frequency index of each right-hand side of the batch.
 struct BatchView {
     int K;
     int fmap[dev::kMaxRhs];
+    double omega[dev::kMaxRhs];   // angular frequency of each right-hand side
 };
 
 // Optional CUDA-event timing of kernel classes on the solver's stream.

@@ -65,22 +65,17 @@ __global__ void k_edge_mass(MeshDev m, const double* __restrict__ sigma, double*
     me_dc[row] = dead ? 0.0 : sa * m.adual[row] * m.elen[row];      // operators.cpp:958-972
 }
 
-__global__ void k_assemble_diag(MeshDev m, const double* __restrict__ Me, const double* __restrict__ omegas,
-                                int nf, double2* d, double2* dinv, float2* d32, float2* dinv32) {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long)m.n_pad * nf) return;
-    const int row = (int)(i / nf), f = (int)(i % nf);   // layout [row][nf]
-    double2 dv, di;
-    if (m.flags[row] & (kFlagConstrained | kFlagPad)) {
-        dv = make_double2(1.0, 0.0);
-        di = dv;
-    } else {
-        dv = make_double2(m.s_diag[row], omegas[f] * Me[row]);
-        di = (hypot(dv.x, dv.y) > 1e-30) ? cdiv(make_double2(1.0, 0.0), dv) : make_double2(1.0, 0.0);
-    }
-    d[i] = dv;
-    dinv[i] = di;
-    if (d32) { d32[i] = make_float2((float)dv.x, (float)dv.y); dinv32[i] = make_float2((float)di.x, (float)di.y); }
+// (S_ii, Me_i) on free rows and (1, 0) on constrained / padding rows: the
+// frequency-independent pair from which the batched kernels form
+// d_f = S_ii + i omega_f Me_i.
+__global__ void k_diag_coeffs(MeshDev m, const double* __restrict__ Me, double2* sm, float2* sm32) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= m.n_pad) return;
+    double2 v;
+    if (m.flags[row] & (kFlagConstrained | kFlagPad)) v = make_double2(1.0, 0.0);
+    else v = make_double2(m.s_diag[row], Me[row]);
+    sm[row] = v;
+    sm32[row] = make_float2((float)v.x, (float)v.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -221,15 +216,15 @@ __global__ void k_dc_phi0(MeshDev m, VecK rhs, RhsInfo info, DcWork w) {
 }
 
 // divJ = G^T (me E) - phi0, zero on BC nodes; |divJ| -> outer-loop test
-__global__ void k_dc_divj(MeshDev m, const double* __restrict__ me, VecK E, int use_phi0, DcWork w,
-                          double tol, RedScratch rs) {
-    const int K = E.K;
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_dc_divj(MeshDev m, const double* __restrict__ me, VecK E,
+                                                    int use_phi0, DcWork w, double tol, RedScratch rs) {
     const long n = (long)m.nn * K;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
     const int k = (int)(i0 % K);
     const bool act = w.st[k].active && !w.st[k].done;
-    double2 acc[1][1] = {{zero2()}};
+    double2 acc[1] = {zero2()};
     for (long i = i0; i < n && act; i += stride) {
         const int v = (int)(i / K);
         double2 d = zero2();
@@ -246,10 +241,10 @@ __global__ void k_dc_divj(MeshDev m, const double* __restrict__ me, VecK E, int 
             if (use_phi0) d = csub(d, w.phi0[i]);
         }
         w.divJ[i] = d;
-        acc[0][0].x += hypot(d.x, d.y) * hypot(d.x, d.y);
+        acc[0].x += d.x * d.x + d.y * d.y;
     }
-    __shared__ double2 out[kMaxRhs];
-    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+    __shared__ double2 out[K];
+    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             DcState S = w.st[threadIdx.x];
             if (S.active && !S.done) {
@@ -275,13 +270,14 @@ __device__ __forceinline__ double2 jac_apply(double2 r, double d) {
 }
 
 // phi = 0, r = divJ, z = r / diag, p = z, rz = (r, z)
-__global__ void k_dc_cg_init(int nn, int K, DcWork w, RedScratch rs) {
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_dc_cg_init(int nn, DcWork w, RedScratch rs) {
     const long n = (long)nn * K;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
     const int k = (int)(i0 % K);
     const bool run = w.st[k].cg_run;
-    double2 acc[1][1] = {{zero2()}};
+    double2 acc[1] = {zero2()};
     for (long i = i0; i < n && run; i += stride) {
         const int v = (int)(i / K);
         const double2 r = w.divJ[i];
@@ -290,22 +286,23 @@ __global__ void k_dc_cg_init(int nn, int K, DcWork w, RedScratch rs) {
         w.r[i] = r;
         w.z[i] = z;
         w.p[i] = z;
-        acc[0][0] = cadd(acc[0][0], cjmul(r, z));
+        acc[0] = cadd(acc[0], cjmul(r, z));
     }
-    __shared__ double2 out[kMaxRhs];
-    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+    __shared__ double2 out[K];
+    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K && w.st[threadIdx.x].cg_run) w.st[threadIdx.x].rz = out[threadIdx.x];
     }
 }
 
 // Ap = L p, (p, Ap) -> alpha   (forward_solver_fv.cpp:681-692)
-__global__ void k_dc_cg_ap(MeshDev m, int K, DcWork w, RedScratch rs) {
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_dc_cg_ap(MeshDev m, DcWork w, RedScratch rs) {
     const long n = (long)m.nn * K;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
     const int k = (int)(i0 % K);
     const bool run = w.st[k].cg_run;
-    double2 acc[1][1] = {{zero2()}};
+    double2 acc[1] = {zero2()};
     for (long i = i0; i < n && run; i += stride) {
         const int v = (int)(i / K);
         const double2 pv = w.p[i];
@@ -317,10 +314,10 @@ __global__ void k_dc_cg_ap(MeshDev m, int K, DcWork w, RedScratch rs) {
             s.y += a * pw.y;
         }
         w.Ap[i] = s;
-        acc[0][0] = cadd(acc[0][0], cjmul(pv, s));
+        acc[0] = cadd(acc[0], cjmul(pv, s));
     }
-    __shared__ double2 out[kMaxRhs];
-    if (grid_reduce<1, kMaxRhs, 1>(acc, k, rs, out)) {
+    __shared__ double2 out[K];
+    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             DcState S = w.st[threadIdx.x];
             if (S.cg_run) {
@@ -334,7 +331,8 @@ __global__ void k_dc_cg_ap(MeshDev m, int K, DcWork w, RedScratch rs) {
 }
 
 // phi += alpha p, r -= alpha Ap, |r| test, z = r / diag, beta   (:693-710)
-__global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch rs) {
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_dc_cg_update(int nn, int cg_max, DcWork w, RedScratch rs) {
     const long n = (long)nn * K;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
@@ -342,7 +340,7 @@ __global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch r
     const DcState S0 = w.st[k];
     const bool run = S0.cg_run;
     const double2 al = S0.alpha;
-    double2 acc[1][2] = {{zero2(), zero2()}};
+    double2 acc[2] = {zero2(), zero2()};
     for (long i = i0; i < n && run; i += stride) {
         const int v = (int)(i / K);
         w.phi[i] = cadd(w.phi[i], cmul(al, w.p[i]));
@@ -350,12 +348,11 @@ __global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch r
         w.r[i] = r;
         const double2 z = jac_apply(r, w.jac_diag[v]);
         w.z[i] = z;
-        const double ar = hypot(r.x, r.y);
-        acc[0][0].x += ar * ar;
-        acc[0][1] = cadd(acc[0][1], cjmul(r, z));
+        acc[0].x += r.x * r.x + r.y * r.y;
+        acc[1] = cadd(acc[1], cjmul(r, z));
     }
-    __shared__ double2 out[2 * kMaxRhs];
-    if (grid_reduce<2, kMaxRhs, 1>(acc, k, rs, out)) {
+    __shared__ double2 out[2 * K];
+    if (grid_reduce_lanes<2, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             DcState S = w.st[threadIdx.x];
             if (S.cg_run) {
@@ -364,7 +361,7 @@ __global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch r
                 if (sqrt(S.rn) < 1e-10 * S.dn) {
                     S.cg_run = 0;
                 } else {
-                    const double2 rzn = out[kMaxRhs + threadIdx.x];
+                    const double2 rzn = out[K + threadIdx.x];
                     S.beta = cdiv(rzn, make_double2(S.rz.x + 1e-30, S.rz.y));
                     S.rz = rzn;
                     if (S.cg_iter >= cg_max) S.cg_run = 0;
@@ -376,7 +373,8 @@ __global__ void k_dc_cg_update(int nn, int K, int cg_max, DcWork w, RedScratch r
 }
 
 // p = z + beta p
-__global__ void k_dc_cg_p(int nn, int K, DcWork w) {
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_dc_cg_p(int nn, DcWork w) {
     const long n = (long)nn * K;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
@@ -712,10 +710,8 @@ void edge_mass(const MeshDev& m, const double* sigma, double* Me, double* me_dc,
     ck();
 }
 
-void assemble_diag(const MeshDev& m, const double* Me, const double* omegas, int nf, double2* d,
-                   double2* dinv, float2* d32, float2* dinv32, cudaStream_t s) {
-    const long n = (long)m.n_pad * nf;
-    k_assemble_diag<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(m, Me, omegas, nf, d, dinv, d32, dinv32);
+void diag_coeffs(const MeshDev& m, const double* Me, double2* sm, float2* sm32, cudaStream_t s) {
+    k_diag_coeffs<<<grid1(m.n_pad), kBlock, 0, s>>>(m, Me, sm, sm32);
     ck();
 }
 
@@ -780,9 +776,24 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
     ck();
 }
 
-long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
-                  double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk) {
-    const int K = E.K;
+template <class KernelT>
+int dc_wave(KernelT kernel, int cap) {
+    static int g = 0;
+    if (g == 0) {
+        int dev = 0, sms = 0, nb = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0);
+        g = (nb > 0 ? nb : 1) * (sms > 0 ? sms : 1);
+    }
+    return g < cap ? g : cap;
+}
+
+template <int K>
+long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
+                    double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
+                    DcCounters* counters) {
+    if (counters) counters->calls += 1;
     long long launches = 0;
     std::vector<DcState> hs(K);
     for (int k = 0; k < K; ++k) {
@@ -792,26 +803,29 @@ long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, 
         hs[k] = S;
     }
     cudaMemcpyAsync(w.st, hs.data(), sizeof(DcState) * K, cudaMemcpyHostToDevice, s);
-    const int gv = red.max_blocks;
+    const int cap = red.max_blocks;
+    const int g_divj = dc_wave(k_dc_divj<K>, cap), g_init = dc_wave(k_dc_cg_init<K>, cap);
+    const int g_ap = dc_wave(k_dc_cg_ap<K>, cap), g_up = dc_wave(k_dc_cg_update<K>, cap);
+    const int g_p = dc_wave(k_dc_cg_p<K>, 1 << 20);
     const int cg_max = m.nn > 500 ? m.nn : 500;
-    const long nn_k = (long)m.nn * K;
     const int ge = (int)(((long)m.n_pad * K + kBlock - 1) / kBlock);
     for (int outer = 0; outer < max_outer; ++outer) {
-        k_dc_divj<<<gv, kBlock, 0, s>>>(m, me_dc, E, use_phi0 ? 1 : 0, w, tol, red);
+        k_dc_divj<K><<<g_divj, kBlock, 0, s>>>(m, me_dc, E, use_phi0 ? 1 : 0, w, tol, red);
         ck(); ++launches;
         cudaMemcpyAsync(hs.data(), w.st, sizeof(DcState) * K, cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
         bool any = false;
         for (int k = 0; k < K; ++k) any |= (hs[k].active && !hs[k].done);
         if (!any) break;
-        k_dc_cg_init<<<gv, kBlock, 0, s>>>(m.nn, K, w, red);
+        k_dc_cg_init<K><<<g_init, kBlock, 0, s>>>(m.nn, w, red);
         ck(); ++launches;
+        int chunk = cg_chunk;
         for (int it = 0; it < cg_max;) {
-            const int n_it = (cg_max - it) < cg_chunk ? (cg_max - it) : cg_chunk;
+            const int n_it = (cg_max - it) < chunk ? (cg_max - it) : chunk;
             for (int j = 0; j < n_it; ++j) {
-                k_dc_cg_ap<<<gv, kBlock, 0, s>>>(m, K, w, red);
-                k_dc_cg_update<<<gv, kBlock, 0, s>>>(m.nn, K, cg_max, w, red);
-                k_dc_cg_p<<<gv, kBlock, 0, s>>>(m.nn, K, w);
+                k_dc_cg_ap<K><<<g_ap, kBlock, 0, s>>>(m, w, red);
+                k_dc_cg_update<K><<<g_up, kBlock, 0, s>>>(m.nn, cg_max, w, red);
+                k_dc_cg_p<K><<<g_p, kBlock, 0, s>>>(m.nn, w);
                 launches += 3;
             }
             ck();
@@ -821,13 +835,29 @@ long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, 
             bool run = false;
             for (int k = 0; k < K; ++k) run |= hs[k].cg_run != 0;
             if (!run) break;
+            chunk = chunk < 200 ? 2 * chunk : chunk;   // polls grow sparser as PCG runs on
+        }
+        if (counters) {
+            counters->outer += 1;
+            for (int k = 0; k < K; ++k) if (hs[k].active && !hs[k].done) counters->cg_iterations += hs[k].cg_iter;
         }
         k_dc_grad<<<ge, kBlock, 0, s>>>(m, E, w);
         k_dc_outer_done<<<1, 32, 0, s>>>(K, w);
         ck(); launches += 2;
     }
-    (void)nn_k;
     return launches;
+}
+
+long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
+                  double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
+                  DcCounters* counters) {
+    switch (E.K) {
+        case 2: return divcorr_k<2>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
+        case 4: return divcorr_k<4>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
+        case 8: return divcorr_k<8>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
+        case 16: return divcorr_k<16>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
+        default: throw std::runtime_error("divergence correction batch must be 2, 4, 8 or 16");
+    }
 }
 
 void station_impedance(const StationDev& st, VecK E, const double* omegas, int nf, HCache* hc, double2* Z,

@@ -92,11 +92,11 @@ namespace phys {
 // build_edge_mass (operators.cpp:481-518) and me_sigma of
 // build_div_laplacian / compute_div_sigma_E (:956-973, :1030-1048).
 void edge_mass(const MeshDev& m, const double* sigma, double* Me, double* me_dc, cudaStream_t s);
-// A diagonal for each frequency: S_ii + i omega Me_i on free rows, 1 on
-// constrained / padding rows (operators.cpp:607-616, forward_solver_fv.cpp:224-234),
-// and its SSOR inverse (ssor.h:37-44). d/dinv: [n_pad][nf]; d32/dinv32 optional.
-void assemble_diag(const MeshDev& m, const double* Me, const double* omegas, int nf, double2* d,
-                   double2* dinv, float2* d32, float2* dinv32, cudaStream_t s);
+// Frequency-independent diagonal pairs (S_ii, Me_i) of A on free rows, (1, 0)
+// on constrained / padding rows (operators.cpp:607-616, forward_solver_fv.cpp:224-234);
+// d_f = S_ii + i omega_f Me_i and its SSOR inverse (ssor.h:37-44) are formed
+// by the kernels that need them.
+void diag_coeffs(const MeshDev& m, const double* Me, double2* sm, float2* sm32, cudaStream_t s);
 // E_primary on edges of direction pol for each rhs (forward_solver_fv.cpp:121-136, :318-323);
 void primary_field(const MeshDev& m, VecK out, const RhsInfo& info, bool bc_only, cudaStream_t s);
 // rhs_total of build_rhs (:244-255) from the BC values in `ebc`.
@@ -138,9 +138,10 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
 // One full divcorr_poisson_ call on every active rhs of E; phi0 optional.
 // Returns the number of kernel launches. Iteration caps: outer <= max_outer,
 // PCG <= max(500, nn) per outer (the reference's caps).
+struct DcCounters { int calls = 0, outer = 0; long long cg_iterations = 0; };
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w,
                   int max_outer, double tol, const int* active_host, dev::RedScratch red,
-                  cudaStream_t s, int cg_chunk);
+                  cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr);
 
 // ---- stations (forward_solver_fv.cpp:1490-1727, :1804-2065) ----
 // Z and H cache per (frequency f, station); E1 = rhs 2f, E2 = rhs 2f+1 of E.

@@ -101,7 +101,7 @@ void GpuSolver::free_all() {
     dfree(d_op_rp); dfree(d_op_rs); dfree(d_col); dfree(d_val); dfree(d_val32);
     dfree(d_colour_list);
     dfree(d_sigma); dfree(d_Me); dfree(d_me_dc);
-    dfree(d_diag); dfree(d_dinv); dfree(d_diag32); dfree(d_dinv32); dfree(d_omegas);
+    dfree(d_diag); dfree(d_diag32); dfree(d_omegas);
     dfree(red.partial); dfree(red.final_); dfree(red.counter);
     dfree(kv.x); dfree(kv.b); dfree(kv.r); dfree(kv.r0); dfree(kv.p); dfree(kv.v); dfree(kv.s); dfree(kv.t);
     dfree(kv.ph); dfree(kv.sh); dfree(kv.y);
@@ -346,6 +346,8 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     cuda_ok(cudaMemsetAsync(red.counter, 0, sizeof(unsigned int), stream), "memset");
     d_sigma = dalloc<double>(L.nc);
     d_Me = dalloc<double>(n_pad);
+    d_diag = dalloc<double2>(n_pad);
+    d_diag32 = dalloc<float2>(n_pad);
     d_me_dc = dalloc<double>(n_pad);
     d_host_stage = dalloc<double2>(std::max(ne, 1));
     d_stage_real = dalloc<double>(std::max(ne, L.nc));
@@ -362,7 +364,8 @@ void GpuSolver::set_sigma(const double* sigma, int n) {
     sigma_h.assign(sigma, sigma + n);
     cuda_ok(cudaMemcpyAsync(d_sigma, sigma, sizeof(double) * n, cudaMemcpyHostToDevice, stream), "sigma");
     phys::edge_mass(md, d_sigma, d_Me, d_me_dc, stream);
-    ++launches;
+    phys::diag_coeffs(md, d_Me, d_diag, d_diag32, stream);
+    launches += 2;
     have_sigma = true;
     lap_built = false;
     if (stations_set) {
@@ -495,9 +498,12 @@ void GpuSolver::ensure_sigma_device() {
 KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
     KrylovCtx<double> c;
     c.A = OpView<double>{d_op_rp, d_op_rs, d_col, d_val, n_pad};
-    c.D = DiagView<double>{d_diag, d_dinv, diag_nf};
+    c.D = DiagView<double>{d_diag};
     c.B.K = K;
-    for (int k = 0; k < dev::kMaxRhs; ++k) c.B.fmap[k] = (k < K) ? fmap[k] : 0;
+    for (int k = 0; k < dev::kMaxRhs; ++k) {
+        c.B.fmap[k] = (k < K) ? fmap[k] : 0;
+        c.B.omega[k] = (k < K && c.B.fmap[k] < (int)fz_freqs.size()) ? 2.0 * kPi * fz_freqs[c.B.fmap[k]] : 0.0;
+    }
     c.colour_ptr = colour_ptr;
     c.colour_list = d_colour_list;
     c.n_pad = n_pad;
@@ -539,20 +545,13 @@ void GpuSolver::factorize(const std::vector<double>& freqs) {
     ensure_sigma_device();
     const int nf = (int)freqs.size();
     if (diag_cap < nf) {
-        dfree(d_diag); dfree(d_dinv); dfree(d_diag32); dfree(d_dinv32); dfree(d_omegas);
-        d_diag = dalloc<double2>((size_t)n_pad * nf);
-        d_dinv = dalloc<double2>((size_t)n_pad * nf);
-        d_diag32 = dalloc<float2>((size_t)n_pad * nf);
-        d_dinv32 = dalloc<float2>((size_t)n_pad * nf);
+        dfree(d_omegas);
         d_omegas = dalloc<double>(nf);
         diag_cap = nf;
     }
     std::vector<double> om(nf);
     for (int f = 0; f < nf; ++f) om[f] = 2.0 * kPi * freqs[f];
     cuda_ok(cudaMemcpyAsync(d_omegas, om.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, stream), "omegas");
-    phys::assemble_diag(md, d_Me, d_omegas, nf, d_diag, d_dinv, d_diag32, d_dinv32, stream);
-    diag_nf = nf;
-    ++launches;
     fz_freqs = freqs;
     current_omega = om.back();
 }
@@ -642,7 +641,7 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     const KrylovCtx<double> c = kctx(K, fmap);
     KrylovCtx<float> f;
     f.A = OpView<float>{d_op_rp, d_op_rs, d_col, d_val32, n_pad};
-    f.D = DiagView<float>{d_diag32, d_dinv32, diag_nf};
+    f.D = DiagView<float>{d_diag32};
     f.B = c.B;
     f.colour_ptr = c.colour_ptr;
     f.colour_list = c.colour_list;
@@ -750,6 +749,20 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
     return R;
 }
 
+void GpuSolver::begin_call() {
+    stats.forward_iterations = 0;
+    stats.adjoint_iterations = 0;
+    stats.refinements = 0;
+    dcc = phys::DcCounters();
+}
+
+void GpuSolver::end_call() {
+    stats.divcorr_calls = dcc.calls;
+    stats.divcorr_outer = dcc.outer;
+    stats.divcorr_cg_iterations = dcc.cg_iterations;
+    stats.kernel_launches = launches;
+}
+
 void GpuSolver::timer_start() { cuda_ok(cudaEventRecord(ev_start, stream), "event"); }
 
 double GpuSolver::timer_stop() {
@@ -805,7 +818,7 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
         ensure_dc(K);
         const int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
         launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
-                                  red, stream, 25);
+                                  red, stream, 25, &dcc);
         timer.end(th);
     }
     phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
@@ -817,6 +830,7 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
     E_nf = nf;
     stats.n_rhs = Kreal;
     stats.total_iterations = 0;
+    for (int k = 0; k < Kreal; ++k) stats.forward_iterations += R.iters[k];
     for (int k = 0; k < Kreal && k < 64; ++k) {
         stats.iterations[k] = R.iters[k];
         stats.status[k] = R.status[k];
@@ -828,7 +842,9 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
 }
 
 void GpuSolver::compute_single_frequency(double freq, double* Z_out) {
+    begin_call();
     run_forward(std::vector<double>{freq}, Z_out);
+    end_call();
 }
 
 void GpuSolver::background_E(int pol, double* out) {
@@ -879,7 +895,7 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
     ++launches;
     int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
     launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                              active.data(), red, stream, 25);
+                              active.data(), red, stream, 25, &dcc);
     timer.end(th);
     std::vector<int> done(K, 0);
     std::vector<double> prev(K, 1e30);
@@ -912,7 +928,7 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
         if (!anyd) break;
         th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
         launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                                  dca.data(), red, stream, 25);
+                                  dca.data(), red, stream, 25, &dcc);
         timer.end(th);
         std::vector<BicgState> hs(K);
         for (int k = 0; k < K; ++k) {
@@ -968,6 +984,7 @@ void GpuSolver::run_adjoint(int K, const int* fmap, const RhsInfo& info, double2
         ++nr;
     }
     stats.n_rhs = nr;
+    stats.adjoint_iterations += stats.total_iterations;
     stats.kernel_launches = launches;
 }
 
@@ -975,6 +992,7 @@ void GpuSolver::adjoint_solve(const double* rhs_h, double* out, bool perturbatio
     (void)perturbation;
     if (fz_freqs.empty()) throw std::logic_error("no factorised frequency");
     const auto t0 = std::chrono::steady_clock::now();
+    begin_call();
     ensure_fields(2);
     ensure_vecs(2);
     const int K = 2;
@@ -989,6 +1007,7 @@ void GpuSolver::adjoint_solve(const double* rhs_h, double* out, bool perturbatio
     phys::from_permuted(md, VecK{d_lam, K}, 0, d_host_stage, stream);
     cuda_ok(cudaMemcpyAsync(out, d_host_stage, sizeof(double2) * L.ne, cudaMemcpyDeviceToHost, stream), "lam");
     sync();
+    end_call();
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -1042,6 +1061,7 @@ void GpuSolver::release() {
 void GpuSolver::forward_batch(const double* freqs, int nf, double* Z_out, double* E_out) {
     if (nf < 1) throw std::invalid_argument("no frequencies");
     const auto t0 = std::chrono::steady_clock::now();
+    begin_call();
     long long it_total = 0;
     for (int f0 = 0; f0 < nf; f0 += 8) {
         const int g = std::min(8, nf - f0);
@@ -1059,12 +1079,14 @@ void GpuSolver::forward_batch(const double* freqs, int nf, double* Z_out, double
     }
     stats.total_iterations = (int)it_total;
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    end_call();
 }
 
 void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,
                                double* grad) {
     if (nf < 1) throw std::invalid_argument("no frequencies");
     const auto t0 = std::chrono::steady_clock::now();
+    begin_call();
     const int ns = sd.ns;
     if (obs_cap < nf) {
         dfree(d_obs); dfree(d_err);
@@ -1099,7 +1121,7 @@ void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, c
     sync();
     stats.total_iterations = (int)it_total;
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    stats.kernel_launches = launches;
+    end_call();
 }
 
 }  // namespace m3d

@@ -56,6 +56,8 @@ public:
     KernelTimer timer;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     void timer_start();
+    void begin_call();
+    void end_call();
     double timer_stop();
     double tol_override = 0.0;
     double current_omega = 0.0;
@@ -90,9 +92,9 @@ private:
 
     // factorised frequencies (diagonals)
     std::vector<double> fz_freqs;
-    int diag_cap = 0, diag_nf = 1;
-    double2 *d_diag = nullptr, *d_dinv = nullptr;
-    float2 *d_diag32 = nullptr, *d_dinv32 = nullptr;
+    int diag_cap = 0;
+    double2* d_diag = nullptr;    // [n_pad] (S_ii, Me_i) pairs, see phys::diag_coeffs
+    float2* d_diag32 = nullptr;
     double* d_omegas = nullptr;
 
     // reductions
@@ -160,6 +162,7 @@ private:
                        const std::vector<int>& active, double tol, std::vector<int>& iters,
                        std::vector<int>& status, std::vector<double>& tres);
     long nnz_off = 0;
+    phys::DcCounters dcc;   // divergence-correction counters of the current call
     void sync();
 };
 

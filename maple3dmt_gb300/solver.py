@@ -205,7 +205,10 @@ class ForwardSolverFV:
         n = min(s.n_rhs, 64)
         return dict(n_rhs=s.n_rhs, iterations=list(s.iterations[:n]), status=list(s.status[:n]),
                     true_residual=list(s.true_residual[:n]), total_iterations=s.total_iterations,
-                    refinements=s.refinements, seconds=s.seconds, kernel_launches=s.kernel_launches)
+                    refinements=s.refinements, seconds=s.seconds, kernel_launches=s.kernel_launches,
+                    divcorr_calls=s.divcorr_calls, divcorr_outer=s.divcorr_outer,
+                    divcorr_cg_iterations=s.divcorr_cg_iterations,
+                    forward_iterations=s.forward_iterations, adjoint_iterations=s.adjoint_iterations)
 
 
 def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:
