@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--forward", default="interleaved", choices=["interleaved", "reference"])
     ap.add_argument("--min-level", type=int, default=6)
     ap.add_argument("--max-level", type=int, default=7)

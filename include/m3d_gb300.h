@@ -7,8 +7,9 @@
  * names the reference member it replaces.
  *
  * Conventions
- *  - Plain host pointers and sizes only; all buffers are caller-owned host
- *    memory; complex vectors are interleaved (re, im) doubles.
+ *  - Plain pointers and sizes only; all buffers are caller-owned host
+ *    memory, except for m3d_dot_batched, whose vectors are device pointers;
+ *    complex vectors are interleaved (re, im) doubles.
  *  - Edge vectors use the reference's edge numbering (StaggeredGrid edge ids,
  *    src/octree/staggered_grid.cpp:82-121); cell vectors the leaf order;
  *    impedances are [station][4] in the order Zxx, Zxy, Zyx, Zyy.
@@ -192,6 +193,16 @@ int m3d_forward_batch(m3d_solver* s, const double* freqs, int n_freqs, double* Z
  * frequencies and polarisations; Z_out nullable [n_freqs][n_stations][4]. */
 int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const double* obs_Z,
                        const double* obs_err, double* Z_out, double* grad);
+
+/* Batched Hermitian inner products out[k] = sum_i conj(x[i][k]) * y[i][k] of
+ * K interleaved complex-FP64 DEVICE vectors x, y ([n][K] complex; K in
+ * {1, 2, 4, 8, 16}); out is a device pointer to K complex values.  The
+ * reduction of BiCGStabSolver::dot (include/maple3dmt/forward/bicgstab.h:68-73)
+ * for K systems in one pass, exposed for callers that keep their own vectors
+ * on the device (misfit and model norms of an inversion).  Runs on the
+ * solver's stream with the reduction scratch of m3d_solver_setup (required
+ * first) and synchronises before returning. */
+int m3d_dot_batched(m3d_solver* s, const double* x, const double* y, long long n, int K, double* out);
 
 int m3d_get_stats(const m3d_solver* s, m3d_stats* out);
 

@@ -222,6 +222,18 @@ extern "C" int m3d_gradient_batch(m3d_solver* h, const double* freqs, int nf, co
     return guarded(h, [&](m3d::GpuSolver& s) { s.gradient_batch(freqs, nf, obs_Z, obs_err, Z_out, grad); });
 }
 
+extern "C" int m3d_dot_batched(m3d_solver* h, const double* x, const double* y, long long n, int K,
+                               double* out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (K != 1 && K != 2 && K != 4 && K != 8 && K != 16)
+        return fail(h, M3D_ERR_ARG, "K must be 1, 2, 4, 8 or 16");
+    if (n < 0 || !out || (n > 0 && (!x || !y))) return fail(h, M3D_ERR_ARG, "invalid vectors");
+    return guarded(h, [&](m3d::GpuSolver& s) {
+        s.dot_batched(reinterpret_cast<const double2*>(x), reinterpret_cast<const double2*>(y), n, K,
+                      reinterpret_cast<double2*>(out));
+    });
+}
+
 extern "C" int m3d_get_stats(const m3d_solver* h, m3d_stats* out) {
     if (!h || !h->s || !out) return M3D_ERR_ARG;
     *out = h->s->stats;

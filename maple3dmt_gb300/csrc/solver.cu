@@ -1,6 +1,8 @@
 // GpuSolver implementation: see solver.hpp.
 #include "solver.hpp"
 
+#include "cuda/dot.cuh"
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -1052,6 +1054,14 @@ void GpuSolver::delta_impedance(const double* dE, int pol, double* dZ) {
 void GpuSolver::release() {
     fz_freqs.clear();
     E_nf = 0;
+}
+
+void GpuSolver::dot_batched(const double2* x, const double2* y, long long n, int K, double2* out) {
+    cuda_ok(cudaSetDevice(device), "cudaSetDevice");
+    const int cap = std::min(dev::kDotMaxBlocks, red.max_blocks);
+    cuda_ok(dev::launch_dot_batched(x, y, n, K, cap, red, out, stream), "dot launch");
+    ++launches;
+    sync();
 }
 
 // ---------------------------------------------------------------------------

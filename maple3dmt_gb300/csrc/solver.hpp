@@ -51,6 +51,9 @@ public:
     void forward_batch(const double* freqs, int nf, double* Z_out, double* E_out);
     void gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,
                         double* grad);
+    // batched Hermitian dot of caller-owned device vectors on the solver's
+    // stream, with the reduction scratch allocated by setup
+    void dot_batched(const double2* x, const double2* y, long long n, int K, double2* out);
 
     m3d_stats stats{};
     KernelTimer timer;

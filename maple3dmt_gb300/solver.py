@@ -182,6 +182,11 @@ class ForwardSolverFV:
                                              Z.ctypes.data_as(c_double_p), g.ctypes.data_as(c_double_p)))
         return Z, g
 
+    def dot_batched(self, x_ptr: int, y_ptr: int, n: int, K: int, out_ptr: int):
+        """Hermitian dots of K interleaved complex128 device vectors ([n][K]);
+        writes K complex values at device address out_ptr."""
+        self._ck(self.lib.m3d_dot_batched(self.h, x_ptr, y_ptr, int(n), int(K), out_ptr))
+
     def timer_start(self):
         self._ck(self.lib.m3d_timer_start(self.h))
 

@@ -182,3 +182,27 @@ def test_c2_scale_true_residual(lib):
     assert s.ne == 1687305
     assert np.isfinite(Z).all()
     assert all(t <= 1e-7 for t in st["true_residual"][:4]), st
+
+
+@pytest.mark.parametrize("K", [1, 2, 4, 8, 16])
+def test_dot_batched_matches_numpy(g_small, K):
+    """Batched Hermitian dot of device vectors (the BiCGStab dot for K
+    systems): FP64 sums in a different order, so 1e-12 relative."""
+    import torch
+    from maple3dmt_gb300.solver import SolverError
+    s = _gpu(g_small)
+    rng = np.random.default_rng(K)
+    for n in (0, 1, 1000, 300001):
+        x = rng.normal(size=(n, K)) + 1j * rng.normal(size=(n, K))
+        y = rng.normal(size=(n, K)) + 1j * rng.normal(size=(n, K))
+        dx = torch.from_numpy(x).to("cuda:0")
+        dy = torch.from_numpy(y).to("cuda:0")
+        out = torch.full((K,), complex(7.0, 7.0), dtype=torch.complex128, device="cuda:0")
+        torch.cuda.synchronize()
+        s.dot_batched(dx.data_ptr(), dy.data_ptr(), n, K, out.data_ptr())
+        want = (np.conj(x) * y).sum(axis=0)
+        got = out.cpu().numpy()
+        assert np.abs(got - want).max() <= 1e-12 * max(np.abs(want).max(), 1.0), (n, K)
+    with pytest.raises(SolverError) as e:
+        s.dot_batched(dx.data_ptr(), dy.data_ptr(), 10, 3, out.data_ptr())
+    assert e.value.code == 1
