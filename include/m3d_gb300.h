@@ -8,14 +8,16 @@
  *
  * Conventions
  *  - Plain pointers and sizes only; all buffers are caller-owned host
- *    memory, except for m3d_dot_batched, whose vectors are device pointers;
- *    complex vectors are interleaved (re, im) doubles.
+ *    memory, except for m3d_dot_batched and m3d_dot_batched_noalloc, whose
+ *    vectors are device pointers; complex vectors are interleaved (re, im)
+ *    doubles.
  *  - Edge vectors use the reference's edge numbering (StaggeredGrid edge ids,
  *    src/octree/staggered_grid.cpp:82-121); cell vectors the leaf order;
  *    impedances are [station][4] in the order Zxx, Zxy, Zyx, Zyy.
- *  - Every function returns M3D_OK (0) or one M3D_ERR_* code and has
- *    synchronised the device before it returns; m3d_last_error() gives the
- *    message of the last failure on that handle.
+ *  - Every function returns M3D_OK (0) or one M3D_ERR_* code and, except
+ *    m3d_dot_batched_noalloc (stream-ordered), has synchronised the device
+ *    before it returns; m3d_last_error() gives the message of the last
+ *    failure on that handle.
  *  - A solver handle is single-threaded, like the reference (not re-entrant).
  *  - Solver state follows the reference's ordering rules: a frequency must be
  *    solved (m3d_compute_single_frequency) or factorised before the adjoint,
@@ -203,6 +205,20 @@ int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const do
  * solver's stream with the reduction scratch of m3d_solver_setup (required
  * first) and synchronises before returning. */
 int m3d_dot_batched(m3d_solver* s, const double* x, const double* y, long long n, int K, double* out);
+
+/* Allocation-free m3d_dot_batched (no counterpart in the reference): same
+ * kernel and result, but no solver handle and no device allocation, for
+ * callers that own all device memory and may not allocate.  Its reduction
+ * scratch is a fixed 256 KiB static device array per device (K <= 16
+ * right-hand sides x 1024 blocks); K > 16 returns M3D_ERR_TOO_LARGE, n is
+ * unlimited.  x, y, out are device pointers on the current device; the call
+ * enqueues on `stream` (a cudaStream_t; NULL = legacy default stream) and
+ * returns without synchronising.  The first call on each device looks up the
+ * scratch address (set-up); make it before latency-critical work.  Calls on
+ * the same device share the scratch: calls in flight at the same time (two
+ * streams, or two host threads without a lock) race and give wrong results,
+ * so issue them on one stream or serialise them. */
+int m3d_dot_batched_noalloc(const double* x, const double* y, long long n, int K, double* out, void* stream);
 
 int m3d_get_stats(const m3d_solver* s, m3d_stats* out);
 
