@@ -49,6 +49,12 @@ def parse():
     ap.add_argument("--min-level", type=int, default=6)
     ap.add_argument("--max-level", type=int, default=7)
     ap.add_argument("--nfreq", type=int, default=8)
+    # profiling runs only (a capped solve is not a bench number): Krylov
+    # iteration cap per solve, and skipping the CPU baseline
+    ap.add_argument("--maxiter", type=int, default=5000)
+    ap.add_argument("--row-kernels", type=int, default=1, choices=[0, 1],
+                    help="0: CSR rows read by the lanes; 1: slice-staged rows (bulk copies to shared memory)")
+    ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
 
@@ -222,9 +228,10 @@ def run_ours(args, rank, world, local_rank):
     import numpy as np
     from maple3dmt_gb300.solver import solver_for_survey
     sv, obs, err = workload(args)
-    s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=5000,
+    s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=args.maxiter,
                           precision=1 if args.precision == "mixed" else 0,
-                          forward_interleaved=1 if args.forward == "interleaved" else 0)
+                          forward_interleaved=1 if args.forward == "interleaved" else 0,
+                          row_kernels=args.row_kernels)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -259,7 +266,9 @@ def run_ours(args, rank, world, local_rank):
         st = s.stats()
         iters.append(st["total_iterations"])
         solver_stats = {k: st[k] for k in ("forward_iterations", "adjoint_iterations", "refinements",
-                                           "divcorr_calls", "divcorr_outer", "divcorr_cg_iterations")}
+                                           "divcorr_calls", "divcorr_outer", "divcorr_cg_iterations",
+                                           "divcorr_cg_sweeps")}
+        solver_stats["iterations_per_rhs"] = st["iterations"]
     launches = s.stats()["kernel_launches"] - launches0
     kt = s.kernel_times()
     s.set_kernel_timing(False)
@@ -286,7 +295,7 @@ def run_ours(args, rank, world, local_rank):
     h2d = s.nc * 8 + obs.size * 16 + err.size * 8
     d2h = s.nc * 8 + nf * len(sv.stations) * 4 * 16
     try:
-        cb = cpu_reference(args)
+        cb = None if args.no_cpu else cpu_reference(args)
     except Exception as exc:  # the baseline must not hide the GPU number
         cb = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
     line = {
@@ -298,7 +307,8 @@ def run_ours(args, rank, world, local_rank):
                                f"({s.ne} edges, {s.nc} cells), 121 stations, {nf} freqs 0.01-100 Hz, "
                                f"forward+adjoint+sensitivity gradient step ({solves_per_step} solves)",
                    "tol": 1e-7, "precision": args.precision, "forward": args.forward,
-                   "colours": s.n_colours, "l2": "inputs larger than L2 (matrix alone 260 MB)",
+                   "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
+                   "l2": "inputs larger than L2 (matrix alone 260 MB)",
                    "parallelism": f"replica x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

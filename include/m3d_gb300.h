@@ -112,6 +112,8 @@ typedef struct m3d_params {
     int forward_interleaved;  /* 0: forward as the reference (full BiCGStab, then divergence
                                  correction, forward_solver_fv.cpp:346-367); 1: forward solved
                                  with interleaved divergence correction like the adjoint (:778-888) */
+    int row_kernels;          /* SpMV / SSOR row kernels: 0 CSR rows read by the lanes,
+                                 1 32-row slices bulk-copied to shared memory */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -131,6 +133,7 @@ typedef struct m3d_stats {
     long long divcorr_cg_iterations;  /* Jacobi-PCG iterations, summed over rhs */
     long long forward_iterations;     /* Krylov iterations of the forward phase, summed over rhs */
     long long adjoint_iterations;     /* ... of the adjoint phase */
+    long long divcorr_cg_sweeps;      /* batched PCG iterations run (each serves every rhs of a batch) */
 } m3d_stats;
 
 void m3d_params_default(m3d_params* p);

@@ -24,6 +24,7 @@ class Params(C.Structure):
         ("max_refinements", C.c_int),
         ("print_level", C.c_int),
         ("forward_interleaved", C.c_int),
+        ("row_kernels", C.c_int),
     ]
 
 
@@ -43,6 +44,7 @@ class Stats(C.Structure):
         ("divcorr_cg_iterations", C.c_longlong),
         ("forward_iterations", C.c_longlong),
         ("adjoint_iterations", C.c_longlong),
+        ("divcorr_cg_sweeps", C.c_longlong),
     ]
 
 

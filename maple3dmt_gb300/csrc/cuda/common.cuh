@@ -64,6 +64,18 @@ __device__ __forceinline__ double2 shfl_xor(double2 v, int m) {
     return v;
 }
 
+// Blocks of `threads` threads with `smem` bytes of dynamic shared memory of
+// `kernel` that are resident on the current device at once (occupancy API x
+// SM count); cached per (device, kernel, threads, smem).
+int resident_blocks(const void* kernel, int threads = kBlock, int smem = 0);
+
+// One resident wave of `kernel`, at most `cap` blocks.
+template <class F>
+inline int wave_grid(F* kernel, int cap, int threads = kBlock, int smem = 0) {
+    const int g = resident_blocks(reinterpret_cast<const void*>(kernel), threads, smem);
+    return g < cap ? g : cap;
+}
+
 // Scratch for grid reductions: partial[block][kMaxQ * kMaxRhs] and a counter
 // that the last block resets.
 struct RedScratch {
@@ -144,12 +156,14 @@ __device__ bool grid_reduce(const double2 (&acc)[KT][NQ], int rhs0, RedScratch r
 // summed by a fixed set of threads, then in a fixed order).  Deterministic
 // for a fixed launch shape.  Returns true in the last block, where
 // out[q * K + k] (shared, NQ*K entries) holds the totals.
-template <int NQ, int K>
+template <int NQ, int K, int NT = kBlock>
 __device__ bool grid_reduce_lanes(double2 (&acc)[NQ], RedScratch rs, double2* out) {
     static_assert(K >= 1 && K <= 32 && (K & (K - 1)) == 0, "K must be a power of two <= 32");
+    static_assert(NT % 32 == 0 && NT >= 32, "block size must be whole warps");
     constexpr int PK = NQ * K;
-    __shared__ double2 sm[kWarpsPerBlock][PK];
-    __shared__ double2 chunk[kBlock];
+    constexpr int NW = NT / 32;
+    __shared__ double2 sm[NW][PK];
+    __shared__ double2 chunk[NT];
     __shared__ bool am_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -162,7 +176,7 @@ __device__ bool grid_reduce_lanes(double2 (&acc)[NQ], RedScratch rs, double2* ou
     __syncthreads();
     if (threadIdx.x < PK) {
         double2 s = make_double2(0.0, 0.0);
-        for (int w = 0; w < kWarpsPerBlock; ++w) s = cadd(s, sm[w][threadIdx.x]);
+        for (int w = 0; w < NW; ++w) s = cadd(s, sm[w][threadIdx.x]);
         __stcg(&rs.partial[(size_t)blockIdx.x * PK + threadIdx.x], s);
         __threadfence();
     }
@@ -174,7 +188,7 @@ __device__ bool grid_reduce_lanes(double2 (&acc)[NQ], RedScratch rs, double2* ou
     __syncthreads();
     if (!am_last) return false;
     __threadfence();
-    constexpr int CH = kBlock / PK > 0 ? kBlock / PK : 1;   // threads per total
+    constexpr int CH = NT / PK > 0 ? NT / PK : 1;   // threads per total
     const int p = threadIdx.x % PK, j = threadIdx.x / PK;
     double2 s = make_double2(0.0, 0.0);
     if (j < CH)

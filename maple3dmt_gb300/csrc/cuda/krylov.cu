@@ -2,9 +2,34 @@
 #include "krylov.cuh"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <stdexcept>
+#include <tuple>
+#include <utility>
 
 namespace m3d {
+
+namespace dev {
+
+int resident_blocks(const void* kernel, int threads, int smem) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void*, int, int>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(dev, kernel, threads, smem);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int sms = 0, nb = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, (size_t)smem);
+    const int g = std::max(1, nb) * std::max(1, sms);
+    cache[key] = g;
+    return g;
+}
+
+}  // namespace dev
 
 using namespace dev;
 
@@ -312,6 +337,265 @@ __global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D,
 }
 
 // ---------------------------------------------------------------------------
+// Slice-staged row kernels (segments of staged.cuh in shared memory).
+// ---------------------------------------------------------------------------
+
+// Threads per block of the staged kernels and passes over a 32-row slice:
+// K lanes per row, so a slice is 32 K lane-rows; up to 256 threads per block.
+template <int K> struct StagedShape {
+    static constexpr int NT = (32 * K < 256) ? 32 * K : 256;
+    static constexpr int PASSES = 32 * K / NT;
+    static constexpr int ROWS_PER_PASS = 32 / PASSES;
+};
+
+// Persistent slice pipeline of one block: work items i = blockIdx.x,
+// blockIdx.x + gridDim.x, ... < n_items; item i's lower (PARTS & 1) and upper
+// (PARTS & 2) segments are bulk-copied into stage k & 1 one item ahead of
+// use, so the next slice's matrix stream is in flight while body() runs.
+// Every wait is bounded: on a timeout the block sets kErrCopyTimeout in *err,
+// skips the stage, waits (bounded) for its copy in flight and stops.
+template <int PARTS, class Body>
+__device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__ seg, const int4* __restrict__ work,
+                                               long n_items, int stage_bytes, unsigned* err, Body body) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int4 wk[2];
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    __syncthreads();
+    auto issue = [&](long i, int stg) {   // thread 0 only
+        const int4 w = __ldg(&work[i]);
+        wk[stg] = w;
+        const SegItem it = unpack(w);
+        unsigned bytes = 0;
+        if (PARTS & 1) bytes += (unsigned)it.lo_len * 16u;
+        if (PARTS & 2) bytes += (unsigned)it.up_len * 16u;
+        unsigned char* dst = dsm + (size_t)stg * stage_bytes;
+        mbar_expect_tx(&bar[stg], bytes);
+        if (PARTS & 1) {
+            bulk_g2s(dst, seg + (size_t)it.lo_off * 16, (unsigned)it.lo_len * 16u, &bar[stg]);
+            dst += (size_t)it.lo_len * 16;
+        }
+        if (PARTS & 2) bulk_g2s(dst, seg + (size_t)it.up_off * 16, (unsigned)it.up_len * 16u, &bar[stg]);
+    };
+    long i = blockIdx.x;
+    if (threadIdx.x == 0 && i < n_items) issue(i, 0);
+    for (int k = 0; i < n_items; i += gridDim.x, ++k) {
+        const int stg = k & 1;
+        if (threadIdx.x == 0 && i + gridDim.x < n_items) {
+            fence_proxy_async_smem();
+            issue(i + gridDim.x, stg ^ 1);
+        }
+        const bool ok = mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
+        if (ok) {
+            body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
+        } else {
+            atomicOr(err, kErrCopyTimeout);
+            abort_flag = 1;
+        }
+        __syncthreads();
+        if (abort_flag) {
+            // never consume a stage that did not arrive; let the copy already
+            // issued for the next item land (bounded) before the block leaves
+            if (threadIdx.x == 0 && i + gridDim.x < n_items)
+                mbar_wait_bounded(&bar[stg ^ 1], (unsigned)((k + 1) >> 1) & 1u);
+            __syncthreads();
+            break;
+        }
+    }
+}
+
+// Sum over one staged row's entries [b, e): a_j * v[c_j][rhs], U gathers in
+// flight at a time, added to s in entry order.
+template <class R, int K, int U>
+__device__ __forceinline__ cplx<R> seg_row_dot(const int* __restrict__ col, const R* __restrict__ val, int b, int e,
+                                               const cplx<R>* __restrict__ v, int rhs, cplx<R> s) {
+    using C = cplx<R>;
+    for (int k = b; k < e; k += U) {
+        C xv[U];
+        R av[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool ok = k + u < e;
+            const int cu = ok ? col[k + u] : 0;
+            av[u] = ok ? val[k + u] : (R)0;
+            xv[u] = ok ? v[(size_t)cu * K + rhs] : cm<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) { s.x += av[u] * xv[u].x; s.y += av[u] * xv[u].y; }
+    }
+    return s;
+}
+
+// Lower then upper entries of one row as one sequence, so a row of up to U
+// entries in total is one round of gathers.
+template <class R, int K, int U>
+__device__ __forceinline__ cplx<R> seg_row_dot2(const SegRows<R>& lo, const SegRows<R>& up, int r,
+                                                const cplx<R>* __restrict__ v, int rhs) {
+    using C = cplx<R>;
+    const int bl = lo.begin_of(r), nl = lo.end[r] - bl;
+    const int bu = up.begin_of(r), n = nl + up.end[r] - bu;
+    C s = cm<R>(0, 0);
+    for (int k = 0; k < n; k += U) {
+        C xv[U];
+        R av[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int j = k + u;
+            const bool inl = j < nl, ok = j < n;
+            const int cu = inl ? lo.col[bl + j] : (ok ? up.col[bu + j - nl] : 0);
+            av[u] = inl ? lo.val[bl + j] : (ok ? up.val[bu + j - nl] : (R)0);
+            xv[u] = ok ? v[(size_t)cu * K + rhs] : cm<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) { s.x += av[u] * xv[u].x; s.y += av[u] * xv[u].y; }
+    }
+    return s;
+}
+
+template <class R> struct StagedUnroll { static constexpr int SPMV = 16, SWEEP = 8; };
+template <> struct StagedUnroll<double> { static constexpr int SPMV = 8, SWEEP = 8; };
+
+// SpMV over slice-staged rows, same modes and reductions as k_spmv.
+template <class R, int K, int MODE>
+__global__ void __launch_bounds__(StagedShape<K>::NT) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
+                                                                BatchView B, const cplx<R>* __restrict__ x,
+                                                                cplx<R>* __restrict__ y,
+                                                                const cplx<R>* __restrict__ aux,
+                                                                cplx<R>* __restrict__ aux_out, BicgState* st,
+                                                                RedScratch rs) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int RPW = Rpw<K>::v;
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kSpmvAs || MODE == kSpmvTrueRes) ? 2 : 3;
+    constexpr bool REDUCE = MODE != kSpmvPlain;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    C accR[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) accR[q] = cm<R>(0, 0);
+    slice_pipeline<3>(S.seg, S.work_nat, n_slices, S.stage_spmv, S.err, [&](const SegItem& it, const unsigned char* base) {
+        SegRows<R> lo, up;
+        lo.bind(base);
+        up.bind(base + (size_t)it.lo_len * 16);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int row = it.slice * kSlice + lr;
+            const size_t i = (size_t)row * K + rhs;
+            const C xi = x[i];
+            const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
+            const C d = diag_of(D, row, om);
+            const C s = seg_row_dot2<R, K, StagedUnroll<R>::SPMV>(lo, up, lr, x, rhs);
+            const C yv = cadd(s, cmul(d, xi));
+            if (MODE == kSpmvPlain) {
+                y[i] = yv;
+            } else if (MODE == kSpmvAp) {
+                y[i] = yv;
+                accR[0] = cadd(accR[0], cjmul(av, yv));
+            } else if (MODE == kSpmvAs) {
+                y[i] = yv;
+                accR[0].x += yv.x * yv.x + yv.y * yv.y;
+                accR[1] = cadd(accR[1], cjmul(yv, av));
+            } else if (MODE == kSpmvInit) {
+                const C rv = csub(av, yv);
+                y[i] = rv;
+                aux_out[i] = rv;
+                accR[0].x += av.x * av.x + av.y * av.y;
+                accR[1].x += rv.x * rv.x + rv.y * rv.y;
+                accR[2] = cadd(accR[2], cjmul(rv, rv));
+            } else {  // kSpmvTrueRes
+                const C rv = csub(av, yv);
+                y[i] = rv;
+                accR[0].x += rv.x * rv.x + rv.y * rv.y;
+                accR[1].x += av.x * av.x + av.y * av.y;
+            }
+        }
+    });
+    if (!REDUCE) return;
+    double2 acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = to_d(accR[q]);
+    __shared__ double2 out[NQ * K];
+    if (grid_reduce_lanes<NQ, K, Sh::NT>(acc, rs, out)) {
+        if (threadIdx.x < K) {
+            BicgState T = st[threadIdx.x];
+            if (MODE == kSpmvAp) ep_r0v(T, out, threadIdx.x, K);
+            else if (MODE == kSpmvAs) ep_omega(T, out, threadIdx.x, K);
+            else if (MODE == kSpmvInit) ep_init(T, out, threadIdx.x, K);
+            else ep_trueres(T, out, threadIdx.x, K);
+            st[threadIdx.x] = T;
+        }
+    }
+}
+
+// SSOR forward sweep of one colour over slice-staged lower parts
+// (ssor.h:58-66); items work_col[0..count) of the colour.
+template <class R, int K>
+__global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_fwd_st(SegView<R> S, const int4* __restrict__ work,
+                                                                    int count, DiagView<R> D, BatchView B,
+                                                                    const cplx<R>* __restrict__ in, cplx<R>* y) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int RPW = Rpw<K>::v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    slice_pipeline<1>(S.seg, work, count, S.stage_lo, S.err, [&](const SegItem& it, const unsigned char* base) {
+        SegRows<R> lo;
+        lo.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int row = it.slice * kSlice + lr;
+            const size_t i = (size_t)row * K + rhs;
+            const C iv = in[i];
+            const C d = diag_of(D, row, om);
+            const C s = seg_row_dot<R, K, StagedUnroll<R>::SWEEP>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs,
+                                                                  cm<R>(0, 0));
+            y[i] = cmul(csub(iv, s), inv_c(d));
+        }
+    });
+}
+
+// SSOR backward sweep of one colour over slice-staged upper parts (ssor.h:69-78).
+template <class R, int K>
+__global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_bwd_st(SegView<R> S, const int4* __restrict__ work,
+                                                                    int count, DiagView<R> D, BatchView B,
+                                                                    const cplx<R>* __restrict__ y, cplx<R>* out) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int RPW = Rpw<K>::v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    slice_pipeline<2>(S.seg, work, count, S.stage_up, S.err, [&](const SegItem& it, const unsigned char* base) {
+        SegRows<R> up;
+        up.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int row = it.slice * kSlice + lr;
+            const size_t i = (size_t)row * K + rhs;
+            const C yv = y[i];
+            const C d = diag_of(D, row, om);
+            const C s = seg_row_dot<R, K, StagedUnroll<R>::SWEEP>(up.col, up.val, up.begin_of(lr), up.end[lr], out,
+                                                                  rhs, cm<R>(0, 0));
+            out[i] = csub(yv, cmul(s, inv_c(d)));
+        }
+    });
+}
+
+// ---------------------------------------------------------------------------
 // Vector updates (thread per element (row, rhs); rhs = element % K is fixed
 // per thread because the grid stride is a multiple of K).
 // ---------------------------------------------------------------------------
@@ -413,21 +697,6 @@ inline void check_launch(long long* counter) {
     if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e));
 }
 
-// One resident wave of `kernel` (blocks per SM from the occupancy API x SMs),
-// capped by the reduction scratch; cached per kernel instantiation.
-template <class KernelT>
-int wave_grid(KernelT kernel, int cap) {
-    static int g = 0;
-    if (g == 0) {
-        int dev = 0, sms = 0, nb = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0);
-        g = std::max(1, nb) * std::max(1, sms);
-    }
-    return std::min(g, cap);
-}
-
 inline int blocks_for(long work, int per_block, int cap) {
     long b = (work + per_block - 1) / per_block;
     if (b < 1) b = 1;
@@ -435,11 +704,60 @@ inline int blocks_for(long work, int per_block, int cap) {
     return (int)b;
 }
 
-// Algorithmic bytes: matrix entries (value + column) once, the diagonals in
-// use, and each vector stream of the kernel once (gathers counted once).
+// Algorithmic bytes of one matrix pass: off-diagonal entries (value +
+// column), one row pointer and one (S_ii, Me_i) diagonal pair per row,
+//   M = nnz_off (b_r + 4) + 4 (n + 1) + n b_c,
+// the diagonals of every frequency being formed from the pair on the fly.
+// Vector streams are added by the callers, each counted once per pass
+// (gathers included once).
 template <class R>
 double matrix_bytes(const KrylovCtx<R>& c) {
-    return (double)c.nnz * (sizeof(R) + 4) + (double)c.n_rows * c.n_freq * sizeof(cplx<R>);
+    return (double)c.nnz * (sizeof(R) + 4) + 4.0 * ((double)c.n_rows + 1) + (double)c.n_rows * sizeof(cplx<R>);
+}
+
+// Launches one staged kernel: at most one resident wave of blocks (of
+// StagedShape<K>::NT threads with two stages of dynamic shared memory), no
+// more than there are work items, no more than `cap`.
+template <class F, class... Args>
+void launch_staged(F* kernel, int nt, int stage_bytes, long items, int cap, cudaStream_t st, Args... args) {
+    const int smem = 2 * stage_bytes;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    long g = std::min<long>((long)wave_grid(kernel, cap, nt, smem), std::max<long>(items, 1));
+    kernel<<<(int)g, nt, smem, st>>>(args...);
+}
+
+template <class R, int K>
+void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
+                 cplx<R>* aux_out, BicgState* st) {
+    constexpr int NT = StagedShape<K>::NT;
+    const long ns = c.n_pad / kSlice;
+    const int sb = c.seg.stage_spmv;
+    // reducing modes: every block must reach the reduction, so the grid stays
+    // within the partial-sum scratch
+    const int cap = (mode == kSpmvPlain) ? (1 << 20) : c.red.max_blocks;
+    switch (mode) {
+        case kSpmvPlain:
+            launch_staged(k_spmv_st<R, K, kSpmvPlain>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
+                          aux_out, st, c.red);
+            break;
+        case kSpmvAp:
+            launch_staged(k_spmv_st<R, K, kSpmvAp>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
+                          aux_out, st, c.red);
+            break;
+        case kSpmvAs:
+            launch_staged(k_spmv_st<R, K, kSpmvAs>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
+                          aux_out, st, c.red);
+            break;
+        case kSpmvInit:
+            launch_staged(k_spmv_st<R, K, kSpmvInit>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
+                          aux_out, st, c.red);
+            break;
+        default:
+            launch_staged(k_spmv_st<R, K, kSpmvTrueRes>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
+                          aux_out, st, c.red);
+            break;
+    }
 }
 
 template <class R, int K>
@@ -456,6 +774,12 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
     const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * streams) : -1;
     const int cap = c.red.max_blocks;
+    if (c.row_kernels == kRowsStaged) {
+        spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st);
+        check_launch(c.launches);
+        if (c.timer) c.timer->end(th);
+        return;
+    }
     switch (mode) {
         case kSpmvPlain:
             k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
@@ -489,11 +813,29 @@ template <class R, int K>
 void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
     constexpr int G = kSlice / Rpw<K>::v;   // row-group tasks per slice
     const int nc = (int)c.colour_ptr.size() - 1;
-    // whole apply: matrix once (lower forward, upper backward), the inverse
-    // diagonal twice, vectors in, y (written, read back), out
+    // whole apply: matrix once (lower forward, upper backward), vectors in,
+    // y (written, read back), out
     const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) +
-                                            (double)c.n_rows * c.n_freq * sizeof(cplx<R>) +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * 4) : -1;
+    if (c.row_kernels == kRowsStaged) {
+        constexpr int NT = StagedShape<K>::NT;
+        for (int col = 0; col < nc; ++col) {
+            const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+            if (s1 <= s0) continue;
+            launch_staged(k_ssor_fwd_st<R, K>, NT, c.seg.stage_lo, s1 - s0, 1 << 20, c.stream, c.seg,
+                          c.seg.work_col + s0, s1 - s0, c.D, c.B, in, y);
+            check_launch(c.launches);
+        }
+        for (int col = nc - 1; col >= 0; --col) {
+            const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+            if (s1 <= s0) continue;
+            launch_staged(k_ssor_bwd_st<R, K>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+                          c.seg.work_col + s0, s1 - s0, c.D, c.B, (const cplx<R>*)y, out);
+            check_launch(c.launches);
+        }
+        if (c.timer) c.timer->end(th);
+        return;
+    }
     for (int col = 0; col < nc; ++col) {
         const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "staged.cuh"
 
 namespace m3d {
 
@@ -106,7 +107,14 @@ struct KrylovCtx {
     long nnz;              // true off-diagonal entries (algorithmic bytes)
     int n_rows;            // real edge rows
     int n_freq;            // distinct diagonals in use
+    // slice-staged copy of A's off-diagonal part (see staged.cuh) and which
+    // row kernels run: kRowsDirect (CSR rows read by the lanes) or
+    // kRowsStaged (segments bulk-copied to shared memory)
+    dev::SegView<R> seg;
+    int row_kernels;
 };
+
+enum RowKernels : int { kRowsDirect = 0, kRowsStaged = 1 };
 
 // Work vectors of one batched solve, each [n_pad][K] complex of type R.
 template <class R>

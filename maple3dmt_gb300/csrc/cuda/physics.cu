@@ -776,19 +776,6 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
     ck();
 }
 
-template <class KernelT>
-int dc_wave(KernelT kernel, int cap) {
-    static int g = 0;
-    if (g == 0) {
-        int dev = 0, sms = 0, nb = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBlock, 0);
-        g = (nb > 0 ? nb : 1) * (sms > 0 ? sms : 1);
-    }
-    return g < cap ? g : cap;
-}
-
 template <int K>
 long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
                     double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
@@ -804,9 +791,9 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
     }
     cudaMemcpyAsync(w.st, hs.data(), sizeof(DcState) * K, cudaMemcpyHostToDevice, s);
     const int cap = red.max_blocks;
-    const int g_divj = dc_wave(k_dc_divj<K>, cap), g_init = dc_wave(k_dc_cg_init<K>, cap);
-    const int g_ap = dc_wave(k_dc_cg_ap<K>, cap), g_up = dc_wave(k_dc_cg_update<K>, cap);
-    const int g_p = dc_wave(k_dc_cg_p<K>, 1 << 20);
+    const int g_divj = wave_grid(k_dc_divj<K>, cap), g_init = wave_grid(k_dc_cg_init<K>, cap);
+    const int g_ap = wave_grid(k_dc_cg_ap<K>, cap), g_up = wave_grid(k_dc_cg_update<K>, cap);
+    const int g_p = wave_grid(k_dc_cg_p<K>, 1 << 20);
     const int cg_max = m.nn > 500 ? m.nn : 500;
     const int ge = (int)(((long)m.n_pad * K + kBlock - 1) / kBlock);
     for (int outer = 0; outer < max_outer; ++outer) {
@@ -820,7 +807,8 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
         k_dc_cg_init<K><<<g_init, kBlock, 0, s>>>(m.nn, w, red);
         ck(); ++launches;
         int chunk = cg_chunk;
-        for (int it = 0; it < cg_max;) {
+        int it = 0;
+        for (; it < cg_max;) {
             const int n_it = (cg_max - it) < chunk ? (cg_max - it) : chunk;
             for (int j = 0; j < n_it; ++j) {
                 k_dc_cg_ap<K><<<g_ap, kBlock, 0, s>>>(m, w, red);
@@ -839,6 +827,7 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
         }
         if (counters) {
             counters->outer += 1;
+            counters->cg_sweeps += it;
             for (int k = 0; k < K; ++k) if (hs[k].active && !hs[k].done) counters->cg_iterations += hs[k].cg_iter;
         }
         k_dc_grad<<<ge, kBlock, 0, s>>>(m, E, w);

@@ -138,7 +138,7 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
 // One full divcorr_poisson_ call on every active rhs of E; phi0 optional.
 // Returns the number of kernel launches. Iteration caps: outer <= max_outer,
 // PCG <= max(500, nn) per outer (the reference's caps).
-struct DcCounters { int calls = 0, outer = 0; long long cg_iterations = 0; };
+struct DcCounters { int calls = 0, outer = 0; long long cg_iterations = 0, cg_sweeps = 0; };
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w,
                   int max_outer, double tol, const int* active_host, dev::RedScratch red,
                   cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr);

@@ -80,6 +80,57 @@ __global__ void k_add_f32_scaled(double2* __restrict__ x, const float2* __restri
 }
 
 
+// Compact layout of the mixed-precision inner solve: lane j of a K_c-wide
+// batch works on right-hand side map[j] of the K-wide FP64 batch (-1: padding).
+
+// b32[row][j] = y64[row][map[j]] / scale[j]   (0 on padding lanes)
+__global__ void k_to_f32_lanes(const double2* __restrict__ y, int K, float2* __restrict__ b, int Kc,
+                               const int* __restrict__ map, const double* __restrict__ scale, long n_rows) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rows * Kc) return;
+    const long row = i / Kc;
+    const int j = (int)(i % Kc), m = map[j];
+    const double s = scale[j];
+    float2 v = make_float2(0.f, 0.f);
+    if (m >= 0 && s > 0.0) {
+        const double2 w = y[row * K + m];
+        v = make_float2((float)(w.x / s), (float)(w.y / s));
+    }
+    b[i] = v;
+}
+
+// x64[row][map[j]] += x32[row][j] * scale[j] for lanes with add[j] set
+__global__ void k_add_f32_lanes(double2* __restrict__ x, int K, const float2* __restrict__ d, int Kc,
+                                const int* __restrict__ map, const int* __restrict__ add,
+                                const double* __restrict__ scale, long n_rows) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rows * Kc) return;
+    const long row = i / Kc;
+    const int j = (int)(i % Kc), m = map[j];
+    if (m < 0 || !add[j] || scale[j] == 0.0) return;
+    const float2 v = d[i];
+    double2 xv = x[row * K + m];
+    xv.x += (double)v.x * scale[j];
+    xv.y += (double)v.y * scale[j];
+    x[row * K + m] = xv;
+}
+
+// Repacks up to five K_s-wide FP32 vectors into K_d-wide ones:
+// dst[row][j] = src[row][sel[j]] (0 where sel[j] < 0).
+struct LaneMove {
+    const float2* src[5];
+    float2* dst[5];
+    int nvec;
+};
+__global__ void k_gather_lanes(LaneMove mv, int Ks, int Kd, const int* __restrict__ sel, long n_rows) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_rows * Kd) return;
+    const long row = i / Kd;
+    const int j = (int)(i % Kd), sj = sel[j];
+    for (int v = 0; v < mv.nvec; ++v)
+        mv.dst[v][i] = sj >= 0 ? mv.src[v][row * Ks + sj] : make_float2(0.f, 0.f);
+}
+
 }  // namespace
 
 GpuSolver::GpuSolver(int dev_) : device(dev_) {
@@ -101,6 +152,8 @@ void GpuSolver::free_all() {
     dfree(md.inc_ptr); dfree(md.inc_edge); dfree(md.inc_other); dfree(md.inc_gv); dfree(md.inc_gw);
     dfree(md.node_bc); dfree(md.e_node); dfree(md.e_g); dfree(md.cell_ptr); dfree(md.cell_edge);
     dfree(d_op_rp); dfree(d_op_rs); dfree(d_col); dfree(d_val); dfree(d_val32);
+    dfree(d_seg64); dfree(d_seg32); dfree(d_work64); dfree(d_work32); dfree(d_seg_err);
+    seg64 = dev::SegView<double>{}; seg32 = dev::SegView<float>{};
     dfree(d_colour_list);
     dfree(d_sigma); dfree(d_Me); dfree(d_me_dc);
     dfree(d_diag); dfree(d_diag32); dfree(d_omegas);
@@ -110,6 +163,10 @@ void GpuSolver::free_all() {
     dfree(kv32.x); dfree(kv32.b); dfree(kv32.r); dfree(kv32.r0); dfree(kv32.p); dfree(kv32.v); dfree(kv32.s);
     dfree(kv32.t); dfree(kv32.ph); dfree(kv32.sh); dfree(kv32.y); dfree(d_scale);
     kv32_K = 0;
+    dfree(kv32b.x); dfree(kv32b.b); dfree(kv32b.r); dfree(kv32b.r0); dfree(kv32b.p); dfree(kv32b.v);
+    dfree(kv32b.s); dfree(kv32b.t); dfree(kv32b.ph); dfree(kv32b.sh); dfree(kv32b.y);
+    dfree(d_lane_map); dfree(d_lane_add); dfree(d_lane_sel);
+    kv32b_K = 0;
     dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
     dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_diag); dfree(dc.st);
@@ -333,6 +390,7 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     d_op_rp = dupload(op_rp, stream); d_op_rs = dupload(op_rs, stream);
     d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
     d_colour_list = dupload(colour_list, stream);
+    build_segments(op_rp, op_rs, ecol, eval);
     {
         std::vector<float> ev32(eval.begin(), eval.end());
         d_val32 = dupload(ev32, stream);
@@ -520,6 +578,8 @@ KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
     std::vector<int> fs(fmap, fmap + K);
     std::sort(fs.begin(), fs.end());
     c.n_freq = (int)(std::unique(fs.begin(), fs.end()) - fs.begin());
+    c.seg = seg64;
+    c.row_kernels = P.row_kernels;
     return c;
 }
 
@@ -639,6 +699,23 @@ void GpuSolver::ensure_vecs32(int K) {
     kv32_K = K;
 }
 
+void GpuSolver::ensure_vecs32b(int K) {
+    if (kv32b_K >= K) return;
+    KrylovVecs<float>& v = kv32b;
+    dfree(v.x); dfree(v.b); dfree(v.r); dfree(v.r0); dfree(v.p); dfree(v.v); dfree(v.s);
+    dfree(v.t); dfree(v.ph); dfree(v.sh); dfree(v.y);
+    const size_t n = (size_t)n_pad * K;
+    v.x = dalloc<float2>(n); v.b = dalloc<float2>(n); v.r = dalloc<float2>(n); v.r0 = dalloc<float2>(n);
+    v.p = dalloc<float2>(n); v.v = dalloc<float2>(n); v.s = dalloc<float2>(n); v.t = dalloc<float2>(n);
+    v.ph = dalloc<float2>(n); v.sh = dalloc<float2>(n); v.y = dalloc<float2>(n);
+    if (!d_lane_map) {
+        d_lane_map = dalloc<int>(dev::kMaxRhs);
+        d_lane_add = dalloc<int>(dev::kMaxRhs);
+        d_lane_sel = dalloc<int>(dev::kMaxRhs);
+    }
+    kv32b_K = K;
+}
+
 KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     const KrylovCtx<double> c = kctx(K, fmap);
     KrylovCtx<float> f;
@@ -657,13 +734,91 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     f.nnz = c.nnz;
     f.n_rows = c.n_rows;
     f.n_freq = c.n_freq;
+    f.seg = seg32;
+    f.row_kernels = c.row_kernels;
     return f;
 }
 
 BatchResult GpuSolver::solve_any(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
                                  double tol, int maxiter) {
-    if (P.precision == 1) return solve_batch_mixed(K, fmap, b, x, active, tol, maxiter);
-    return solve_batch(K, fmap, b, x, active, tol, maxiter);
+    BatchResult R = (P.precision == 1) ? solve_batch_mixed(K, fmap, b, x, active, tol, maxiter)
+                                       : solve_batch(K, fmap, b, x, active, tol, maxiter);
+    check_seg_err();
+    return R;
+}
+
+void GpuSolver::check_seg_err() {
+    if (!d_seg_err) return;
+    unsigned e = 0;
+    cuda_ok(cudaMemcpyAsync(&e, d_seg_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "seg err");
+    sync();
+    if (e) throw std::runtime_error("slice-staged copy did not complete (barrier wait timed out)");
+}
+
+// Slice segments (staged.cuh) of the split operator for both precisions:
+// per 32-row slice a lower and an upper segment, each [uint16 row ends]
+// [int32 columns, padded to 4] [values, padded to 16 bytes], 16-byte aligned,
+// and one work item per slice in natural and in colour-sweep order.
+void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs,
+                               const std::vector<int>& ecol, const std::vector<double>& eval) {
+    const int ns = n_slices;
+    auto build = [&](auto tag, std::vector<unsigned char>& buf, std::vector<int4>& work, int& st_lo, int& st_up,
+                     int& st_spmv) {
+        using R = decltype(tag);
+        buf.clear();
+        work.assign((size_t)ns, make_int4(0, 0, 0, 0));
+        st_lo = st_up = st_spmv = 0;
+        auto put = [&](int s, bool upper) -> std::pair<long, int> {
+            const long off = (long)buf.size();
+            uint16_t end[dev::kSlice];
+            std::vector<int> cols;
+            std::vector<R> vals;
+            for (int r = 0; r < dev::kSlice; ++r) {
+                const int row = s * dev::kSlice + r;
+                const int b = upper ? op_rs[row] : op_rp[row];
+                const int e = upper ? op_rp[row + 1] : op_rs[row];
+                for (int k = b; k < e; ++k) { cols.push_back(ecol[k]); vals.push_back((R)eval[k]); }
+                if (cols.size() > 65535) throw std::runtime_error("slice segment too large");
+                end[r] = (uint16_t)cols.size();
+            }
+            const size_t n = cols.size();
+            const size_t n4 = (n + 3) & ~(size_t)3;
+            const size_t per = 16 / sizeof(R);
+            const size_t nv = (n + per - 1) / per * per;
+            const size_t bytes = dev::kSegHeader + 4 * n4 + sizeof(R) * nv;
+            buf.resize(off + bytes, 0);
+            std::memcpy(buf.data() + off, end, sizeof(end));
+            std::memcpy(buf.data() + off + dev::kSegHeader, cols.data(), 4 * n);
+            std::memcpy(buf.data() + off + dev::kSegHeader + 4 * n4, vals.data(), sizeof(R) * n);
+            if ((long)(bytes / 16) > 65535) throw std::runtime_error("slice segment too large");
+            return {off / 16, (int)(bytes / 16)};
+        };
+        for (int s = 0; s < ns; ++s) {
+            const auto lo = put(s, false);
+            const auto up = put(s, true);
+            if (lo.first > 2000000000L || up.first > 2000000000L) throw std::runtime_error("mesh too large for segments");
+            work[s] = make_int4(s, (int)lo.first, (int)up.first, (lo.second << 16) | up.second);
+            st_lo = std::max(st_lo, lo.second * 16);
+            st_up = std::max(st_up, up.second * 16);
+            st_spmv = std::max(st_spmv, (lo.second + up.second) * 16);
+        }
+        std::vector<int4> wc(colour_list.size());
+        for (size_t i = 0; i < colour_list.size(); ++i) wc[i] = work[colour_list[i]];
+        work.insert(work.end(), wc.begin(), wc.end());
+    };
+    std::vector<unsigned char> b64, b32;
+    std::vector<int4> w64, w32;
+    int l64, u64, s64, l32, u32, s32;
+    build(double(0), b64, w64, l64, u64, s64);
+    build(float(0), b32, w32, l32, u32, s32);
+    d_seg64 = dupload(b64, stream);
+    d_seg32 = dupload(b32, stream);
+    d_work64 = dupload(w64, stream);
+    d_work32 = dupload(w32, stream);
+    d_seg_err = dalloc<unsigned>(1);
+    cuda_ok(cudaMemsetAsync(d_seg_err, 0, sizeof(unsigned), stream), "memset");
+    seg64 = dev::SegView<double>{d_seg64, d_work64, d_work64 + ns, s64, l64, u64, d_seg_err};
+    seg32 = dev::SegView<float>{d_seg32, d_work32, d_work32 + ns, s32, l32, u32, d_seg_err};
 }
 
 // Mixed precision: each step computes r = b - A x in FP64, solves A d = r
@@ -671,22 +826,30 @@ BatchResult GpuSolver::solve_any(int K, const int* fmap, double2* b, double2* x,
 // tolerance max(tol / ||r||_rel, 1e-5)), and adds d to x in FP64.  Steps repeat
 // until the FP64 true residual meets tol, the iteration budget is spent or a
 // step fails to reduce the residual by 10 %.
+//
+// The FP32 solve runs only the right-hand sides that still need it, packed
+// into the narrowest power-of-two batch (>= 2 lanes); whenever at most half of
+// the lanes are still iterating, the survivors' x, r, r0, p, v and Krylov
+// scalars are repacked into a batch half as wide (or narrower), after the
+// finished lanes' corrections have been added to the FP64 x.  Converged
+// systems then stop costing vector traffic; the matrix stream is shared by
+// whatever remains.
 BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, double2* x,
                                          const std::vector<int>& active, double tol, int maxiter) {
     ensure_vecs(K);
     ensure_vecs32(K);
+    ensure_vecs32b(std::max(2, K / 2));
     const KrylovCtx<double> c64 = kctx(K, fmap);
-    const KrylovCtx<float> c32 = kctx32(K, fmap);
-    KrylovVecs<float> v = kv32;
     BatchResult R;
     R.K = K;
     R.iters.assign(K, 0); R.status.assign(K, kInactive); R.res.assign(K, 0.0); R.true_res.assign(K, 0.0);
     std::vector<int> run = active;
     std::vector<double> prev(K, 1e300), scale(K, 0.0);
     std::vector<BicgState> hs(K);
-    const long n = (long)n_pad * K;
     const int chunk = 10;
     const int max_steps = 2 + std::max(0, P.max_refinements) * 4;
+    auto pow2_at_least = [](int n) { int k = 2; while (k < n) k *= 2; return k; };
+    auto launch_grid = [](long n) { return (int)((n + 255) / 256); };
     for (int step = 0; step <= max_steps; ++step) {
         // FP64 true residual y = b - A x
         for (int k = 0; k < K; ++k) {
@@ -697,7 +860,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
         spmv(c64, kSpmvTrueRes, x, kv.y, b, nullptr, d_states);
         cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
         sync();
-        bool any = false;
+        std::vector<int> lanes;   // current lane -> right-hand side of the FP64 batch
         for (int k = 0; k < K; ++k) {
             if (!active[k]) continue;
             const double rel = hs[k].true_res;
@@ -712,39 +875,100 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             }
             prev[k] = rel;
             scale[k] = hs[k].rnorm;
-            any = true;
+            lanes.push_back(k);
         }
-        if (!any) break;
-        std::vector<double> sc(K, 0.0);
-        for (int k = 0; k < K; ++k) sc[k] = run[k] ? scale[k] : 0.0;
-        cuda_ok(cudaMemcpyAsync(d_scale, sc.data(), sizeof(double) * K, cudaMemcpyHostToDevice, stream), "scale");
-        k_to_f32_scaled<<<(int)((n + 255) / 256), 256, 0, stream>>>(kv.y, kv32.b, d_scale, K, n);
-        cuda_ok(cudaMemsetAsync(kv32.x, 0, sizeof(float2) * (size_t)n, stream), "memset");
+        if (lanes.empty()) break;
+        int Kc = pow2_at_least((int)lanes.size());
+        lanes.resize(Kc, -1);
+        KrylovVecs<float> cur = kv32, other = kv32b;
+        int cur_cap = kv32_K, other_cap = kv32b_K;
+        if (Kc > other_cap) { /* start in the wide set */ } else { std::swap(cur, other); std::swap(cur_cap, other_cap); }
+        // per-lane maps, scales and frequencies of the packed batch
+        std::vector<int> map(dev::kMaxRhs, -1), add(dev::kMaxRhs, 0), fm(dev::kMaxRhs, 0);
+        std::vector<double> sc(dev::kMaxRhs, 0.0);
+        auto upload_lanes = [&](int Kn) {
+            for (int j = 0; j < dev::kMaxRhs; ++j) {
+                map[j] = (j < Kn) ? lanes[j] : -1;
+                sc[j] = (j < Kn && lanes[j] >= 0) ? scale[lanes[j]] : 0.0;
+                fm[j] = (j < Kn && lanes[j] >= 0) ? fmap[lanes[j]] : fmap[lanes[0] >= 0 ? lanes[0] : 0];
+            }
+            cuda_ok(cudaMemcpyAsync(d_lane_map, map.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "map");
+            cuda_ok(cudaMemcpyAsync(d_scale, sc.data(), sizeof(double) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "scale");
+        };
+        // flushes lanes with add[j] set: x64 += scale * x32
+        auto flush = [&](const KrylovVecs<float>& v, int Kn) {
+            cuda_ok(cudaMemcpyAsync(d_lane_add, add.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "add");
+            k_add_f32_lanes<<<launch_grid((long)n_pad * Kn), 256, 0, stream>>>(x, K, v.x, Kn, d_lane_map, d_lane_add,
+                                                                           d_scale, (long)n_pad);
+            ++launches;
+        };
+        upload_lanes(Kc);
+        k_to_f32_lanes<<<launch_grid((long)n_pad * Kc), 256, 0, stream>>>(kv.y, K, cur.b, Kc, d_lane_map, d_scale,
+                                                                      (long)n_pad);
+        cuda_ok(cudaMemsetAsync(cur.x, 0, sizeof(float2) * (size_t)n_pad * Kc, stream), "memset");
         launches += 2;
-        for (int k = 0; k < K; ++k) {
-            std::memset(&hs[k], 0, sizeof(BicgState));
-            hs[k].tol = std::min(0.5, std::max(tol / R.true_res[k], 1e-5));
-            hs[k].maxiter = std::max(1, maxiter - R.iters[k]);
-            hs[k].status = run[k] ? kRunning : kInactive;
+        std::vector<BicgState> ls(Kc);
+        for (int j = 0; j < Kc; ++j) {
+            std::memset(&ls[j], 0, sizeof(BicgState));
+            const int k = lanes[j];
+            if (k < 0) { ls[j].status = kInactive; continue; }
+            ls[j].tol = std::min(0.5, std::max(tol / R.true_res[k], 1e-5));
+            ls[j].maxiter = std::max(1, maxiter - R.iters[k]);
+            ls[j].status = kRunning;
         }
-        cuda_ok(cudaMemcpyAsync(d_states, hs.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream), "states");
-        bicg_init(c32, v, d_states);
+        cuda_ok(cudaMemcpyAsync(d_states, ls.data(), sizeof(BicgState) * Kc, cudaMemcpyHostToDevice, stream), "states");
+        KrylovCtx<float> c32 = kctx32(Kc, fm.data());
+        bicg_init(c32, cur, d_states);
         int it = 0;
+        auto record = [&](int j) {   // lane j leaves the batch
+            const int k = lanes[j];
+            if (k < 0) return;
+            R.iters[k] += ls[j].iter;
+            if (ls[j].status == kBreakdown) R.status[k] = kBreakdown;
+        };
         for (;;) {
-            cuda_ok(cudaMemcpyAsync(hs.data(), d_states, sizeof(BicgState) * K, cudaMemcpyDeviceToHost, stream), "states");
+            cuda_ok(cudaMemcpyAsync(ls.data(), d_states, sizeof(BicgState) * Kc, cudaMemcpyDeviceToHost, stream), "states");
             sync();
-            bool r = false;
-            for (int k = 0; k < K; ++k) r |= hs[k].status == kRunning;
-            if (!r || it >= maxiter) break;
-            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c32, v, d_states);
+            int nrun = 0;
+            for (int j = 0; j < Kc; ++j) nrun += (lanes[j] >= 0 && ls[j].status == kRunning);
+            if (nrun == 0 || it >= maxiter) break;
+            const int Kn = pow2_at_least(nrun);
+            if (Kn < Kc && Kn <= other_cap) {
+                // finished lanes: add their corrections and record them
+                for (int j = 0; j < dev::kMaxRhs; ++j)
+                    add[j] = (j < Kc && lanes[j] >= 0 && ls[j].status != kRunning) ? 1 : 0;
+                flush(cur, Kc);
+                std::vector<int> sel(dev::kMaxRhs, -1), nl(Kn, -1);
+                std::vector<BicgState> ns(Kn);
+                int q = 0;
+                for (int j = 0; j < Kc; ++j) {
+                    if (lanes[j] < 0) continue;
+                    if (ls[j].status == kRunning) { sel[q] = j; nl[q] = lanes[j]; ns[q] = ls[j]; ++q; }
+                    else record(j);
+                }
+                for (; q < Kn; ++q) { std::memset(&ns[q], 0, sizeof(BicgState)); ns[q].status = kInactive; }
+                cuda_ok(cudaMemcpyAsync(d_lane_sel, sel.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "sel");
+                LaneMove mv{};
+                mv.nvec = 5;
+                const float2* srcs[5] = {cur.x, cur.r, cur.r0, cur.p, cur.v};
+                float2* dsts[5] = {other.x, other.r, other.r0, other.p, other.v};
+                for (int v = 0; v < 5; ++v) { mv.src[v] = srcs[v]; mv.dst[v] = dsts[v]; }
+                k_gather_lanes<<<launch_grid((long)n_pad * Kn), 256, 0, stream>>>(mv, Kc, Kn, d_lane_sel, (long)n_pad);
+                ++launches;
+                lanes = nl;
+                ls = ns;
+                cuda_ok(cudaMemcpyAsync(d_states, ls.data(), sizeof(BicgState) * Kn, cudaMemcpyHostToDevice, stream), "states");
+                upload_lanes(Kn);
+                std::swap(cur, other);
+                std::swap(cur_cap, other_cap);
+                Kc = Kn;
+                c32 = kctx32(Kc, fm.data());
+            }
+            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c32, cur, d_states);
         }
-        for (int k = 0; k < K; ++k) {
-            if (!run[k]) continue;
-            R.iters[k] += hs[k].iter;
-            if (hs[k].status == kBreakdown) R.status[k] = kBreakdown;
-        }
-        k_add_f32_scaled<<<(int)((n + 255) / 256), 256, 0, stream>>>(x, kv32.x, d_scale, K, n);
-        ++launches;
+        for (int j = 0; j < dev::kMaxRhs; ++j) add[j] = (j < Kc && lanes[j] >= 0) ? 1 : 0;
+        flush(cur, Kc);
+        for (int j = 0; j < Kc; ++j) record(j);
         if (step > 0) ++stats.refinements;
     }
     timer.collect();
@@ -762,6 +986,7 @@ void GpuSolver::end_call() {
     stats.divcorr_calls = dcc.calls;
     stats.divcorr_outer = dcc.outer;
     stats.divcorr_cg_iterations = dcc.cg_iterations;
+    stats.divcorr_cg_sweeps = dcc.cg_sweeps;
     stats.kernel_launches = launches;
 }
 

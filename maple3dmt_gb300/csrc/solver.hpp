@@ -87,6 +87,15 @@ private:
     int *d_op_rp = nullptr, *d_op_rs = nullptr, *d_col = nullptr;
     double* d_val = nullptr;
     float* d_val32 = nullptr;
+    // slice-staged segments of the same operator (staged.cuh), per precision
+    unsigned char *d_seg64 = nullptr, *d_seg32 = nullptr;
+    int4 *d_work64 = nullptr, *d_work32 = nullptr;   // [n_slices] natural order, then colour order
+    dev::SegView<double> seg64{};
+    dev::SegView<float> seg32{};
+    unsigned* d_seg_err = nullptr;
+    void build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs, const std::vector<int>& ecol,
+                        const std::vector<double>& eval);
+    void check_seg_err();
 
     // sigma
     std::vector<double> sigma_h;
@@ -108,6 +117,10 @@ private:
     int kv_K = 0;
     KrylovVecs<float> kv32{};     // complex-FP32 inner solve of the mixed-precision path
     int kv32_K = 0;
+    KrylovVecs<float> kv32b{};    // second set for repacking the batch to fewer lanes
+    int kv32b_K = 0;
+    int *d_lane_map = nullptr, *d_lane_add = nullptr, *d_lane_sel = nullptr;   // [16] lane maps
+    void ensure_vecs32b(int K);
     double* d_scale = nullptr;    // [16] per-rhs residual norms of the refinement step
     // fields of the last forward solve: [n_pad][Kf], rhs 2f+p
     double2* d_E = nullptr;

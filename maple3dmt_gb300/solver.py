@@ -213,7 +213,8 @@ class ForwardSolverFV:
                     refinements=s.refinements, seconds=s.seconds, kernel_launches=s.kernel_launches,
                     divcorr_calls=s.divcorr_calls, divcorr_outer=s.divcorr_outer,
                     divcorr_cg_iterations=s.divcorr_cg_iterations,
-                    forward_iterations=s.forward_iterations, adjoint_iterations=s.adjoint_iterations)
+                    forward_iterations=s.forward_iterations, adjoint_iterations=s.adjoint_iterations,
+                    divcorr_cg_sweeps=s.divcorr_cg_sweeps)
 
 
 def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:

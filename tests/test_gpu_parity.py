@@ -41,11 +41,12 @@ def g_small(lib):
     return load_golden("small_block")
 
 
+@pytest.mark.parametrize("row_kernels", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("interleaved", [0, 1])
-def test_forward_matches_oracle(g_small, precision, interleaved):
+def test_forward_matches_oracle(g_small, precision, interleaved, row_kernels):
     g = g_small
-    s = _gpu(g, precision=precision, forward_interleaved=interleaved)
+    s = _gpu(g, precision=precision, forward_interleaved=interleaved, row_kernels=row_kernels)
     o = _oracle(g)
     for fr in g["freqs"]:
         Zg = s.compute_single_frequency(fr)
