@@ -410,60 +410,62 @@ __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__
     }
 }
 
-// Sum over one staged row's entries [b, e): a_j * v[c_j][rhs], U gathers in
-// flight at a time, added to s in entry order.
-template <class R, int K, int U>
+// Four values of a staged row from shared memory.
+__device__ __forceinline__ void lds4(const float* p, float (&a)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&a)[4]) {
+    const double2 q0 = *reinterpret_cast<const double2*>(p);
+    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+    a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
+}
+
+// s + sum over one staged row's entries [b, e) (b, e multiples of 4) of
+// a_j * v[c_j][rhs]: 16-byte shared-memory reads, eight gathers in flight,
+// sums in entry order.
+template <class R, int K>
 __device__ __forceinline__ cplx<R> seg_row_dot(const int* __restrict__ col, const R* __restrict__ val, int b, int e,
                                                const cplx<R>* __restrict__ v, int rhs, cplx<R> s) {
     using C = cplx<R>;
-    for (int k = b; k < e; k += U) {
-        C xv[U];
-        R av[U];
+    for (int k = b; k < e; k += 8) {
+        const bool two = k + 4 < e;
+        const int4 c0 = *reinterpret_cast<const int4*>(col + k);
+        R a0[4], a1[4] = {0, 0, 0, 0};
+        lds4(val + k, a0);
+        C x[8];
+        x[0] = v[(size_t)c0.x * K + rhs];
+        x[1] = v[(size_t)c0.y * K + rhs];
+        x[2] = v[(size_t)c0.z * K + rhs];
+        x[3] = v[(size_t)c0.w * K + rhs];
+        if (two) {
+            const int4 c1 = *reinterpret_cast<const int4*>(col + k + 4);
+            lds4(val + k + 4, a1);
+            x[4] = v[(size_t)c1.x * K + rhs];
+            x[5] = v[(size_t)c1.y * K + rhs];
+            x[6] = v[(size_t)c1.z * K + rhs];
+            x[7] = v[(size_t)c1.w * K + rhs];
+        } else {
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const bool ok = k + u < e;
-            const int cu = ok ? col[k + u] : 0;
-            av[u] = ok ? val[k + u] : (R)0;
-            xv[u] = ok ? v[(size_t)cu * K + rhs] : cm<R>(0, 0);
+            for (int u = 4; u < 8; ++u) x[u] = cm<R>(0, 0);
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) { s.x += av[u] * xv[u].x; s.y += av[u] * xv[u].y; }
+        for (int u = 0; u < 4; ++u) { s.x += a0[u] * x[u].x; s.y += a0[u] * x[u].y; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a1[u] * x[4 + u].x; s.y += a1[u] * x[4 + u].y; }
     }
     return s;
 }
 
-// Lower then upper entries of one row as one sequence, so a row of up to U
-// entries in total is one round of gathers.
-template <class R, int K, int U>
-__device__ __forceinline__ cplx<R> seg_row_dot2(const SegRows<R>& lo, const SegRows<R>& up, int r,
-                                                const cplx<R>* __restrict__ v, int rhs) {
-    using C = cplx<R>;
-    const int bl = lo.begin_of(r), nl = lo.end[r] - bl;
-    const int bu = up.begin_of(r), n = nl + up.end[r] - bu;
-    C s = cm<R>(0, 0);
-    for (int k = 0; k < n; k += U) {
-        C xv[U];
-        R av[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int j = k + u;
-            const bool inl = j < nl, ok = j < n;
-            const int cu = inl ? lo.col[bl + j] : (ok ? up.col[bu + j - nl] : 0);
-            av[u] = inl ? lo.val[bl + j] : (ok ? up.val[bu + j - nl] : (R)0);
-            xv[u] = ok ? v[(size_t)cu * K + rhs] : cm<R>(0, 0);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) { s.x += av[u] * xv[u].x; s.y += av[u] * xv[u].y; }
-    }
-    return s;
-}
-
-template <class R> struct StagedUnroll { static constexpr int SPMV = 16, SWEEP = 8; };
-template <> struct StagedUnroll<double> { static constexpr int SPMV = 8, SWEEP = 8; };
+// Register cap of the staged kernels: 1024 resident threads per SM for
+// complex FP32, 768 for complex FP64 (twice the registers per gather).
+template <class R, int K> struct StagedMinBlocks {
+    static constexpr int v = (sizeof(R) == 8 ? 768 : 1024) / StagedShape<K>::NT;
+};
 
 // SpMV over slice-staged rows, same modes and reductions as k_spmv.
 template <class R, int K, int MODE>
-__global__ void __launch_bounds__(StagedShape<K>::NT) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
                                                                 BatchView B, const cplx<R>* __restrict__ x,
                                                                 cplx<R>* __restrict__ y,
                                                                 const cplx<R>* __restrict__ aux,
@@ -493,7 +495,9 @@ __global__ void __launch_bounds__(StagedShape<K>::NT) k_spmv_st(SegView<R> S, lo
             const C xi = x[i];
             const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
             const C d = diag_of(D, row, om);
-            const C s = seg_row_dot2<R, K, StagedUnroll<R>::SPMV>(lo, up, lr, x, rhs);
+            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], x, rhs,
+                                          seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], x, rhs,
+                                                            cm<R>(0, 0)));
             const C yv = cadd(s, cmul(d, xi));
             if (MODE == kSpmvPlain) {
                 y[i] = yv;
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT) k_spmv_st(SegView<R> S, lo
 // SSOR forward sweep of one colour over slice-staged lower parts
 // (ssor.h:58-66); items work_col[0..count) of the colour.
 template <class R, int K>
-__global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_fwd_st(SegView<R> S, const int4* __restrict__ work,
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_fwd_st(SegView<R> S, const int4* __restrict__ work,
                                                                     int count, DiagView<R> D, BatchView B,
                                                                     const cplx<R>* __restrict__ in, cplx<R>* y) {
     using C = cplx<R>;
@@ -559,8 +563,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_fwd_st(SegView<R> S
             const size_t i = (size_t)row * K + rhs;
             const C iv = in[i];
             const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K, StagedUnroll<R>::SWEEP>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs,
-                                                                  cm<R>(0, 0));
+            const C s = seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs, cm<R>(0, 0));
             y[i] = cmul(csub(iv, s), inv_c(d));
         }
     });
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_fwd_st(SegView<R> S
 
 // SSOR backward sweep of one colour over slice-staged upper parts (ssor.h:69-78).
 template <class R, int K>
-__global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_bwd_st(SegView<R> S, const int4* __restrict__ work,
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_bwd_st(SegView<R> S, const int4* __restrict__ work,
                                                                     int count, DiagView<R> D, BatchView B,
                                                                     const cplx<R>* __restrict__ y, cplx<R>* out) {
     using C = cplx<R>;
@@ -588,8 +591,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT) k_ssor_bwd_st(SegView<R> S
             const size_t i = (size_t)row * K + rhs;
             const C yv = y[i];
             const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K, StagedUnroll<R>::SWEEP>(up.col, up.val, up.begin_of(lr), up.end[lr], out,
-                                                                  rhs, cm<R>(0, 0));
+            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], out, rhs, cm<R>(0, 0));
             out[i] = csub(yv, cmul(s, inv_c(d)));
         }
     });

@@ -176,7 +176,7 @@ __global__ void k_dc_lap(MeshDev m, const double* __restrict__ me, DcWork w) {
     const int a = m.inc_ptr[v], b = m.inc_ptr[v + 1];
     if (m.node_bc[v]) {
         w.lap_diag[v] = 1.0;
-        w.jac_diag[v] = 1.0;
+        w.jac_inv[v] = 1.0;
         for (int q = a; q < b; ++q) w.lap_off[q] = 0.0;
         return;
     }
@@ -195,7 +195,9 @@ __global__ void k_dc_lap(MeshDev m, const double* __restrict__ me, DcWork w) {
         w.lap_off[q] = off;
     }
     w.lap_diag[v] = diag;
-    w.jac_diag[v] = any ? diag : 1.0;
+    // Jacobi preconditioner z = r / diag (r where the diagonal is absent or
+    // below 1e-30), stored as its inverse so the PCG multiplies
+    w.jac_inv[v] = (any && fabs(diag) > 1e-30) ? 1.0 / diag : 1.0;
 }
 
 // phi0_v = sum_e G[e,v] rhs_e / (i omega)
@@ -265,9 +267,15 @@ __global__ void __launch_bounds__(kBlock) k_dc_divj(MeshDev m, const double* __r
     }
 }
 
-__device__ __forceinline__ double2 jac_apply(double2 r, double d) {
-    return (fabs(d) > 1e-30) ? make_double2(r.x / d, r.y / d) : r;
+__device__ __forceinline__ double2 jac_apply(double2 r, double dinv) {
+    return make_double2(r.x * dinv, r.y * dinv);
 }
+
+// The node Laplacian is real symmetric and the Jacobi preconditioner real
+// positive, so (r, z) = sum |r|^2 / d and (p, L p) are real: the PCG scalars
+// alpha, beta and (r, z) are carried as reals (imaginary parts zero), which
+// is the reference's complex recurrence (forward_solver_fv.cpp:681-710)
+// without its rounding-level imaginary parts, at a third of the FP64 work.
 
 // phi = 0, r = divJ, z = r / diag, p = z, rz = (r, z)
 template <int K>
@@ -281,16 +289,16 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_init(int nn, DcWork w, RedScra
     for (long i = i0; i < n && run; i += stride) {
         const int v = (int)(i / K);
         const double2 r = w.divJ[i];
-        const double2 z = jac_apply(r, w.jac_diag[v]);
+        const double2 z = jac_apply(r, w.jac_inv[v]);
         w.phi[i] = zero2();
         w.r[i] = r;
         w.z[i] = z;
         w.p[i] = z;
-        acc[0] = cadd(acc[0], cjmul(r, z));
+        acc[0].x += r.x * z.x + r.y * z.y;
     }
     __shared__ double2 out[K];
     if (grid_reduce_lanes<1, K>(acc, rs, out)) {
-        if (threadIdx.x < K && w.st[threadIdx.x].cg_run) w.st[threadIdx.x].rz = out[threadIdx.x];
+        if (threadIdx.x < K && w.st[threadIdx.x].cg_run) w.st[threadIdx.x].rz = make_double2(out[threadIdx.x].x, 0.0);
     }
 }
 
@@ -307,23 +315,35 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_ap(MeshDev m, DcWork w, RedScr
         const int v = (int)(i / K);
         const double2 pv = w.p[i];
         double2 s = make_double2(w.lap_diag[v] * pv.x, w.lap_diag[v] * pv.y);
-        for (int q = m.inc_ptr[v]; q < m.inc_ptr[v + 1]; ++q) {
-            const double a = w.lap_off[q];
-            const double2 pw = w.p[(size_t)m.inc_other[q] * K + k];
-            s.x += a * pw.x;
-            s.y += a * pw.y;
+        const int q0 = __ldg(&m.inc_ptr[v]), q1 = __ldg(&m.inc_ptr[v + 1]);
+        // eight incidences per round, all gathers in flight before the sums
+        for (int q = q0; q < q1; q += 8) {
+            double a[8];
+            double2 pw[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const bool ok = q + u < q1;
+                const int o = ok ? __ldg(&m.inc_other[q + u]) : 0;
+                a[u] = ok ? __ldg(&w.lap_off[q + u]) : 0.0;
+                pw[u] = ok ? w.p[(size_t)o * K + k] : zero2();
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                s.x += a[u] * pw[u].x;
+                s.y += a[u] * pw[u].y;
+            }
         }
         w.Ap[i] = s;
-        acc[0] = cadd(acc[0], cjmul(pv, s));
+        acc[0].x += pv.x * s.x + pv.y * s.y;
     }
     __shared__ double2 out[K];
     if (grid_reduce_lanes<1, K>(acc, rs, out)) {
         if (threadIdx.x < K) {
             DcState S = w.st[threadIdx.x];
             if (S.cg_run) {
-                const double2 pAp = out[threadIdx.x];
-                if (hypot(pAp.x, pAp.y) < 1e-30) S.cg_run = 0;
-                else S.alpha = cdiv(S.rz, pAp);
+                const double pAp = out[threadIdx.x].x;
+                if (fabs(pAp) < 1e-30) S.cg_run = 0;
+                else S.alpha = make_double2(S.rz.x / pAp, 0.0);
             }
             w.st[threadIdx.x] = S;
         }
@@ -339,17 +359,23 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_update(int nn, int cg_max, DcW
     const int k = (int)(i0 % K);
     const DcState S0 = w.st[k];
     const bool run = S0.cg_run;
-    const double2 al = S0.alpha;
+    const double al = S0.alpha.x;
     double2 acc[2] = {zero2(), zero2()};
     for (long i = i0; i < n && run; i += stride) {
         const int v = (int)(i / K);
-        w.phi[i] = cadd(w.phi[i], cmul(al, w.p[i]));
-        const double2 r = csub(w.r[i], cmul(al, w.Ap[i]));
+        const double2 pv = w.p[i], apv = w.Ap[i];
+        double2 ph = w.phi[i];
+        ph.x += al * pv.x;
+        ph.y += al * pv.y;
+        w.phi[i] = ph;
+        double2 r = w.r[i];
+        r.x -= al * apv.x;
+        r.y -= al * apv.y;
         w.r[i] = r;
-        const double2 z = jac_apply(r, w.jac_diag[v]);
+        const double2 z = jac_apply(r, w.jac_inv[v]);
         w.z[i] = z;
         acc[0].x += r.x * r.x + r.y * r.y;
-        acc[1] = cadd(acc[1], cjmul(r, z));
+        acc[1].x += r.x * z.x + r.y * z.y;
     }
     __shared__ double2 out[2 * K];
     if (grid_reduce_lanes<2, K>(acc, rs, out)) {
@@ -361,9 +387,9 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_update(int nn, int cg_max, DcW
                 if (sqrt(S.rn) < 1e-10 * S.dn) {
                     S.cg_run = 0;
                 } else {
-                    const double2 rzn = out[K + threadIdx.x];
-                    S.beta = cdiv(rzn, make_double2(S.rz.x + 1e-30, S.rz.y));
-                    S.rz = rzn;
+                    const double rzn = out[K + threadIdx.x].x;
+                    S.beta = make_double2(rzn / (S.rz.x + 1e-30), 0.0);
+                    S.rz = make_double2(rzn, 0.0);
                     if (S.cg_iter >= cg_max) S.cg_run = 0;
                 }
             }
@@ -381,8 +407,14 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_p(int nn, DcWork w) {
     if (i0 >= n) return;
     const int k = (int)(i0 % K);
     if (!w.st[k].cg_run) return;
-    const double2 be = w.st[k].beta;
-    for (long i = i0; i < n; i += stride) w.p[i] = cadd(w.z[i], cmul(be, w.p[i]));
+    const double be = w.st[k].beta.x;
+    for (long i = i0; i < n; i += stride) {
+        const double2 z = w.z[i];
+        double2 pv = w.p[i];
+        pv.x = z.x + be * pv.x;
+        pv.y = z.y + be * pv.y;
+        w.p[i] = pv;
+    }
 }
 
 // E -= G phi on edges that are not BC (:714-720), for rhs still in the outer loop

@@ -127,7 +127,7 @@ struct DcWork {
     double2 *divJ, *phi, *r, *z, *p, *Ap, *phi0;  // [nn][K]
     double* lap_diag;   // [nn] L_vv (1 on BC nodes)
     double* lap_off;    // [inc] off-diagonal per incidence entry (0 on BC rows / columns)
-    double* jac_diag;   // [nn] Jacobi diagonal (1 where L has no diagonal entry)
+    double* jac_inv;    // [nn] inverse Jacobi diagonal (1 where L has no usable diagonal)
     DcState* st;        // [K]
 };
 

@@ -4,10 +4,13 @@
 // TMA engine's 1-D mode) moves into shared memory:
 //
 //   segment = [uint16 end[32]]                 row r owns entries [end[r-1], end[r])
-//             [int32 col[n4]]                  n4 = n rounded up to 4
-//             [R val[nv]]                      nv = n rounded up to 16 / sizeof(R)
+//             [int32 col[n]]
+//             [R val[n]]
 //
-// so every segment starts and ends on a 16-byte boundary.  A slice's work item
+// with every row padded to a multiple of four entries (padding entries point
+// at the row itself with value 0), so rows start on 16-byte boundaries and
+// are read four entries at a time, and every segment starts and ends on a
+// 16-byte boundary.  A slice's work item
 // (int4) is {slice, lower offset, upper offset, (lower length << 16) | upper
 // length}, offsets and lengths in 16-byte units.  Kernels keep two segments in
 // flight per block (double buffering on two mbarriers): the next slice's
@@ -116,9 +119,8 @@ struct SegRows {
     __device__ __forceinline__ void bind(const unsigned char* base) {
         end = reinterpret_cast<const uint16_t*>(base);
         const int n = end[kSlice - 1];
-        const int n4 = (n + 3) & ~3;
         col = reinterpret_cast<const int*>(base + kSegHeader);
-        val = reinterpret_cast<const R*>(base + kSegHeader + 4 * n4);
+        val = reinterpret_cast<const R*>(base + kSegHeader + 4 * n);
     }
     __device__ __forceinline__ int begin_of(int r) const { return r ? end[r - 1] : 0; }
 };

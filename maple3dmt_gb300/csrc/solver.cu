@@ -37,6 +37,15 @@ T* dupload(const std::vector<T>& v, cudaStream_t s) {
     return p;
 }
 
+// Krylov work vectors start zeroed: staged row kernels read padding entries
+// (value 0) on the row itself, and 0 * x must never meet uninitialised bits.
+template <class T>
+T* dalloc_zero(size_t n, cudaStream_t s) {
+    T* p = dalloc<T>(n);
+    cuda_ok(cudaMemsetAsync(p, 0, (n ? n : 1) * sizeof(T), s), "memset");
+    return p;
+}
+
 template <class T>
 void dfree(T*& p) {
     if (p) cudaFree(p);
@@ -169,7 +178,7 @@ void GpuSolver::free_all() {
     kv32b_K = 0;
     dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
-    dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_diag); dfree(dc.st);
+    dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_inv); dfree(dc.st);
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
     dfree(d_host_stage); dfree(d_stage_real); dfree(d_states); dfree(d_states2);
@@ -505,9 +514,8 @@ void GpuSolver::ensure_vecs(int K) {
     dfree(kv.x); dfree(kv.b); dfree(kv.r); dfree(kv.r0); dfree(kv.p); dfree(kv.v); dfree(kv.s); dfree(kv.t);
     dfree(kv.ph); dfree(kv.sh); dfree(kv.y);
     const size_t n = (size_t)n_pad * K;
-    kv.x = dalloc<double2>(n); kv.b = dalloc<double2>(n); kv.r = dalloc<double2>(n); kv.r0 = dalloc<double2>(n);
-    kv.p = dalloc<double2>(n); kv.v = dalloc<double2>(n); kv.s = dalloc<double2>(n); kv.t = dalloc<double2>(n);
-    kv.ph = dalloc<double2>(n); kv.sh = dalloc<double2>(n); kv.y = dalloc<double2>(n);
+    for (double2** q : {&kv.x, &kv.b, &kv.r, &kv.r0, &kv.p, &kv.v, &kv.s, &kv.t, &kv.ph, &kv.sh, &kv.y})
+        *q = dalloc_zero<double2>(n, stream);
     kv_K = K;
 }
 
@@ -523,7 +531,7 @@ void GpuSolver::ensure_fields(int K) {
 void GpuSolver::ensure_dc(int K) {
     if (!dc.lap_diag) {
         dc.lap_diag = dalloc<double>(L.nn);
-        dc.jac_diag = dalloc<double>(L.nn);
+        dc.jac_inv = dalloc<double>(L.nn);
         dc.lap_off = dalloc<double>(2 * (size_t)L.ne);
         dc.st = dalloc<phys::DcState>(dev::kMaxRhs);
     }
@@ -692,9 +700,9 @@ void GpuSolver::ensure_vecs32(int K) {
     dfree(kv32.x); dfree(kv32.b); dfree(kv32.r); dfree(kv32.r0); dfree(kv32.p); dfree(kv32.v); dfree(kv32.s);
     dfree(kv32.t); dfree(kv32.ph); dfree(kv32.sh); dfree(kv32.y);
     const size_t n = (size_t)n_pad * K;
-    kv32.x = dalloc<float2>(n); kv32.b = dalloc<float2>(n); kv32.r = dalloc<float2>(n); kv32.r0 = dalloc<float2>(n);
-    kv32.p = dalloc<float2>(n); kv32.v = dalloc<float2>(n); kv32.s = dalloc<float2>(n); kv32.t = dalloc<float2>(n);
-    kv32.ph = dalloc<float2>(n); kv32.sh = dalloc<float2>(n); kv32.y = dalloc<float2>(n);
+    for (float2** q : {&kv32.x, &kv32.b, &kv32.r, &kv32.r0, &kv32.p, &kv32.v, &kv32.s, &kv32.t, &kv32.ph, &kv32.sh,
+                       &kv32.y})
+        *q = dalloc_zero<float2>(n, stream);
     if (!d_scale) d_scale = dalloc<double>(dev::kMaxRhs);
     kv32_K = K;
 }
@@ -705,9 +713,8 @@ void GpuSolver::ensure_vecs32b(int K) {
     dfree(v.x); dfree(v.b); dfree(v.r); dfree(v.r0); dfree(v.p); dfree(v.v); dfree(v.s);
     dfree(v.t); dfree(v.ph); dfree(v.sh); dfree(v.y);
     const size_t n = (size_t)n_pad * K;
-    v.x = dalloc<float2>(n); v.b = dalloc<float2>(n); v.r = dalloc<float2>(n); v.r0 = dalloc<float2>(n);
-    v.p = dalloc<float2>(n); v.v = dalloc<float2>(n); v.s = dalloc<float2>(n); v.t = dalloc<float2>(n);
-    v.ph = dalloc<float2>(n); v.sh = dalloc<float2>(n); v.y = dalloc<float2>(n);
+    for (float2** q : {&v.x, &v.b, &v.r, &v.r0, &v.p, &v.v, &v.s, &v.t, &v.ph, &v.sh, &v.y})
+        *q = dalloc_zero<float2>(n, stream);
     if (!d_lane_map) {
         d_lane_map = dalloc<int>(dev::kMaxRhs);
         d_lane_add = dalloc<int>(dev::kMaxRhs);
@@ -757,8 +764,9 @@ void GpuSolver::check_seg_err() {
 
 // Slice segments (staged.cuh) of the split operator for both precisions:
 // per 32-row slice a lower and an upper segment, each [uint16 row ends]
-// [int32 columns, padded to 4] [values, padded to 16 bytes], 16-byte aligned,
-// and one work item per slice in natural and in colour-sweep order.
+// [int32 columns] [values], every row padded to a multiple of four entries,
+// 16-byte aligned, and one work item per slice in natural and in
+// colour-sweep order.
 void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs,
                                const std::vector<int>& ecol, const std::vector<double>& eval) {
     const int ns = n_slices;
@@ -778,6 +786,9 @@ void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<
                 const int b = upper ? op_rs[row] : op_rp[row];
                 const int e = upper ? op_rp[row + 1] : op_rs[row];
                 for (int k = b; k < e; ++k) { cols.push_back(ecol[k]); vals.push_back((R)eval[k]); }
+                // pad the row to whole groups of four with zero entries on the
+                // row itself (a finite value times zero)
+                while (cols.size() % 4) { cols.push_back(row); vals.push_back((R)0); }
                 if (cols.size() > 65535) throw std::runtime_error("slice segment too large");
                 end[r] = (uint16_t)cols.size();
             }
