@@ -114,6 +114,8 @@ typedef struct m3d_params {
                                  with interleaved divergence correction like the adjoint (:778-888) */
     int row_kernels;          /* SpMV / SSOR row kernels: 0 CSR rows read by the lanes,
                                  1 32-row slices bulk-copied to shared memory */
+    int divcorr_precond;      /* divergence-correction PCG preconditioner: 0 Jacobi (the
+                                 reference's), 1 aggregation multigrid V-cycle */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -241,6 +243,10 @@ typedef struct m3d_kernel_times {
     long long launches[5];
     double ms[5];
     double bytes[5];
+    /* the same split by batch width: [class][K = 2, 4, 8, 16, other] */
+    long long launches_k[5][5];
+    double ms_k[5][5];
+    double bytes_k[5][5];
 } m3d_kernel_times;
 
 int m3d_set_kernel_timing(m3d_solver* s, int on);   /* also resets the totals */

@@ -25,6 +25,7 @@ class Params(C.Structure):
         ("print_level", C.c_int),
         ("forward_interleaved", C.c_int),
         ("row_kernels", C.c_int),
+        ("divcorr_precond", C.c_int),
     ]
 
 
@@ -54,6 +55,9 @@ class KernelTimes(C.Structure):
         ("launches", C.c_longlong * 5),
         ("ms", C.c_double * 5),
         ("bytes", C.c_double * 5),
+        ("launches_k", (C.c_longlong * 5) * 5),
+        ("ms_k", (C.c_double * 5) * 5),
+        ("bytes_k", (C.c_double * 5) * 5),
     ]
 
 

@@ -44,9 +44,10 @@ cudaEvent_t KernelTimer::get() {
     return e;
 }
 
-int KernelTimer::begin(int cls, double algorithmic_bytes) {
+int KernelTimer::begin(int cls, double algorithmic_bytes, int K) {
     if (!on) return -1;
-    Pair p{cls, get(), get(), algorithmic_bytes};
+    const int kb = K == 2 ? 0 : K == 4 ? 1 : K == 8 ? 2 : K == 16 ? 3 : 4;
+    Pair p{cls, kb, get(), get(), algorithmic_bytes};
     cudaEventRecord(p.a, stream);
     open.push_back(p);
     return (int)open.size() - 1;
@@ -66,6 +67,9 @@ void KernelTimer::collect() {
             ms[p.cls] += t;
             bytes[p.cls] += p.bytes;
             launches[p.cls] += 1;
+            ms_k[p.cls][p.kb] += t;
+            bytes_k[p.cls][p.kb] += p.bytes;
+            launches_k[p.cls][p.kb] += 1;
         }
         pool.push_back(p.a);
         pool.push_back(p.b);
@@ -76,7 +80,10 @@ void KernelTimer::collect() {
 
 void KernelTimer::reset() {
     collect();
-    for (int i = 0; i < kNumCls; ++i) { launches[i] = 0; ms[i] = 0; bytes[i] = 0; }
+    for (int i = 0; i < kNumCls; ++i) {
+        launches[i] = 0; ms[i] = 0; bytes[i] = 0;
+        for (int j = 0; j < kNumKBins; ++j) { launches_k[i][j] = 0; ms_k[i][j] = 0; bytes_k[i][j] = 0; }
+    }
 }
 
 KernelTimer::~KernelTimer() {
@@ -340,129 +347,6 @@ __global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D,
 // Slice-staged row kernels (segments of staged.cuh in shared memory).
 // ---------------------------------------------------------------------------
 
-// Threads per block of the staged kernels and passes over a 32-row slice:
-// K lanes per row, so a slice is 32 K lane-rows; up to 256 threads per block.
-template <int K> struct StagedShape {
-    static constexpr int NT = (32 * K < 256) ? 32 * K : 256;
-    static constexpr int PASSES = 32 * K / NT;
-    static constexpr int ROWS_PER_PASS = 32 / PASSES;
-};
-
-// Persistent slice pipeline of one block: work items i = blockIdx.x,
-// blockIdx.x + gridDim.x, ... < n_items; item i's lower (PARTS & 1) and upper
-// (PARTS & 2) segments are bulk-copied into stage k & 1 one item ahead of
-// use, so the next slice's matrix stream is in flight while body() runs.
-// Every wait is bounded: on a timeout the block sets kErrCopyTimeout in *err,
-// skips the stage, waits (bounded) for its copy in flight and stops.
-template <int PARTS, class Body>
-__device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__ seg, const int4* __restrict__ work,
-                                               long n_items, int stage_bytes, unsigned* err, Body body) {
-    extern __shared__ __align__(128) unsigned char dsm[];
-    __shared__ __align__(8) uint64_t bar[2];
-    __shared__ int4 wk[2];
-    __shared__ int abort_flag;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-        fence_mbar_init();
-        abort_flag = 0;
-    }
-    __syncthreads();
-    auto issue = [&](long i, int stg) {   // thread 0 only
-        const int4 w = __ldg(&work[i]);
-        wk[stg] = w;
-        const SegItem it = unpack(w);
-        unsigned bytes = 0;
-        if (PARTS & 1) bytes += (unsigned)it.lo_len * 16u;
-        if (PARTS & 2) bytes += (unsigned)it.up_len * 16u;
-        unsigned char* dst = dsm + (size_t)stg * stage_bytes;
-        mbar_expect_tx(&bar[stg], bytes);
-        if (PARTS & 1) {
-            bulk_g2s(dst, seg + (size_t)it.lo_off * 16, (unsigned)it.lo_len * 16u, &bar[stg]);
-            dst += (size_t)it.lo_len * 16;
-        }
-        if (PARTS & 2) bulk_g2s(dst, seg + (size_t)it.up_off * 16, (unsigned)it.up_len * 16u, &bar[stg]);
-    };
-    long i = blockIdx.x;
-    if (threadIdx.x == 0 && i < n_items) issue(i, 0);
-    for (int k = 0; i < n_items; i += gridDim.x, ++k) {
-        const int stg = k & 1;
-        if (threadIdx.x == 0 && i + gridDim.x < n_items) {
-            fence_proxy_async_smem();
-            issue(i + gridDim.x, stg ^ 1);
-        }
-        const bool ok = mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
-        if (ok) {
-            body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
-        } else {
-            atomicOr(err, kErrCopyTimeout);
-            abort_flag = 1;
-        }
-        __syncthreads();
-        if (abort_flag) {
-            // never consume a stage that did not arrive; let the copy already
-            // issued for the next item land (bounded) before the block leaves
-            if (threadIdx.x == 0 && i + gridDim.x < n_items)
-                mbar_wait_bounded(&bar[stg ^ 1], (unsigned)((k + 1) >> 1) & 1u);
-            __syncthreads();
-            break;
-        }
-    }
-}
-
-// Four values of a staged row from shared memory.
-__device__ __forceinline__ void lds4(const float* p, float (&a)[4]) {
-    const float4 q = *reinterpret_cast<const float4*>(p);
-    a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
-}
-__device__ __forceinline__ void lds4(const double* p, double (&a)[4]) {
-    const double2 q0 = *reinterpret_cast<const double2*>(p);
-    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
-    a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
-}
-
-// s + sum over one staged row's entries [b, e) (b, e multiples of 4) of
-// a_j * v[c_j][rhs]: 16-byte shared-memory reads, eight gathers in flight,
-// sums in entry order.
-template <class R, int K>
-__device__ __forceinline__ cplx<R> seg_row_dot(const int* __restrict__ col, const R* __restrict__ val, int b, int e,
-                                               const cplx<R>* __restrict__ v, int rhs, cplx<R> s) {
-    using C = cplx<R>;
-    for (int k = b; k < e; k += 8) {
-        const bool two = k + 4 < e;
-        const int4 c0 = *reinterpret_cast<const int4*>(col + k);
-        R a0[4], a1[4] = {0, 0, 0, 0};
-        lds4(val + k, a0);
-        C x[8];
-        x[0] = v[(size_t)c0.x * K + rhs];
-        x[1] = v[(size_t)c0.y * K + rhs];
-        x[2] = v[(size_t)c0.z * K + rhs];
-        x[3] = v[(size_t)c0.w * K + rhs];
-        if (two) {
-            const int4 c1 = *reinterpret_cast<const int4*>(col + k + 4);
-            lds4(val + k + 4, a1);
-            x[4] = v[(size_t)c1.x * K + rhs];
-            x[5] = v[(size_t)c1.y * K + rhs];
-            x[6] = v[(size_t)c1.z * K + rhs];
-            x[7] = v[(size_t)c1.w * K + rhs];
-        } else {
-#pragma unroll
-            for (int u = 4; u < 8; ++u) x[u] = cm<R>(0, 0);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) { s.x += a0[u] * x[u].x; s.y += a0[u] * x[u].y; }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) { s.x += a1[u] * x[4 + u].x; s.y += a1[u] * x[4 + u].y; }
-    }
-    return s;
-}
-
-// Register cap of the staged kernels: 1024 resident threads per SM for
-// complex FP32, 768 for complex FP64 (twice the registers per gather).
-template <class R, int K> struct StagedMinBlocks {
-    static constexpr int v = (sizeof(R) == 8 ? 768 : 1024) / StagedShape<K>::NT;
-};
-
 // SpMV over slice-staged rows, same modes and reductions as k_spmv.
 template <class R, int K, int MODE>
 __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
@@ -495,9 +379,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
             const C xi = x[i];
             const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
             const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], x, rhs,
-                                          seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], x, rhs,
-                                                            cm<R>(0, 0)));
+            const C s = seg_row_dot_lu<R, K>(lo, up, lr, x, rhs);
             const C yv = cadd(s, cmul(d, xi));
             if (MODE == kSpmvPlain) {
                 y[i] = yv;
@@ -717,18 +599,6 @@ double matrix_bytes(const KrylovCtx<R>& c) {
     return (double)c.nnz * (sizeof(R) + 4) + 4.0 * ((double)c.n_rows + 1) + (double)c.n_rows * sizeof(cplx<R>);
 }
 
-// Launches one staged kernel: at most one resident wave of blocks (of
-// StagedShape<K>::NT threads with two stages of dynamic shared memory), no
-// more than there are work items, no more than `cap`.
-template <class F, class... Args>
-void launch_staged(F* kernel, int nt, int stage_bytes, long items, int cap, cudaStream_t st, Args... args) {
-    const int smem = 2 * stage_bytes;
-    if (smem > 48 * 1024)
-        cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    long g = std::min<long>((long)wave_grid(kernel, cap, nt, smem), std::max<long>(items, 1));
-    kernel<<<(int)g, nt, smem, st>>>(args...);
-}
-
 template <class R, int K>
 void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
                  cplx<R>* aux_out, BicgState* st) {
@@ -774,7 +644,7 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
     }
     const int streams = 2 + (aux ? 1 : 0) + (aux_out ? 1 : 0);
     const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
-                                            (double)c.n_rows * K * sizeof(cplx<R>) * streams) : -1;
+                                            (double)c.n_rows * K * sizeof(cplx<R>) * streams, K) : -1;
     const int cap = c.red.max_blocks;
     if (c.row_kernels == kRowsStaged) {
         spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st);
@@ -818,7 +688,7 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) 
     // whole apply: matrix once (lower forward, upper backward), vectors in,
     // y (written, read back), out
     const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) +
-                                            (double)c.n_rows * K * sizeof(cplx<R>) * 4) : -1;
+                                            (double)c.n_rows * K * sizeof(cplx<R>) * 4, K) : -1;
     if (c.row_kernels == kRowsStaged) {
         constexpr int NT = StagedShape<K>::NT;
         for (int col = 0; col < nc; ++col) {
@@ -860,19 +730,19 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     const long n = (long)c.n_pad * K;
     const int gv = c.grid_vec;
     const double vb = (double)c.n_rows * K * sizeof(cplx<R>);
-    int th = c.timer ? c.timer->begin(kClsVec, 4 * vb) : -1;
+    int th = c.timer ? c.timer->begin(kClsVec, 4 * vb, K) : -1;
     k_update_p<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.p, v.v, st);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.p, v.y, v.ph);
     spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
-    th = c.timer ? c.timer->begin(kClsVec, 3 * vb) : -1;
+    th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
     k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.s, v.y, v.sh);
     spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
-    th = c.timer ? c.timer->begin(kClsVec, 8 * vb) : -1;
+    th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
     k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);

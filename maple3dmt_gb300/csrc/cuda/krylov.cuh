@@ -76,13 +76,17 @@ struct KernelTimer {
     bool on = false;
     cudaStream_t stream = nullptr;
     std::vector<cudaEvent_t> pool;
-    struct Pair { int cls; cudaEvent_t a, b; double bytes; };
+    struct Pair { int cls; int kb; cudaEvent_t a, b; double bytes; };
     std::vector<Pair> open;
     long long launches[kNumCls] = {0, 0, 0, 0, 0};
     double ms[kNumCls] = {0, 0, 0, 0, 0};
     double bytes[kNumCls] = {0, 0, 0, 0, 0};
+    static constexpr int kNumKBins = 5;   // K = 2, 4, 8, 16, other
+    long long launches_k[kNumCls][kNumKBins] = {};
+    double ms_k[kNumCls][kNumKBins] = {};
+    double bytes_k[kNumCls][kNumKBins] = {};
     cudaEvent_t get();
-    int begin(int cls, double algorithmic_bytes);   // returns handle or -1
+    int begin(int cls, double algorithmic_bytes, int K = 0);   // returns handle or -1
     void end(int handle);
     void collect();   // synchronises and folds finished pairs into the totals
     void reset();

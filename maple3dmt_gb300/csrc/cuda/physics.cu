@@ -1,7 +1,9 @@
 // Non-Krylov kernels of the solve path.  See physics.cuh for the reference
 // code each launcher restates.
 #include "physics.cuh"
+#include "staged.cuh"
 
+#include <algorithm>
 #include <stdexcept>
 #include <vector>
 
@@ -177,7 +179,10 @@ __global__ void k_dc_lap(MeshDev m, const double* __restrict__ me, DcWork w) {
     if (m.node_bc[v]) {
         w.lap_diag[v] = 1.0;
         w.jac_inv[v] = 1.0;
-        for (int q = a; q < b; ++q) w.lap_off[q] = 0.0;
+        for (int q = a; q < b; ++q) {
+            w.lap_off[q] = 0.0;
+            reinterpret_cast<double*>(w.lap_seg)[w.lap_qpos[q]] = 0.0;
+        }
         return;
     }
     double diag = 0.0;
@@ -193,6 +198,7 @@ __global__ void k_dc_lap(MeshDev m, const double* __restrict__ me, DcWork w) {
             if (!m.node_bc[m.inc_other[q]]) off = gv * we * gw;
         }
         w.lap_off[q] = off;
+        reinterpret_cast<double*>(w.lap_seg)[w.lap_qpos[q]] = off;
     }
     w.lap_diag[v] = diag;
     // Jacobi preconditioner z = r / diag (r where the diagonal is absent or
@@ -302,42 +308,41 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_init(int nn, DcWork w, RedScra
     }
 }
 
-// Ap = L p, (p, Ap) -> alpha   (forward_solver_fv.cpp:681-692)
+// Ap = L p, (p, Ap) -> alpha   (forward_solver_fv.cpp:681-692), over
+// 32-node slice segments of L's off-diagonal part staged in shared memory by
+// bulk copies (staged.cuh): off-diagonal sum, then the diagonal term.
+// Right-hand sides whose PCG has stopped do no work.
 template <int K>
-__global__ void __launch_bounds__(kBlock) k_dc_cg_ap(MeshDev m, DcWork w, RedScratch rs) {
-    const long n = (long)m.nn * K;
-    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long stride = (long)gridDim.x * blockDim.x;
-    const int k = (int)(i0 % K);
-    const bool run = w.st[k].cg_run;
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<double, K>::v)
+    k_dc_cg_ap_st(int nn, DcWork w, RedScratch rs) {
+    using Sh = StagedShape<K>;
+    constexpr int RPW = 32 / K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const bool run = w.st[rhs].cg_run;
     double2 acc[1] = {zero2()};
-    for (long i = i0; i < n && run; i += stride) {
-        const int v = (int)(i / K);
-        const double2 pv = w.p[i];
-        double2 s = make_double2(w.lap_diag[v] * pv.x, w.lap_diag[v] * pv.y);
-        const int q0 = __ldg(&m.inc_ptr[v]), q1 = __ldg(&m.inc_ptr[v + 1]);
-        // eight incidences per round, all gathers in flight before the sums
-        for (int q = q0; q < q1; q += 8) {
-            double a[8];
-            double2 pw[8];
+    slice_pipeline<1>(w.lap_seg, w.lap_work, w.n_node_slices, w.lap_stage, w.seg_err,
+                      [&](const SegItem& it, const unsigned char* base) {
+        SegRows<double> L;
+        L.bind(base);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const bool ok = q + u < q1;
-                const int o = ok ? __ldg(&m.inc_other[q + u]) : 0;
-                a[u] = ok ? __ldg(&w.lap_off[q + u]) : 0.0;
-                pw[u] = ok ? w.p[(size_t)o * K + k] : zero2();
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                s.x += a[u] * pw[u].x;
-                s.y += a[u] * pw[u].y;
-            }
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int v = it.slice * kSlice + lr;
+            if (v >= nn || !run) continue;
+            const size_t i = (size_t)v * K + rhs;
+            const double2 pv = w.p[i];
+            const double dg = w.lap_diag[v];
+            double2 s = seg_row_dot<double, K>(L.col, L.val, L.begin_of(lr), L.end[lr], w.p, rhs, zero2());
+            s.x += dg * pv.x;
+            s.y += dg * pv.y;
+            w.Ap[i] = s;
+            acc[0].x += pv.x * s.x + pv.y * s.y;
         }
-        w.Ap[i] = s;
-        acc[0].x += pv.x * s.x + pv.y * s.y;
-    }
+    });
     __shared__ double2 out[K];
-    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
+    if (grid_reduce_lanes<1, K, Sh::NT>(acc, rs, out)) {
         if (threadIdx.x < K) {
             DcState S = w.st[threadIdx.x];
             if (S.cg_run) {
@@ -415,6 +420,313 @@ __global__ void __launch_bounds__(kBlock) k_dc_cg_p(int nn, DcWork w) {
         pv.y = z.y + be * pv.y;
         w.p[i] = pv;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid-preconditioned PCG (AmgDev).  Same recurrence as the Jacobi PCG
+// above with z = M^-1 r from one V-cycle: one damped-Jacobi pre-smoothing
+// step from zero, residual, restriction to the aggregates, the coarse
+// correction, prolongation, one damped-Jacobi post-smoothing step -- a
+// symmetric positive-definite preconditioner, so CG's recurrence and its
+// stopping rule (|r| < 1e-10 |divJ|) are unchanged.
+// ---------------------------------------------------------------------------
+
+// phi = 0, r = divJ   (forward_solver_fv.cpp:668-679 without the Jacobi step)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_cg_init(int nn, DcWork w) {
+    const long n = (long)nn * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        if (!w.st[i % K].cg_run) continue;
+        w.phi[i] = zero2();
+        w.r[i] = w.divJ[i];
+    }
+}
+
+// phi += alpha p, r -= alpha Ap, |r| test   (:693-704)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_cg_update(int nn, int cg_max, DcWork w, RedScratch rs) {
+    const long n = (long)nn * K;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const DcState S0 = w.st[i0 % K];
+    const bool run = S0.cg_run;
+    const double al = S0.alpha.x;
+    double2 acc[1] = {zero2()};
+    for (long i = i0; i < n && run; i += stride) {
+        const double2 pv = w.p[i], apv = w.Ap[i];
+        double2 ph = w.phi[i];
+        ph.x += al * pv.x;
+        ph.y += al * pv.y;
+        w.phi[i] = ph;
+        double2 r = w.r[i];
+        r.x -= al * apv.x;
+        r.y -= al * apv.y;
+        w.r[i] = r;
+        acc[0].x += r.x * r.x + r.y * r.y;
+    }
+    __shared__ double2 out[K];
+    if (grid_reduce_lanes<1, K>(acc, rs, out)) {
+        if (threadIdx.x < K) {
+            DcState S = w.st[threadIdx.x];
+            if (S.cg_run) {
+                S.rn = out[threadIdx.x].x;
+                S.cg_iter += 1;
+                if (sqrt(S.rn) < 1e-10 * S.dn || S.cg_iter >= cg_max) S.cg_run = 0;
+            }
+            w.st[threadIdx.x] = S;
+        }
+    }
+}
+
+// x = omega dinv b   (pre-smoothing from a zero iterate)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_pre(AmgLevelDev L, const double2* __restrict__ b,
+                                                   double2* __restrict__ x, double omega, const DcState* st) {
+    const long n = (long)L.n * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        if (!st[i % K].cg_run) continue;
+        const double s = omega * L.dinv[i / K];
+        const double2 bv = b[i];
+        x[i] = make_double2(s * bv.x, s * bv.y);
+    }
+}
+
+// (A_l x)_i for one row of a CSR level (levels >= 1), eight gathers in flight
+template <int K>
+__device__ __forceinline__ double2 mg_row(const AmgLevelDev& L, int row, const double2* __restrict__ x, int k) {
+    double2 s = zero2();
+    const int q0 = __ldg(&L.ptr[row]), q1 = __ldg(&L.ptr[row + 1]);
+    for (int q = q0; q < q1; q += 8) {
+        double a[8];
+        double2 xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const bool ok = q + u < q1;
+            const int c = ok ? __ldg(&L.col[q + u]) : 0;
+            a[u] = ok ? __ldg(&L.val[q + u]) : 0.0;
+            xv[u] = ok ? x[(size_t)c * K + k] : zero2();
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            s.x += a[u] * xv[u].x;
+            s.y += a[u] * xv[u].y;
+        }
+    }
+    return s;
+}
+
+// r = b - A_l x   (levels >= 1)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_resid(AmgLevelDev L, const DcState* st) {
+    const long n = (long)L.n * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % K);
+        if (!st[k].cg_run) continue;
+        const double2 ax = mg_row<K>(L, (int)(i / K), L.x, k);
+        const double2 bv = L.b[i];
+        L.r[i] = make_double2(bv.x - ax.x, bv.y - ax.y);
+    }
+}
+
+// y = x + omega dinv (b - A_l x)   (post-smoothing, levels >= 1)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_post(AmgLevelDev L, double omega, const DcState* st) {
+    const long n = (long)L.n * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % K);
+        if (!st[k].cg_run) continue;
+        const int row = (int)(i / K);
+        const double2 ax = mg_row<K>(L, row, L.x, k);
+        const double2 bv = L.b[i], xv = L.x[i];
+        const double s = omega * L.dinv[row];
+        L.y[i] = make_double2(xv.x + s * (bv.x - ax.x), xv.y + s * (bv.y - ax.y));
+    }
+}
+
+// b_next[I] = sum over the members i of aggregate I of r[i]
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_restrict(AmgLevelDev L, int n_next, const double2* __restrict__ r,
+                                                        double2* __restrict__ b_next, const DcState* st) {
+    const long n = (long)n_next * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % K);
+        if (!st[k].cg_run) continue;
+        const int I = (int)(i / K);
+        double2 s = zero2();
+        for (int q = L.rptr[I]; q < L.rptr[I + 1]; ++q) {
+            const double2 v = r[(size_t)L.rcol[q] * K + k];
+            s.x += v.x;
+            s.y += v.y;
+        }
+        b_next[i] = s;
+    }
+}
+
+// x[i] += x_next[agg[i]]
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_prolong(AmgLevelDev L, const double2* __restrict__ x_next,
+                                                       double2* __restrict__ x, const DcState* st) {
+    const long n = (long)L.n * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % K);
+        if (!st[k].cg_run) continue;
+        const int a = L.agg[i / K];
+        if (a < 0) continue;
+        const double2 v = x_next[(size_t)a * K + k];
+        double2 xv = x[i];
+        xv.x += v.x;
+        xv.y += v.y;
+        x[i] = xv;
+    }
+}
+
+// coarsest level: x = A_c^-1 b (dense)
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_mg_coarse(int nc, const double* __restrict__ inv,
+                                                      const double2* __restrict__ b, double2* __restrict__ x,
+                                                      const DcState* st) {
+    const long n = (long)nc * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % K);
+        if (!st[k].cg_run) continue;
+        const int row = (int)(i / K);
+        double2 s = zero2();
+        for (int j = 0; j < nc; ++j) {
+            const double a = __ldg(&inv[(size_t)row * nc + j]);
+            const double2 v = b[(size_t)j * K + k];
+            s.x += a * v.x;
+            s.y += a * v.y;
+        }
+        x[i] = s;
+    }
+}
+
+// Level-0 residual r0 = b - L x over the node slice segments.
+template <int K>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<double, K>::v)
+    k_mg0_resid_st(int nn, DcWork w, const double2* __restrict__ b, const double2* __restrict__ x,
+                   double2* __restrict__ r) {
+    using Sh = StagedShape<K>;
+    constexpr int RPW = 32 / K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const bool run = w.st[rhs].cg_run;
+    slice_pipeline<1>(w.lap_seg, w.lap_work, w.n_node_slices, w.lap_stage, w.seg_err,
+                      [&](const SegItem& it, const unsigned char* base) {
+        SegRows<double> L;
+        L.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int v = it.slice * kSlice + lr;
+            if (v >= nn || !run) continue;
+            const size_t i = (size_t)v * K + rhs;
+            const double2 xv = x[i], bv = b[i];
+            const double dg = w.lap_diag[v];
+            double2 s = seg_row_dot<double, K>(L.col, L.val, L.begin_of(lr), L.end[lr], x, rhs, zero2());
+            s.x += dg * xv.x;
+            s.y += dg * xv.y;
+            r[i] = make_double2(bv.x - s.x, bv.y - s.y);
+        }
+    });
+}
+
+// Level-0 post-smoothing z = x + omega dinv (r - L x), then (r, z) -> beta
+// (:705-710): the last kernel of the preconditioner application.
+template <int K>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<double, K>::v)
+    k_mg0_post_st(int nn, DcWork w, const double* __restrict__ dinv, double omega, const double2* __restrict__ x,
+                  RedScratch rs) {
+    using Sh = StagedShape<K>;
+    constexpr int RPW = 32 / K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const bool run = w.st[rhs].cg_run;
+    double2 acc[1] = {zero2()};
+    slice_pipeline<1>(w.lap_seg, w.lap_work, w.n_node_slices, w.lap_stage, w.seg_err,
+                      [&](const SegItem& it, const unsigned char* base) {
+        SegRows<double> L;
+        L.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int v = it.slice * kSlice + lr;
+            if (v >= nn || !run) continue;
+            const size_t i = (size_t)v * K + rhs;
+            const double2 xv = x[i], rv = w.r[i];
+            const double dg = w.lap_diag[v];
+            double2 s = seg_row_dot<double, K>(L.col, L.val, L.begin_of(lr), L.end[lr], x, rhs, zero2());
+            s.x += dg * xv.x;
+            s.y += dg * xv.y;
+            const double sc = omega * dinv[v];
+            const double2 z = make_double2(xv.x + sc * (rv.x - s.x), xv.y + sc * (rv.y - s.y));
+            w.z[i] = z;
+            acc[0].x += rv.x * z.x + rv.y * z.y;
+        }
+    });
+    __shared__ double2 out[K];
+    if (grid_reduce_lanes<1, K, Sh::NT>(acc, rs, out)) {
+        if (threadIdx.x < K) {
+            DcState S = w.st[threadIdx.x];
+            if (S.cg_run) {
+                const double rzn = out[threadIdx.x].x;
+                S.beta = make_double2(S.cg_iter == 0 ? 0.0 : rzn / (S.rz.x + 1e-30), 0.0);
+                S.rz = make_double2(rzn, 0.0);
+            }
+            w.st[threadIdx.x] = S;
+        }
+    }
+}
+
+// One V-cycle: z = M^-1 r for every running right-hand side.  Returns launches.
+template <int K>
+long long mg_apply(const MeshDev& m, DcWork w, const AmgDev& A, RedScratch red, int cap, cudaStream_t s) {
+    long long launches = 0;
+    auto grid = [&](long n) {
+        long g = (n + kBlock - 1) / kBlock;
+        return (int)std::max(1L, std::min(g, (long)8 * 152 * 4));
+    };
+    const int nl = A.n_levels;
+    // level 0: b = r; pre-smoothed iterate in lv[0].x
+    const AmgLevelDev& L0 = A.lv[0];
+    k_mg_pre<K><<<grid((long)m.nn * K), kBlock, 0, s>>>(L0, w.r, L0.x, A.omega, w.st);
+    ++launches;
+    if (nl > 1) {
+        launch_staged(k_mg0_resid_st<K>, StagedShape<K>::NT, w.lap_stage, w.n_node_slices, 1 << 20, s, m.nn, w,
+                      (const double2*)w.r, (const double2*)L0.x, L0.r);
+        k_mg_restrict<K><<<grid((long)A.lv[1].n * K), kBlock, 0, s>>>(L0, A.lv[1].n, L0.r, A.lv[1].b, w.st);
+        launches += 2;
+        // down
+        for (int l = 1; l < nl - 1; ++l) {
+            const AmgLevelDev& L = A.lv[l];
+            k_mg_pre<K><<<grid((long)L.n * K), kBlock, 0, s>>>(L, L.b, L.x, A.omega, w.st);
+            k_mg_resid<K><<<grid((long)L.n * K), kBlock, 0, s>>>(L, w.st);
+            k_mg_restrict<K><<<grid((long)A.lv[l + 1].n * K), kBlock, 0, s>>>(L, A.lv[l + 1].n, L.r, A.lv[l + 1].b,
+                                                                              w.st);
+            launches += 3;
+        }
+        // coarsest
+        const AmgLevelDev& C = A.lv[nl - 1];
+        k_mg_coarse<K><<<grid((long)C.n * K), kBlock, 0, s>>>(A.n_coarse, A.coarse_inv, C.b, C.x, w.st);
+        ++launches;
+        // up: prolong the finished iterate of level l+1 into level l, post-smooth
+        for (int l = nl - 2; l >= 1; --l) {
+            const AmgLevelDev& L = A.lv[l];
+            const double2* xn = (l + 1 == nl - 1) ? A.lv[l + 1].x : A.lv[l + 1].y;
+            k_mg_prolong<K><<<grid((long)L.n * K), kBlock, 0, s>>>(L, xn, L.x, w.st);
+            k_mg_post<K><<<grid((long)L.n * K), kBlock, 0, s>>>(L, A.omega, w.st);
+            launches += 2;
+        }
+        const double2* x1 = (nl - 1 == 1) ? A.lv[1].x : A.lv[1].y;
+        k_mg_prolong<K><<<grid((long)m.nn * K), kBlock, 0, s>>>(L0, x1, L0.x, w.st);
+        ++launches;
+    }
+    launch_staged(k_mg0_post_st<K>, StagedShape<K>::NT, w.lap_stage, w.n_node_slices, cap, s, m.nn, w, L0.dinv,
+                  A.omega, (const double2*)L0.x, red);
+    ++launches;
+    return launches;
 }
 
 // E -= G phi on edges that are not BC (:714-720), for rhs still in the outer loop
@@ -811,7 +1123,7 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
 template <int K>
 long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
                     double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
-                    DcCounters* counters) {
+                    DcCounters* counters, const AmgDev* amg) {
     if (counters) counters->calls += 1;
     long long launches = 0;
     std::vector<DcState> hs(K);
@@ -824,7 +1136,7 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
     cudaMemcpyAsync(w.st, hs.data(), sizeof(DcState) * K, cudaMemcpyHostToDevice, s);
     const int cap = red.max_blocks;
     const int g_divj = wave_grid(k_dc_divj<K>, cap), g_init = wave_grid(k_dc_cg_init<K>, cap);
-    const int g_ap = wave_grid(k_dc_cg_ap<K>, cap), g_up = wave_grid(k_dc_cg_update<K>, cap);
+    const int g_up = wave_grid(k_dc_cg_update<K>, cap);
     const int g_p = wave_grid(k_dc_cg_p<K>, 1 << 20);
     const int cg_max = m.nn > 500 ? m.nn : 500;
     const int ge = (int)(((long)m.n_pad * K + kBlock - 1) / kBlock);
@@ -836,17 +1148,33 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
         bool any = false;
         for (int k = 0; k < K; ++k) any |= (hs[k].active && !hs[k].done);
         if (!any) break;
-        k_dc_cg_init<K><<<g_init, kBlock, 0, s>>>(m.nn, w, red);
-        ck(); ++launches;
-        int chunk = cg_chunk;
+        if (amg) {
+            // z = M^-1 divJ, rz, p = z
+            k_mg_cg_init<K><<<g_p, kBlock, 0, s>>>(m.nn, w);
+            launches += 1 + mg_apply<K>(m, w, *amg, red, cap, s);
+            k_dc_cg_p<K><<<g_p, kBlock, 0, s>>>(m.nn, w);
+            ++launches;
+        } else {
+            k_dc_cg_init<K><<<g_init, kBlock, 0, s>>>(m.nn, w, red);
+            ++launches;
+        }
+        ck();
+        int chunk = amg ? std::max(1, cg_chunk / 4) : cg_chunk;
         int it = 0;
         for (; it < cg_max;) {
             const int n_it = (cg_max - it) < chunk ? (cg_max - it) : chunk;
             for (int j = 0; j < n_it; ++j) {
-                k_dc_cg_ap<K><<<g_ap, kBlock, 0, s>>>(m, w, red);
-                k_dc_cg_update<K><<<g_up, kBlock, 0, s>>>(m.nn, cg_max, w, red);
+                launch_staged(k_dc_cg_ap_st<K>, StagedShape<K>::NT, w.lap_stage, w.n_node_slices, cap, s, m.nn,
+                              w, red);
+                if (amg) {
+                    k_mg_cg_update<K><<<g_up, kBlock, 0, s>>>(m.nn, cg_max, w, red);
+                    launches += 2 + mg_apply<K>(m, w, *amg, red, cap, s);
+                } else {
+                    k_dc_cg_update<K><<<g_up, kBlock, 0, s>>>(m.nn, cg_max, w, red);
+                    launches += 2;
+                }
                 k_dc_cg_p<K><<<g_p, kBlock, 0, s>>>(m.nn, w);
-                launches += 3;
+                ++launches;
             }
             ck();
             it += n_it;
@@ -871,12 +1199,12 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
 
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
                   double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
-                  DcCounters* counters) {
+                  DcCounters* counters, const AmgDev* amg) {
     switch (E.K) {
-        case 2: return divcorr_k<2>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
-        case 4: return divcorr_k<4>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
-        case 8: return divcorr_k<8>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
-        case 16: return divcorr_k<16>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters);
+        case 2: return divcorr_k<2>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
+        case 4: return divcorr_k<4>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
+        case 8: return divcorr_k<8>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
+        case 16: return divcorr_k<16>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
         default: throw std::runtime_error("divergence correction batch must be 2, 4, 8 or 16");
     }
 }

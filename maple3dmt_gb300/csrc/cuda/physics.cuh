@@ -129,6 +129,14 @@ struct DcWork {
     double* lap_off;    // [inc] off-diagonal per incidence entry (0 on BC rows / columns)
     double* jac_inv;    // [nn] inverse Jacobi diagonal (1 where L has no usable diagonal)
     DcState* st;        // [K]
+    // L's off-diagonal part as 32-node slice segments (staged.cuh format, FP64
+    // values, columns fixed per mesh, values rewritten with lap_off)
+    unsigned char* lap_seg;
+    const int4* lap_work;   // [n_node_slices]
+    const int* lap_qpos;    // [inc] index, in doubles into lap_seg, of incidence q's value
+    int lap_stage;          // bytes of the largest node segment
+    int n_node_slices;
+    unsigned* seg_err;
 };
 
 // Laplacian values for the current sigma (build_div_laplacian + Dirichlet rows/cols, :581-606).
@@ -139,9 +147,32 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
 // Returns the number of kernel launches. Iteration caps: outer <= max_outer,
 // PCG <= max(500, nn) per outer (the reference's caps).
 struct DcCounters { int calls = 0, outer = 0; long long cg_iterations = 0, cg_sweeps = 0; };
+// Multigrid V-cycle preconditioner of the node-Laplacian PCG (host setup in
+// host/amg.cpp).  Level 0 is L itself, applied through the node slice
+// segments of DcWork; levels 1.. are CSR Galerkin operators, linked by
+// piecewise-constant aggregation; the coarsest level is solved by a dense
+// inverse.  Work vectors are [n_l][K] complex.
+constexpr int kAmgMaxLevels = 8;
+struct AmgLevelDev {
+    int n;
+    const int *ptr, *col;          // A_l (levels >= 1)
+    const double* val;
+    const double* dinv;            // Jacobi smoother scale
+    const int* agg;                // [n] aggregate in level l+1 (-1: none)
+    const int *rptr, *rcol;        // members of each aggregate of level l+1
+    double2 *b, *x, *y, *r;        // right side, pre-smoothed iterate, post-smoothed iterate, residual
+};
+struct AmgDev {
+    int n_levels = 0;
+    AmgLevelDev lv[kAmgMaxLevels];
+    int n_coarse = 0;
+    const double* coarse_inv = nullptr;   // [n_coarse][n_coarse]
+    double omega = 2.0 / 3.0;             // smoother damping
+};
+
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w,
                   int max_outer, double tol, const int* active_host, dev::RedScratch red,
-                  cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr);
+                  cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr, const AmgDev* amg = nullptr);
 
 // ---- stations (forward_solver_fv.cpp:1490-1727, :1804-2065) ----
 // Z and H cache per (frequency f, station); E1 = rhs 2f, E2 = rhs 2f+1 of E.

@@ -18,6 +18,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -124,6 +126,184 @@ struct SegRows {
     }
     __device__ __forceinline__ int begin_of(int r) const { return r ? end[r - 1] : 0; }
 };
+
+
+// Threads per block of the staged kernels and passes over a 32-row slice:
+// K lanes per row, so a slice is 32 K lane-rows; up to 256 threads per block.
+template <int K> struct StagedShape {
+    static constexpr int NT = (32 * K < 256) ? 32 * K : 256;
+    static constexpr int PASSES = 32 * K / NT;
+    static constexpr int ROWS_PER_PASS = 32 / PASSES;
+};
+
+// Persistent slice pipeline of one block: work items i = blockIdx.x,
+// blockIdx.x + gridDim.x, ... < n_items; item i's lower (PARTS & 1) and upper
+// (PARTS & 2) segments are bulk-copied into stage k & 1 one item ahead of
+// use, so the next slice's matrix stream is in flight while body() runs.
+// Every wait is bounded: on a timeout the block sets kErrCopyTimeout in *err,
+// skips the stage, waits (bounded) for its copy in flight and stops.
+template <int PARTS, class Body>
+__device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__ seg, const int4* __restrict__ work,
+                                               long n_items, int stage_bytes, unsigned* err, Body body) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ int4 wk[2];
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+        abort_flag = 0;
+    }
+    __syncthreads();
+    auto issue = [&](long i, int stg) {   // thread 0 only
+        const int4 w = __ldg(&work[i]);
+        wk[stg] = w;
+        const SegItem it = unpack(w);
+        unsigned bytes = 0;
+        if (PARTS & 1) bytes += (unsigned)it.lo_len * 16u;
+        if (PARTS & 2) bytes += (unsigned)it.up_len * 16u;
+        unsigned char* dst = dsm + (size_t)stg * stage_bytes;
+        mbar_expect_tx(&bar[stg], bytes);
+        if (PARTS & 1) {
+            bulk_g2s(dst, seg + (size_t)it.lo_off * 16, (unsigned)it.lo_len * 16u, &bar[stg]);
+            dst += (size_t)it.lo_len * 16;
+        }
+        if (PARTS & 2) bulk_g2s(dst, seg + (size_t)it.up_off * 16, (unsigned)it.up_len * 16u, &bar[stg]);
+    };
+    long i = blockIdx.x;
+    if (threadIdx.x == 0 && i < n_items) issue(i, 0);
+    for (int k = 0; i < n_items; i += gridDim.x, ++k) {
+        const int stg = k & 1;
+        if (threadIdx.x == 0 && i + gridDim.x < n_items) {
+            fence_proxy_async_smem();
+            issue(i + gridDim.x, stg ^ 1);
+        }
+        const bool ok = mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
+        if (ok) {
+            body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
+        } else {
+            atomicOr(err, kErrCopyTimeout);
+            abort_flag = 1;
+        }
+        __syncthreads();
+        if (abort_flag) {
+            // never consume a stage that did not arrive; let the copy already
+            // issued for the next item land (bounded) before the block leaves
+            if (threadIdx.x == 0 && i + gridDim.x < n_items)
+                mbar_wait_bounded(&bar[stg ^ 1], (unsigned)((k + 1) >> 1) & 1u);
+            __syncthreads();
+            break;
+        }
+    }
+}
+
+// Four values of a staged row from shared memory.
+__device__ __forceinline__ void lds4(const float* p, float (&a)[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&a)[4]) {
+    const double2 q0 = *reinterpret_cast<const double2*>(p);
+    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+    a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
+}
+
+// s + sum over one staged row's entries [b, e) (b, e multiples of 4) of
+// a_j * v[c_j][rhs]: 16-byte shared-memory reads, eight gathers in flight,
+// sums in entry order.
+template <class R, int K>
+__device__ __forceinline__ cplx<R> seg_row_dot(const int* __restrict__ col, const R* __restrict__ val, int b, int e,
+                                               const cplx<R>* __restrict__ v, int rhs, cplx<R> s) {
+    using C = cplx<R>;
+    for (int k = b; k < e; k += 8) {
+        const bool two = k + 4 < e;
+        const int4 c0 = *reinterpret_cast<const int4*>(col + k);
+        R a0[4], a1[4] = {0, 0, 0, 0};
+        lds4(val + k, a0);
+        C x[8];
+        x[0] = v[(size_t)c0.x * K + rhs];
+        x[1] = v[(size_t)c0.y * K + rhs];
+        x[2] = v[(size_t)c0.z * K + rhs];
+        x[3] = v[(size_t)c0.w * K + rhs];
+        if (two) {
+            const int4 c1 = *reinterpret_cast<const int4*>(col + k + 4);
+            lds4(val + k + 4, a1);
+            x[4] = v[(size_t)c1.x * K + rhs];
+            x[5] = v[(size_t)c1.y * K + rhs];
+            x[6] = v[(size_t)c1.z * K + rhs];
+            x[7] = v[(size_t)c1.w * K + rhs];
+        } else {
+#pragma unroll
+            for (int u = 4; u < 8; ++u) x[u] = cm<R>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a0[u] * x[u].x; s.y += a0[u] * x[u].y; }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a1[u] * x[4 + u].x; s.y += a1[u] * x[4 + u].y; }
+    }
+    return s;
+}
+
+// Lower and upper parts of one staged row: the first (up to) eight entries of
+// each part are gathered in one round, longer rows continue part by part.
+template <class R, int K>
+__device__ __forceinline__ cplx<R> seg_row_dot_lu(const SegRows<R>& lo, const SegRows<R>& up, int r,
+                                                  const cplx<R>* __restrict__ v, int rhs) {
+    using C = cplx<R>;
+    const int bl = lo.begin_of(r), el = lo.end[r];
+    const int bu = up.begin_of(r), eu = up.end[r];
+    const bool on[4] = {bl < el, bl + 4 < el, bu < eu, bu + 4 < eu};
+    const int at[4] = {bl, bl + 4, bu, bu + 4};
+    R a[4][4];
+    C x[16];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) {
+        const SegRows<R>& P = g < 2 ? lo : up;
+        if (on[g]) {
+            const int4 c = *reinterpret_cast<const int4*>(P.col + at[g]);
+            lds4(P.val + at[g], a[g]);
+            x[4 * g + 0] = v[(size_t)c.x * K + rhs];
+            x[4 * g + 1] = v[(size_t)c.y * K + rhs];
+            x[4 * g + 2] = v[(size_t)c.z * K + rhs];
+            x[4 * g + 3] = v[(size_t)c.w * K + rhs];
+        } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { a[g][u] = (R)0; x[4 * g + u] = cm<R>(0, 0); }
+        }
+    }
+    C s = cm<R>(0, 0);
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a[g][u] * x[4 * g + u].x; s.y += a[g][u] * x[4 * g + u].y; }
+    if (bl + 8 < el) s = seg_row_dot<R, K>(lo.col, lo.val, bl + 8, el, v, rhs, s);
+#pragma unroll
+    for (int g = 2; g < 4; ++g)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { s.x += a[g][u] * x[4 * g + u].x; s.y += a[g][u] * x[4 * g + u].y; }
+    if (bu + 8 < eu) s = seg_row_dot<R, K>(up.col, up.val, bu + 8, eu, v, rhs, s);
+    return s;
+}
+
+// Register cap of the staged kernels: 768 resident threads per SM for
+// complex FP32, 512 for complex FP64 (sixteen gathers in flight per thread).
+template <class R, int K> struct StagedMinBlocks {
+    static constexpr int t = (sizeof(R) == 8 ? 512 : 768) / StagedShape<K>::NT;
+    static constexpr int v = t > 0 ? t : 1;
+};
+
+// Launches one staged kernel: at most one resident wave of blocks (of
+// StagedShape<K>::NT threads with two stages of dynamic shared memory), no
+// more than there are work items, no more than `cap`.
+template <class F, class... Args>
+inline void launch_staged(F* kernel, int nt, int stage_bytes, long items, int cap, cudaStream_t st, Args... args) {
+    const int smem = 2 * stage_bytes;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    long g = std::min<long>((long)wave_grid(kernel, cap, nt, smem), std::max<long>(items, 1));
+    kernel<<<(int)g, nt, smem, st>>>(args...);
+}
 
 }  // namespace dev
 }  // namespace m3d

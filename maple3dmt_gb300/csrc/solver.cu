@@ -2,6 +2,7 @@
 #include "solver.hpp"
 
 #include "cuda/dot.cuh"
+#include "host/amg.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -179,6 +180,9 @@ void GpuSolver::free_all() {
     dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
     dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_inv); dfree(dc.st);
+    dfree(dc.lap_seg); dfree(d_lap_work); dfree(d_lap_qpos);
+    free_amg();
+    dc.lap_work = nullptr; dc.lap_qpos = nullptr;
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
     dfree(d_host_stage); dfree(d_stage_real); dfree(d_states); dfree(d_states2);
@@ -381,6 +385,49 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     std::vector<int> cell_edge(L.cell_edge.size());
     for (size_t q = 0; q < cell_edge.size(); ++q) cell_edge[q] = iperm[L.cell_edge[q]];
 
+    // node Laplacian off-diagonal pattern as 32-node slice segments (values
+    // are written by k_dc_lap through lap_qpos at every conductivity update)
+    {
+        const int nsl = (nn + dev::kSlice - 1) / dev::kSlice;
+        std::vector<unsigned char> seg;
+        std::vector<int4> work(nsl);
+        std::vector<int> qpos(inc_other.size(), 0);
+        int stage = 0;
+        for (int sl = 0; sl < nsl; ++sl) {
+            const long off = (long)seg.size();
+            uint16_t end[dev::kSlice];
+            std::vector<int> cols;
+            std::vector<long> qs;   // incidence of each entry, -1 for padding
+            for (int r = 0; r < dev::kSlice; ++r) {
+                const int v = sl * dev::kSlice + r;
+                if (v < nn)
+                    for (int q = inc_ptr[v]; q < inc_ptr[v + 1]; ++q) { cols.push_back(inc_other[q]); qs.push_back(q); }
+                while (cols.size() % 4) { cols.push_back(v); qs.push_back(-1); }
+                if (cols.size() > 65535) throw std::runtime_error("node slice segment too large");
+                end[r] = (uint16_t)cols.size();
+            }
+            const size_t n = cols.size();
+            const size_t bytes = dev::kSegHeader + 4 * n + 8 * n;
+            seg.resize(off + bytes, 0);
+            std::memcpy(seg.data() + off, end, sizeof(end));
+            std::memcpy(seg.data() + off + dev::kSegHeader, cols.data(), 4 * n);
+            const long vbase = (off + dev::kSegHeader + 4 * (long)n) / 8;
+            for (size_t j = 0; j < n; ++j)
+                if (qs[j] >= 0) qpos[qs[j]] = (int)(vbase + (long)j);
+            if (off / 16 > 2000000000L || (long)(bytes / 16) > 65535) throw std::runtime_error("node segment too large");
+            work[sl] = make_int4(sl, (int)(off / 16), 0, (int)((bytes / 16) << 16));
+            stage = std::max(stage, (int)bytes);
+        }
+        if (seg.size() / 8 > 2000000000UL) throw std::runtime_error("node segments too large");
+        dc.lap_seg = dupload(seg, stream);
+        dc.lap_work = d_lap_work = dupload(work, stream);
+        dc.lap_qpos = d_lap_qpos = dupload(qpos, stream);
+        dc.lap_stage = stage;
+        dc.n_node_slices = nsl;
+    }
+    h_inc_ptr = inc_ptr;
+    h_inc_other = inc_other;
+
     // upload
     md.ne = ne; md.n_pad = n_pad; md.nc = L.nc; md.nn = nn; md.n_slices = n_slices;
     md.perm = dupload(perm, stream); md.iperm = dupload(iperm, stream);
@@ -538,8 +585,7 @@ void GpuSolver::ensure_dc(int K) {
     if (dc_K >= K) return;
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
     const size_t n = (size_t)L.nn * K;
-    dc.divJ = dalloc<double2>(n); dc.phi = dalloc<double2>(n); dc.r = dalloc<double2>(n);
-    dc.z = dalloc<double2>(n); dc.p = dalloc<double2>(n); dc.Ap = dalloc<double2>(n); dc.phi0 = dalloc<double2>(n);
+    for (double2** q : {&dc.divJ, &dc.phi, &dc.r, &dc.z, &dc.p, &dc.Ap, &dc.phi0}) *q = dalloc_zero<double2>(n, stream);
     dc_K = K;
 }
 
@@ -560,7 +606,88 @@ void GpuSolver::ensure_sigma_device() {
         phys::dc_build_laplacian(md, d_me_dc, dc, stream);
         ++launches;
         lap_built = true;
+        if (P.divcorr_precond == 1) build_amg();
     }
+}
+
+void GpuSolver::free_amg() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : amg_mem) cudaFree(p);
+    amg_mem.clear();
+    amg = phys::AmgDev{};
+    amg_ok = false;
+}
+
+// Aggregation multigrid hierarchy of the node Laplacian just built on the
+// device (host setup, host/amg.cpp); falls back to the Jacobi PCG when the
+// coarsening does not reach a small coarse level.
+void GpuSolver::build_amg() {
+    free_amg();
+    const int nn = L.nn;
+    std::vector<double> diag(nn), off(h_inc_other.size());
+    cuda_ok(cudaMemcpyAsync(diag.data(), dc.lap_diag, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream), "lap");
+    cuda_ok(cudaMemcpyAsync(off.data(), dc.lap_off, sizeof(double) * off.size(), cudaMemcpyDeviceToHost, stream),
+            "lap");
+    sync();
+    CsrReal A0;
+    A0.n_rows = A0.n_cols = nn;
+    A0.ptr.assign(nn + 1, 0);
+    for (int v = 0; v < nn; ++v) {
+        for (int q = h_inc_ptr[v]; q < h_inc_ptr[v + 1]; ++q)
+            if (off[q] != 0.0) { A0.col.push_back(h_inc_other[q]); A0.val.push_back(off[q]); }
+        A0.col.push_back(v);
+        A0.val.push_back(diag[v]);
+        A0.ptr[v + 1] = (int)A0.col.size();
+    }
+    AmgOptions opt;
+    opt.omega_p = 0.0;   // piecewise-constant prolongation (the kernels assume it)
+    AmgHierarchy H;
+    try {
+        amg_build(A0, opt, H);
+    } catch (const std::exception&) {
+        return;   // Jacobi PCG
+    }
+    const int nl = (int)H.levels.size();
+    // a single level (tiny meshes) or a large coarse level: keep the Jacobi PCG
+    if (nl < 2 || nl > phys::kAmgMaxLevels || H.n_coarse > 2048) return;
+    auto up = [&](const auto& v) {
+        auto* p = dupload(v, stream);
+        amg_mem.push_back((void*)p);
+        return p;
+    };
+    auto zeros = [&](size_t n) {
+        double2* p = dalloc_zero<double2>(n, stream);
+        amg_mem.push_back((void*)p);
+        return p;
+    };
+    amg.n_levels = nl;
+    for (int l = 0; l < nl; ++l) {
+        const AmgLevel& Lv = H.levels[l];
+        phys::AmgLevelDev& d = amg.lv[l];
+        d.n = Lv.A.n_rows;
+        if (l > 0) {
+            d.ptr = up(Lv.A.ptr);
+            d.col = up(Lv.A.col);
+            d.val = up(Lv.A.val);
+        }
+        d.dinv = up(Lv.dinv);
+        if (l + 1 < nl) {
+            std::vector<int> agg(d.n, -1);
+            for (int i = 0; i < d.n; ++i)
+                if (Lv.P.ptr[i + 1] > Lv.P.ptr[i]) agg[i] = Lv.P.col[Lv.P.ptr[i]];
+            d.agg = up(agg);
+            d.rptr = up(Lv.R.ptr);
+            d.rcol = up(Lv.R.col);
+        }
+        const size_t n = (size_t)d.n * dev::kMaxRhs;
+        d.b = zeros(n);
+        d.x = zeros(n);
+        d.y = zeros(n);
+        d.r = zeros(n);
+    }
+    amg.n_coarse = H.n_coarse;
+    amg.coarse_inv = up(H.coarse_inv);
+    amg_ok = true;
 }
 
 KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
@@ -830,6 +957,7 @@ void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<
     cuda_ok(cudaMemsetAsync(d_seg_err, 0, sizeof(unsigned), stream), "memset");
     seg64 = dev::SegView<double>{d_seg64, d_work64, d_work64 + ns, s64, l64, u64, d_seg_err};
     seg32 = dev::SegView<float>{d_seg32, d_work32, d_work32 + ns, s32, l32, u32, d_seg_err};
+    dc.seg_err = d_seg_err;
 }
 
 // Mixed precision: each step computes r = b - A x in FP64, solves A d = r
@@ -1054,9 +1182,9 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
     launches += 2;
     if (P.div_correction) {
         ensure_dc(K);
-        const int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
+        const int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
         launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
-                                  red, stream, 25, &dcc);
+                                  red, stream, 25, &dcc, amg_or_null());
         timer.end(th);
     }
     phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
@@ -1131,9 +1259,9 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
     ensure_vecs(K);
     phys::dc_phi0(md, VecK{rhs, K}, info, dc, stream);
     ++launches;
-    int th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
+    int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
     launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                              active.data(), red, stream, 25, &dcc);
+                              active.data(), red, stream, 25, &dcc, amg_or_null());
     timer.end(th);
     std::vector<int> done(K, 0);
     std::vector<double> prev(K, 1e30);
@@ -1164,9 +1292,9 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
         bool anyd = false;
         for (int k = 0; k < K; ++k) anyd |= dca[k] != 0;
         if (!anyd) break;
-        th = timer.on ? timer.begin(kClsDivcorr, 0.0) : -1;
+        th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
         launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                                  dca.data(), red, stream, 25, &dcc);
+                                  dca.data(), red, stream, 25, &dcc, amg_or_null());
         timer.end(th);
         std::vector<BicgState> hs(K);
         for (int k = 0; k < K; ++k) {

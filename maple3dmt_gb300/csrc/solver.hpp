@@ -93,6 +93,16 @@ private:
     dev::SegView<double> seg64{};
     dev::SegView<float> seg32{};
     unsigned* d_seg_err = nullptr;
+    int4* d_lap_work = nullptr;   // node-Laplacian slice work items (dc.lap_work)
+    // multigrid preconditioner of the divergence-correction PCG (rebuilt per sigma)
+    std::vector<int> h_inc_ptr, h_inc_other;
+    phys::AmgDev amg{};
+    bool amg_ok = false;
+    std::vector<void*> amg_mem;
+    void build_amg();
+    void free_amg();
+    const phys::AmgDev* amg_or_null() const { return (amg_ok && P.divcorr_precond == 1) ? &amg : nullptr; }
+    int* d_lap_qpos = nullptr;    // incidence -> value slot in dc.lap_seg
     void build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs, const std::vector<int>& ecol,
                         const std::vector<double>& eval);
     void check_seg_err();

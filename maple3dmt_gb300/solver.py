@@ -201,7 +201,10 @@ class ForwardSolverFV:
     def kernel_times(self) -> dict:
         t = KernelTimes()
         self._ck(self.lib.m3d_get_kernel_times(self.h, C.byref(t)))
-        return {name: dict(launches=t.launches[i], ms=t.ms[i], bytes=t.bytes[i])
+        kb = ("K2", "K4", "K8", "K16", "other")
+        return {name: dict(launches=t.launches[i], ms=t.ms[i], bytes=t.bytes[i],
+                           by_k={kb[j]: dict(launches=t.launches_k[i][j], ms=t.ms_k[i][j], bytes=t.bytes_k[i][j])
+                                 for j in range(5) if t.launches_k[i][j]})
                 for i, name in enumerate(KERNEL_CLASSES)}
 
     def stats(self) -> dict:

@@ -121,10 +121,14 @@ def test_jv_pieces_match_oracle(g_small):
         assert rel(s.extract_delta_impedance_complex(xo, pol), o.delta_impedance(xo, pol)) < 1e-8
 
 
+@pytest.mark.parametrize("divcorr_precond", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_gradient_batch_matches_reference(g_small, precision):
+def test_gradient_batch_matches_reference(g_small, precision, divcorr_precond):
+    """Against the reference's own outputs; both PCG preconditioners of the
+    divergence correction (Jacobi as the reference, aggregation multigrid)
+    stop at the same 1e-10 relative residual."""
     g = g_small
-    s = _gpu(g, precision=precision, forward_interleaved=1)
+    s = _gpu(g, precision=precision, forward_interleaved=1, divcorr_precond=divcorr_precond)
     Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
     ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
     assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
@@ -183,6 +187,25 @@ def test_c2_scale_true_residual(lib):
     assert s.ne == 1687305
     assert np.isfinite(Z).all()
     assert all(t <= 1e-7 for t in st["true_residual"][:4]), st
+
+
+def test_c2_scale_divcorr_preconditioners_agree(lib):
+    """Full-size mesh, the two lowest frequencies (the most divergence
+    correction): impedances with the multigrid-preconditioned PCG agree with
+    the Jacobi PCG (the reference's) to 1e-5 relative -- both solves stop at
+    the 1e-7 true residual, so Z differs at the solve tolerance, not more."""
+    from maple3dmt_gb300 import mesh
+    from maple3dmt_gb300.solver import solver_for_survey
+    sv = mesh.layered_block_survey(min_level=6)
+    Zs = []
+    for pc in (0, 1):
+        s = solver_for_survey(sv, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1, forward_interleaved=1,
+                              divcorr_precond=pc)
+        Zs.append(s.forward_batch(sv.freqs[:2]))
+        st = s.stats()
+        assert all(t <= 1e-7 for t in st["true_residual"][:4]), st
+        s.close()
+    assert rel(Zs[1], Zs[0]) < 1e-5
 
 
 @pytest.mark.parametrize("K", [1, 2, 4, 8, 16])
