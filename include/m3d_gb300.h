@@ -122,7 +122,7 @@ typedef struct m3d_solver m3d_solver;
 
 /* Counters of the last solving call (all right-hand sides of that call). */
 typedef struct m3d_stats {
-    int n_rhs;
+    int n_rhs;                 /* m3d_gradient_batch: forward then adjoint RHS of each frequency group */
     int iterations[64];        /* Krylov iterations per RHS (first 64) */
     int status[64];            /* M3D_SOLVE_* per RHS */
     double true_residual[64];  /* ||b - A x||_2 / ||b||_2 in FP64, before divergence correction */
@@ -136,6 +136,7 @@ typedef struct m3d_stats {
     long long forward_iterations;     /* Krylov iterations of the forward phase, summed over rhs */
     long long adjoint_iterations;     /* ... of the adjoint phase */
     long long divcorr_cg_sweeps;      /* batched PCG iterations run (each serves every rhs of a batch) */
+    double divcorr_setup_ms;          /* host time of the last multigrid setup of the PCG */
 } m3d_stats;
 
 void m3d_params_default(m3d_params* p);

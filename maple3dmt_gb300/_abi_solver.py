@@ -46,6 +46,7 @@ class Stats(C.Structure):
         ("forward_iterations", C.c_longlong),
         ("adjoint_iterations", C.c_longlong),
         ("divcorr_cg_sweeps", C.c_longlong),
+        ("divcorr_setup_ms", C.c_double),
     ]
 
 

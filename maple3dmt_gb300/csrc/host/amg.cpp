@@ -229,6 +229,7 @@ void dense_inverse(const CsrReal& A, std::vector<double>& inv) {
 
 void amg_build(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
     H.levels.clear();
+    H.aggregates.clear();
     H.levels.emplace_back();
     H.levels[0].A = A0;
     for (int l = 0;; ++l) {
@@ -242,6 +243,7 @@ void amg_build(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
         const int na = aggregate(L.A, d, opt.theta, agg);
         if (na == 0 || na > 0.85 * L.A.n_rows) break;   // coarsening stalled
         smoothed_prolongator(L.A, d, agg, na, opt.omega_p, L.P);
+        H.aggregates.push_back(agg);
         transpose(L.P, L.R);
         CsrReal AP;
         spgemm(L.A, L.P, AP);
@@ -253,6 +255,44 @@ void amg_build(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
     if (C.A.n_rows > 4096) throw std::runtime_error("multigrid coarsening left too large a coarse level");
     H.n_coarse = C.A.n_rows;
     dense_inverse(C.A, H.coarse_inv);
+}
+
+void amg_refresh(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
+    if (opt.omega_p != 0.0) throw std::runtime_error("multigrid refresh needs piecewise-constant prolongation");
+    const int nl = (int)H.levels.size();
+    if (nl < 1 || (int)H.aggregates.size() != nl - 1) throw std::runtime_error("no hierarchy to refresh");
+    H.levels[0].A = A0;
+    for (int l = 0; l < nl; ++l) {
+        AmgLevel& L = H.levels[l];
+        const std::vector<double> d = diagonal(L.A);
+        L.dinv.assign(L.A.n_rows, 1.0);
+        for (int i = 0; i < L.A.n_rows; ++i)
+            if (std::fabs(d[i]) > 1e-300) L.dinv[i] = 1.0 / d[i];
+        if (l + 1 == nl) break;
+        const std::vector<int>& agg = H.aggregates[l];
+        if ((int)agg.size() != L.A.n_rows) throw std::runtime_error("hierarchy does not match the operator");
+        // A_{l+1}[I][J] = sum of a_ij over i in I, j in J (P0^T A P0), with the
+        // pattern of the previous coarse operator
+        AmgLevel& C = H.levels[l + 1];
+        std::vector<double> acc(C.A.n_rows, 0.0);
+        std::vector<int> pos(C.A.n_rows, -1);
+        std::fill(C.A.val.begin(), C.A.val.end(), 0.0);
+        for (int I = 0; I < C.A.n_rows; ++I) {
+            for (int k = C.A.ptr[I]; k < C.A.ptr[I + 1]; ++k) pos[C.A.col[k]] = k;
+            for (int q = L.R.ptr[I]; q < L.R.ptr[I + 1]; ++q) {
+                const int i = L.R.col[q];
+                for (int k = L.A.ptr[i]; k < L.A.ptr[i + 1]; ++k) {
+                    const int J = agg[L.A.col[k]];
+                    if (J < 0) continue;
+                    if (pos[J] < C.A.ptr[I]) throw std::runtime_error("coarse pattern changed");
+                    C.A.val[pos[J]] += L.A.val[k];
+                }
+            }
+        }
+    }
+    const AmgLevel& Cl = H.levels.back();
+    H.n_coarse = Cl.A.n_rows;
+    dense_inverse(Cl.A, H.coarse_inv);
 }
 
 }  // namespace m3d

@@ -26,6 +26,7 @@ struct AmgLevel {
 
 struct AmgHierarchy {
     std::vector<AmgLevel> levels;   // levels[0] is the fine operator
+    std::vector<std::vector<int>> aggregates;   // per level l: row -> aggregate of level l+1 (-1: none)
     int n_coarse = 0;               // rows of the coarsest level
     std::vector<double> coarse_inv; // dense inverse of the coarsest operator, row-major
 };
@@ -41,5 +42,11 @@ struct AmgOptions {
 // included).  Rows without strong off-diagonal connections (Dirichlet rows)
 // are left out of every aggregate: the smoother alone handles them.
 void amg_build(const CsrReal& A, const AmgOptions& opt, AmgHierarchy& H);
+
+// Rebuilds the operators of a hierarchy for new values of the same sparsity
+// pattern (a new conductivity on the same mesh), keeping the aggregates of
+// `H` (the costly part of the setup).  Only for piecewise-constant
+// prolongation (omega_p = 0).
+void amg_refresh(const CsrReal& A, const AmgOptions& opt, AmgHierarchy& H);
 
 }  // namespace m3d

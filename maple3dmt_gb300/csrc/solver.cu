@@ -182,6 +182,7 @@ void GpuSolver::free_all() {
     dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_inv); dfree(dc.st);
     dfree(dc.lap_seg); dfree(d_lap_work); dfree(d_lap_qpos);
     free_amg();
+    amg_host = AmgHierarchy{};
     dc.lap_work = nullptr; dc.lap_qpos = nullptr;
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
@@ -622,7 +623,7 @@ void GpuSolver::free_amg() {
 // device (host setup, host/amg.cpp); falls back to the Jacobi PCG when the
 // coarsening does not reach a small coarse level.
 void GpuSolver::build_amg() {
-    free_amg();
+    const auto t0 = std::chrono::steady_clock::now();
     const int nn = L.nn;
     std::vector<double> diag(nn), off(h_inc_other.size());
     cuda_ok(cudaMemcpyAsync(diag.data(), dc.lap_diag, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream), "lap");
@@ -641,11 +642,42 @@ void GpuSolver::build_amg() {
     }
     AmgOptions opt;
     opt.omega_p = 0.0;   // piecewise-constant prolongation (the kernels assume it)
-    AmgHierarchy H;
-    try {
-        amg_build(A0, opt, H);
-    } catch (const std::exception&) {
-        return;   // Jacobi PCG
+    AmgHierarchy& H = amg_host;
+    bool built = false;
+    if (!H.levels.empty() && H.levels[0].A.n_rows == nn) {
+        try {
+            amg_refresh(A0, opt, H);   // same mesh: keep the aggregates
+            built = true;
+        } catch (const std::exception&) {
+            built = false;
+        }
+    }
+    const int nl_dev = amg_ok ? amg.n_levels : 0;
+    if (built && nl_dev == (int)H.levels.size()) {
+        // same hierarchy on the device: refresh the values in place
+        for (int l = 0; l < nl_dev; ++l) {
+            const AmgLevel& Lv = H.levels[l];
+            phys::AmgLevelDev& d = amg.lv[l];
+            if (l > 0)
+                cuda_ok(cudaMemcpyAsync(const_cast<double*>(d.val), Lv.A.val.data(), sizeof(double) * Lv.A.val.size(),
+                                        cudaMemcpyHostToDevice, stream), "mg values");
+            cuda_ok(cudaMemcpyAsync(const_cast<double*>(d.dinv), Lv.dinv.data(), sizeof(double) * Lv.dinv.size(),
+                                    cudaMemcpyHostToDevice, stream), "mg values");
+        }
+        cuda_ok(cudaMemcpyAsync(const_cast<double*>(amg.coarse_inv), H.coarse_inv.data(),
+                                sizeof(double) * H.coarse_inv.size(), cudaMemcpyHostToDevice, stream), "mg values");
+        sync();
+        amg_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return;
+    }
+    free_amg();
+    if (!built) {
+        try {
+            amg_build(A0, opt, H);
+        } catch (const std::exception&) {
+            H = AmgHierarchy{};
+            return;   // Jacobi PCG
+        }
     }
     const int nl = (int)H.levels.size();
     // a single level (tiny meshes) or a large coarse level: keep the Jacobi PCG
@@ -688,6 +720,8 @@ void GpuSolver::build_amg() {
     amg.n_coarse = H.n_coarse;
     amg.coarse_inv = up(H.coarse_inv);
     amg_ok = true;
+    sync();
+    amg_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
 KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
@@ -1126,6 +1160,7 @@ void GpuSolver::end_call() {
     stats.divcorr_outer = dcc.outer;
     stats.divcorr_cg_iterations = dcc.cg_iterations;
     stats.divcorr_cg_sweeps = dcc.cg_sweeps;
+    stats.divcorr_setup_ms = amg_setup_ms;
     stats.kernel_launches = launches;
 }
 
@@ -1472,11 +1507,23 @@ void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, c
     cuda_ok(cudaMemcpyAsync(d_err, err, sizeof(double) * (size_t)ns * nf * 4, cudaMemcpyHostToDevice, stream), "err");
     cuda_ok(cudaMemsetAsync(d_grad, 0, sizeof(double) * L.nc, stream), "memset");
     long long it_total = 0;
+    // per right-hand side counters of every solve of the call: forward then
+    // adjoint of each frequency group
+    std::vector<int> all_it, all_st;
+    std::vector<double> all_tr;
+    auto keep = [&]() {
+        for (int k = 0; k < stats.n_rhs && k < 64; ++k) {
+            all_it.push_back(stats.iterations[k]);
+            all_st.push_back(stats.status[k]);
+            all_tr.push_back(stats.true_residual[k]);
+        }
+    };
     for (int f0 = 0; f0 < nf; f0 += 8) {
         const int g = std::min(8, nf - f0);
         std::vector<double> fr(freqs + f0, freqs + f0 + g);
         run_forward(fr, Z_out ? Z_out + (size_t)f0 * ns * 8 : nullptr);
         it_total += stats.total_iterations;
+        keep();
         const int K = E_K;
         phys::weighted_residual(ns, g, nf, f0, d_obs, d_err, d_Z, d_wr, stream);
         cuda_ok(cudaMemsetAsync(d_adj, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
@@ -1488,12 +1535,19 @@ void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, c
         current_omega = 2.0 * kPi * fr[0];
         run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
         it_total += stats.total_iterations;
+        keep();
         phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, g, 2, d_grad, stream);
         ++launches;
     }
     cuda_ok(cudaMemcpyAsync(grad, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "grad");
     sync();
     stats.total_iterations = (int)it_total;
+    stats.n_rhs = (int)all_it.size();
+    for (size_t k = 0; k < all_it.size() && k < 64; ++k) {
+        stats.iterations[k] = all_it[k];
+        stats.status[k] = all_st[k];
+        stats.true_residual[k] = all_tr[k];
+    }
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     end_call();
 }

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "m3d_gb300.h"
+#include "host/amg.hpp"
 #include "host/layout.hpp"
 #include "cuda/krylov.cuh"
 #include "cuda/physics.cuh"
@@ -98,6 +99,8 @@ private:
     std::vector<int> h_inc_ptr, h_inc_other;
     phys::AmgDev amg{};
     bool amg_ok = false;
+    AmgHierarchy amg_host;          // kept between conductivity updates: aggregates are reused
+    double amg_setup_ms = 0.0;      // host time of the last multigrid setup
     std::vector<void*> amg_mem;
     void build_amg();
     void free_amg();

@@ -190,18 +190,22 @@ def test_c2_scale_true_residual(lib):
 
 
 def test_c2_scale_divcorr_preconditioners_agree(lib):
-    """Full-size mesh, the two lowest frequencies (the most divergence
-    correction): impedances with the multigrid-preconditioned PCG agree with
-    the Jacobi PCG (the reference's) to 1e-5 relative -- both solves stop at
-    the 1e-7 true residual, so Z differs at the solve tolerance, not more."""
+    """Full-size mesh, the two highest frequencies, the reference's forward
+    strategy (BiCGStab to 1e-7, then the divergence correction): impedances
+    with the multigrid-preconditioned PCG agree with the Jacobi PCG (the
+    reference's) to 1e-5 relative -- both solves stop at the 1e-7 true
+    residual and both PCGs at 1e-10, so Z differs at the solve tolerance, not
+    more.  (At 0.01 Hz this strategy does not converge on this mesh without
+    the interleaved divergence correction; the interleaved strategy is the
+    one the gradient runs.)"""
     from maple3dmt_gb300 import mesh
     from maple3dmt_gb300.solver import solver_for_survey
     sv = mesh.layered_block_survey(min_level=6)
     Zs = []
     for pc in (0, 1):
-        s = solver_for_survey(sv, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1, forward_interleaved=1,
+        s = solver_for_survey(sv, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1, forward_interleaved=0,
                               divcorr_precond=pc)
-        Zs.append(s.forward_batch(sv.freqs[:2]))
+        Zs.append(s.forward_batch(sv.freqs[-2:]))
         st = s.stats()
         assert all(t <= 1e-7 for t in st["true_residual"][:4]), st
         s.close()
