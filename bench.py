@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--plain", action="store_true",
                     help="the plain GPU arm the batched solve is compared with: one frequency per call, complex128 "
                          "Krylov, CSR row kernels, Jacobi divergence correction, the reference's forward strategy")
+    ap.add_argument("--ssor-form", type=int, default=1, choices=[0, 1],
+                    help="inner FP32 solve: 0 right-preconditioned SSOR-BiCGStab, 1 Eisenstat split form")
     ap.add_argument("--divcorr-precond", type=int, default=1, choices=[0, 1],
                     help="divergence-correction PCG: 0 Jacobi (the reference's), 1 aggregation multigrid")
     ap.add_argument("--row-kernels", type=int, default=1, choices=[0, 1],
@@ -235,10 +237,12 @@ def run_ours(args, rank, world, local_rank):
     sv, obs, err = workload(args)
     if args.plain:
         args.precision, args.forward, args.row_kernels, args.divcorr_precond = "fp64", "reference", 0, 0
+        args.ssor_form = 0
     s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=args.maxiter,
                           precision=1 if args.precision == "mixed" else 0,
                           forward_interleaved=1 if args.forward == "interleaved" else 0,
-                          row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond)
+                          row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
+                          ssor_form=args.ssor_form)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -332,6 +336,7 @@ def run_ours(args, rank, world, local_rank):
                    "tol": 1e-7, "precision": args.precision, "forward": args.forward,
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
+                   "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
                    "arm": "plain (per frequency, complex128)" if args.plain else "batched",
                    "l2": "inputs larger than L2 (matrix alone 260 MB)",
                    "parallelism": f"replica x{world}"},

@@ -116,6 +116,8 @@ typedef struct m3d_params {
                                  1 32-row slices bulk-copied to shared memory */
     int divcorr_precond;      /* divergence-correction PCG preconditioner: 0 Jacobi (the
                                  reference's), 1 aggregation multigrid V-cycle */
+    int ssor_form;            /* mixed-precision inner solve: 0 right-preconditioned SSOR-BiCGStab
+                                 as the reference, 1 Eisenstat split form (staged rows) */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;

@@ -26,6 +26,7 @@ class Params(C.Structure):
         ("forward_interleaved", C.c_int),
         ("row_kernels", C.c_int),
         ("divcorr_precond", C.c_int),
+        ("ssor_form", C.c_int),
     ]
 
 

@@ -73,6 +73,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->forward_interleaved = 0;
     p->row_kernels = 1;
     p->divcorr_precond = 1;
+    p->ssor_form = 1;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -104,7 +105,8 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
     if (!h || !m3d::leaves_valid(leaves) || !params) return fail(h, M3D_ERR_ARG, "invalid leaves or params");
     if (params->bicgstab_tol <= 0 || params->bicgstab_maxiter < 1 || params->divcorr_iter_per_dc < 1 ||
         params->sigma_bg <= 0 || params->precision < 0 || params->precision > 1 || params->row_kernels < 0 ||
-        params->row_kernels > 1 || params->divcorr_precond < 0 || params->divcorr_precond > 1)
+        params->row_kernels > 1 || params->divcorr_precond < 0 || params->divcorr_precond > 1 ||
+        params->ssor_form < 0 || params->ssor_form > 1)
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
 }

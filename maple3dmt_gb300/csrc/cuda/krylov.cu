@@ -748,6 +748,290 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     if (c.timer) c.timer->end(th);
 }
 
+// ---------------------------------------------------------------------------
+// Eisenstat form of SSOR-BiCGStab (see krylov.cuh): sweeps over the staged
+// lower / upper segments, the BiCGStab p-update fused into the backward
+// sweep, the dot products of the forward sweep summed per colour launch and
+// block, then once in block order by k_eis_reduce.
+// ---------------------------------------------------------------------------
+
+// Per-block partial sums of NQ quantities per right-hand side (lane l on
+// rhs l % K): shuffle tree over the lanes of a right-hand side, warps in order;
+// written to dst[q * K + k].
+template <int NQ, int K, int NT>
+__device__ __forceinline__ void block_partial_lanes(double2 (&acc)[NQ], double2* __restrict__ dst) {
+    constexpr int PK = NQ * K, NW = NT / 32;
+    __shared__ double2 sm[NW][PK];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= K; off >>= 1)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) acc[q] = cadd(acc[q], shfl_xor(acc[q], off));
+    if (lane < K)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) sm[warp][q * K + lane] = acc[q];
+    __syncthreads();
+    if (threadIdx.x < PK) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int w = 0; w < NW; ++w) t = cadd(t, sm[w][threadIdx.x]);
+        dst[threadIdx.x] = t;
+    }
+}
+
+// Backward sweep of one colour: w_i = (z_i - sum_{upper} a_ij w_j) / d_i.
+// FUSE_P: z is the new search direction, p = r + beta (p - omega v) (r on
+// the first iteration, 0 for right-hand sides not running), written back
+// to p (bicgstab.cpp:60-67).
+template <class R, int K, bool FUSE_P>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
+    k_eis_bwd_st(SegView<R> S, const int4* __restrict__ work, int count, DiagView<R> D, BatchView B,
+                 const cplx<R>* __restrict__ z_in, cplx<R>* p, const cplx<R>* __restrict__ r,
+                 const cplx<R>* __restrict__ vv, const BicgState* __restrict__ st, cplx<R>* w) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int RPW = Rpw<K>::v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    bool run = true, first = false;
+    C be = cm<R>(0, 0), omg = cm<R>(0, 0);
+    if (FUSE_P) {
+        const BicgState T = st[rhs];
+        run = T.status == kRunning;
+        first = T.iter == 0;
+        be = from_d<C>(T.beta);
+        omg = from_d<C>(T.omega);
+    }
+    slice_pipeline<2>(S.seg, work, count, S.stage_up, S.err, [&](const SegItem& it, const unsigned char* base) {
+        SegRows<R> up;
+        up.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int row = it.slice * kSlice + lr;
+            const size_t i = (size_t)row * K + rhs;
+            C z;
+            if (FUSE_P) {
+                if (!run) z = cm<R>(0, 0);
+                else if (first) z = r[i];
+                else z = cadd(r[i], cmul(be, csub(p[i], cmul(omg, vv[i]))));
+                p[i] = z;
+            } else {
+                z = z_in[i];
+            }
+            const C d = diag_of(D, row, om);
+            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], w, rhs, cm<R>(0, 0));
+            w[i] = cmul(csub(z, s), inv_c(d));
+        }
+    });
+}
+
+// Forward sweep of one colour: y_i = ((z_i - d_i w_i) - sum_{lower} a_ij y_j) / d_i,
+// out_i = d_i (w_i + y_i) = (A_hat z)_i, with this block's partial dot
+// products of out: (aux, out) (MODE Ap) or (out, out), (out, aux) (MODE As).
+template <class R, int K, int MODE>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
+    k_eis_fwd_st(SegView<R> S, const int4* __restrict__ work, int count, DiagView<R> D, BatchView B,
+                 const cplx<R>* __restrict__ z, const cplx<R>* __restrict__ w, cplx<R>* y,
+                 cplx<R>* __restrict__ out, const cplx<R>* __restrict__ aux, double2* __restrict__ partial) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int RPW = Rpw<K>::v;
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    C accR[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) accR[q] = cm<R>(0, 0);
+    slice_pipeline<1>(S.seg, work, count, S.stage_lo, S.err, [&](const SegItem& it, const unsigned char* base) {
+        SegRows<R> lo;
+        lo.bind(base);
+#pragma unroll
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
+            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+            const int row = it.slice * kSlice + lr;
+            const size_t i = (size_t)row * K + rhs;
+            const C zv = z[i], wv = w[i];
+            const C d = diag_of(D, row, om);
+            const C t = csub(zv, cmul(d, wv));
+            const C s = seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs, cm<R>(0, 0));
+            const C yv = cmul(csub(t, s), inv_c(d));
+            y[i] = yv;
+            const C ov = cmul(d, cadd(wv, yv));
+            out[i] = ov;
+            if (MODE == kSpmvAp) {
+                accR[0] = cadd(accR[0], cjmul(aux[i], ov));
+            } else {
+                accR[0].x += ov.x * ov.x + ov.y * ov.y;
+                accR[1] = cadd(accR[1], cjmul(ov, aux[i]));
+            }
+        }
+    });
+    double2 acc[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = to_d(accR[q]);
+    block_partial_lanes<NQ, K, Sh::NT>(acc, partial + (size_t)blockIdx.x * NQ * K);
+}
+
+// Sums the block partials of all colour launches in slot order and runs the
+// scalar step: alpha (MODE Ap, bicgstab.cpp:79-87) or omega (MODE As, :116-125).
+template <int K, int MODE>
+__global__ void __launch_bounds__(kBlock) k_eis_reduce(const double2* __restrict__ partial, int slots,
+                                                       BicgState* st) {
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+    constexpr int PK = NQ * K;
+    constexpr int CH = kBlock / PK;
+    __shared__ double2 chunk[kBlock];
+    __shared__ double2 out[PK];
+    const int p = threadIdx.x % PK, j = threadIdx.x / PK;
+    double2 s = make_double2(0.0, 0.0);
+    if (j < CH)
+        for (int b = j; b < slots; b += CH) s = cadd(s, partial[(size_t)b * PK + p]);
+    chunk[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < PK) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int jj = 0; jj < CH; ++jj) t = cadd(t, chunk[jj * PK + threadIdx.x]);
+        out[threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        BicgState T = st[threadIdx.x];
+        if (MODE == kSpmvAp) ep_r0v(T, out, threadIdx.x, K);
+        else ep_omega(T, out, threadIdx.x, K);
+        st[threadIdx.x] = T;
+    }
+}
+
+// r = r0 = D y (the split right side b_hat = D (D + L)^-1 b), |b_hat|, (r0, r) -> start
+template <class R, int K>
+__global__ void __launch_bounds__(kBlock) k_eis_init(long n, DiagView<R> D, BatchView B,
+                                                     const cplx<R>* __restrict__ y, cplx<R>* __restrict__ r,
+                                                     cplx<R>* __restrict__ r0, BicgState* st, RedScratch rs) {
+    using C = cplx<R>;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int rhs = (int)(i0 % K);
+    const R om = (R)B.omega[rhs];
+    R bb = 0;
+    C rr = cm<R>(0, 0);
+    for (long i = i0; i < n; i += stride) {
+        const C rv = cmul(diag_of(D, (int)(i / K), om), y[i]);
+        r[i] = rv;
+        r0[i] = rv;
+        bb += rv.x * rv.x + rv.y * rv.y;
+        rr = cadd(rr, cjmul(rv, rv));
+    }
+    double2 acc[3] = {make_double2((double)bb, 0.0), make_double2((double)bb, 0.0), to_d(rr)};
+    __shared__ double2 out[3 * K];
+    if (grid_reduce_lanes<3, K>(acc, rs, out)) {
+        if (threadIdx.x < K) {
+            BicgState T = st[threadIdx.x];
+            ep_init(T, out, threadIdx.x, K);
+            st[threadIdx.x] = T;
+        }
+    }
+}
+
+// Blocks of one staged launch (as launch_staged chooses them).
+template <class F>
+int staged_grid(F* kernel, int nt, int stage_bytes, long items, int cap) {
+    const int smem = 2 * stage_bytes;
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(reinterpret_cast<const void*>(kernel), cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return (int)std::min<long>((long)wave_grid(kernel, cap, nt, smem), std::max<long>(items, 1));
+}
+
+// out = A_hat z over every colour; FUSE_P: z is the updated p (see k_eis_bwd_st).
+template <class R, int K, bool FUSE_P, int MODE>
+void eis_apply_k(const KrylovCtx<R>& c, const cplx<R>* z, cplx<R>* p, const cplx<R>* r, const cplx<R>* vv,
+                 BicgState* st, cplx<R>* w, cplx<R>* y, cplx<R>* out, const cplx<R>* aux) {
+    constexpr int NT = StagedShape<K>::NT;
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+    const int nc = (int)c.colour_ptr.size() - 1;
+    for (int col = nc - 1; col >= 0; --col) {
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+        if (s1 <= s0) continue;
+        launch_staged(k_eis_bwd_st<R, K, FUSE_P>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+                      c.seg.work_col + s0, s1 - s0, c.D, c.B, z, p, r, vv, (const BicgState*)st, w);
+        check_launch(c.launches);
+    }
+    const cplx<R>* zz = FUSE_P ? (const cplx<R>*)p : z;
+    int slot = 0;
+    for (int col = 0; col < nc; ++col) {
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+        if (s1 <= s0) continue;
+        auto kf = k_eis_fwd_st<R, K, MODE>;
+        const int g = staged_grid(kf, NT, c.seg.stage_lo, s1 - s0, 1 << 20);
+        if (slot + g > c.eis_slots) throw std::runtime_error("Eisenstat partial-sum scratch too small");
+        kf<<<g, NT, 2 * c.seg.stage_lo, c.stream>>>(c.seg, c.seg.work_col + s0, s1 - s0, c.D, c.B, zz,
+                                                      (const cplx<R>*)w, y, out, aux,
+                                                      c.eis_partial + (size_t)slot * NQ * K);
+        check_launch(c.launches);
+        slot += g;
+    }
+    k_eis_reduce<K, MODE><<<1, kBlock, 0, c.stream>>>(c.eis_partial, slot, st);
+    check_launch(c.launches);
+}
+
+template <class R, int K>
+void eis_init_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+    constexpr int NT = StagedShape<K>::NT;
+    const int nc = (int)c.colour_ptr.size() - 1;
+    for (int col = 0; col < nc; ++col) {
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+        if (s1 <= s0) continue;
+        launch_staged(k_ssor_fwd_st<R, K>, NT, c.seg.stage_lo, s1 - s0, 1 << 20, c.stream, c.seg,
+                      c.seg.work_col + s0, s1 - s0, c.D, c.B, (const cplx<R>*)v.b, v.y);
+        check_launch(c.launches);
+    }
+    const long n = (long)c.n_pad * K;
+    k_eis_init<R, K><<<wave_grid(k_eis_init<R, K>, c.grid_vec), kBlock, 0, c.stream>>>(n, c.D, c.B, v.y, v.r, v.r0,
+                                                                                    st, c.red);
+    check_launch(c.launches);
+}
+
+template <class R, int K>
+void eis_iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+    const long n = (long)c.n_pad * K;
+    const int gv = c.grid_vec;
+    const double vb = (double)c.n_rows * K * sizeof(cplx<R>);
+    // p update + v = A_hat p: matrix once, r, p (read, write), v (read, write), w (write, read), y
+    int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + 9 * vb, K) : -1;
+    eis_apply_k<R, K, true, kSpmvAp>(c, nullptr, v.p, v.r, v.v, st, v.ph, v.y, v.v, v.r0);
+    if (c.timer) c.timer->end(th);
+    th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
+    k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
+    check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
+    // t = A_hat s: matrix once, s (twice), w (write, read), y, t, dot operand s
+    th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + 7 * vb, K) : -1;
+    eis_apply_k<R, K, false, kSpmvAs>(c, v.s, nullptr, nullptr, nullptr, st, v.ph, v.y, v.t, v.s);
+    if (c.timer) c.timer->end(th);
+    th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
+    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.p, v.s, v.s,
+                                                                              v.t, st, c.red);
+    check_launch(c.launches);
+    if (c.timer) c.timer->end(th);
+}
+
+template <class R, int K>
+void eis_finish_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, cplx<R>* out) {
+    constexpr int NT = StagedShape<K>::NT;
+    const int nc = (int)c.colour_ptr.size() - 1;
+    for (int col = nc - 1; col >= 0; --col) {
+        const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
+        if (s1 <= s0) continue;
+        launch_staged(k_eis_bwd_st<R, K, false>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+                      c.seg.work_col + s0, s1 - s0, c.D, c.B, (const cplx<R>*)v.x, (cplx<R>*)nullptr,
+                      (const cplx<R>*)nullptr, (const cplx<R>*)nullptr, (const BicgState*)nullptr, out);
+        check_launch(c.launches);
+    }
+}
+
 }  // namespace
 
 #define M3D_DISPATCH_K(K_, CALL)                                    \
@@ -786,6 +1070,28 @@ void bicg_iteration(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st
 #undef CALL
 }
 
+template <class R>
+void eis_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+    if (c.row_kernels != kRowsStaged) throw std::logic_error("Eisenstat form needs the staged row kernels");
+#define CALL(K) eis_init_k<R, K>(c, v, st)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
+template <class R>
+void eis_iteration(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
+#define CALL(K) eis_iteration_k<R, K>(c, v, st)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
+template <class R>
+void eis_finish(const KrylovCtx<R>& c, const KrylovVecs<R>& v, cplx<R>* out) {
+#define CALL(K) eis_finish_k<R, K>(c, v, out)
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
 template void spmv<double>(const KrylovCtx<double>&, int, const double2*, double2*, const double2*, double2*, BicgState*);
 template void spmv<float>(const KrylovCtx<float>&, int, const float2*, float2*, const float2*, float2*, BicgState*);
 template void ssor_apply<double>(const KrylovCtx<double>&, const double2*, double2*, double2*);
@@ -794,5 +1100,9 @@ template void bicg_init<double>(const KrylovCtx<double>&, const KrylovVecs<doubl
 template void bicg_init<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
 template void bicg_iteration<double>(const KrylovCtx<double>&, const KrylovVecs<double>&, BicgState*);
 template void bicg_iteration<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
+
+template void eis_init<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
+template void eis_iteration<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
+template void eis_finish<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, float2*);
 
 }  // namespace m3d

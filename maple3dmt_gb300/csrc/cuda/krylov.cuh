@@ -116,6 +116,10 @@ struct KrylovCtx {
     // kRowsStaged (segments bulk-copied to shared memory)
     dev::SegView<R> seg;
     int row_kernels;
+    // Eisenstat form of SSOR-BiCGStab (staged rows only): per-colour block
+    // partial sums of the sweeps' dot products, summed by one reduction kernel
+    double2* eis_partial = nullptr;   // [eis_slots][kMaxQ * kMaxRhs]
+    int eis_slots = 0;
 };
 
 enum RowKernels : int { kRowsDirect = 0, kRowsStaged = 1 };
@@ -144,5 +148,21 @@ template <class R>
 void bicg_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st);
 template <class R>
 void bicg_iteration(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st);
+
+// BiCGStab on the split-preconditioned operator A_hat = M1^-1 A M2^-1 of the
+// SSOR splitting M = (D + L) D^-1 (D + U), M1 = (D + L) D^-1, M2 = D + U
+// (S. C. Eisenstat, "Efficient implementation of a class of preconditioned
+// conjugate gradient methods", SIAM J. Sci. Stat. Comput. 2 (1981)):
+//   A_hat z = D (w + (D + L)^-1 (z - D w)),  w = (D + U)^-1 z,
+// one backward and one forward sweep per application and no separate SpMV.
+// eis_init: r = b_hat = D (D + L)^-1 b, r0 = r, x_hat = 0 (x must be zero);
+// eis_iteration: one BiCGStab step on A_hat (x holds x_hat);
+// eis_finish: out = M2^-1 x_hat = (D + U)^-1 x_hat, the correction in x-space.
+template <class R>
+void eis_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st);
+template <class R>
+void eis_iteration(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st);
+template <class R>
+void eis_finish(const KrylovCtx<R>& c, const KrylovVecs<R>& v, dev::cplx<R>* out);
 
 }  // namespace m3d

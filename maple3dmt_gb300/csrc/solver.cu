@@ -175,8 +175,9 @@ void GpuSolver::free_all() {
     kv32_K = 0;
     dfree(kv32b.x); dfree(kv32b.b); dfree(kv32b.r); dfree(kv32b.r0); dfree(kv32b.p); dfree(kv32b.v);
     dfree(kv32b.s); dfree(kv32b.t); dfree(kv32b.ph); dfree(kv32b.sh); dfree(kv32b.y);
-    dfree(d_lane_map); dfree(d_lane_add); dfree(d_lane_sel);
+    dfree(d_lane_map); dfree(d_lane_add); dfree(d_lane_sel); dfree(d_eis_partial);
     kv32b_K = 0;
+    eis_slots = 0;
     dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     dfree(dc.divJ); dfree(dc.phi); dfree(dc.r); dfree(dc.z); dfree(dc.p); dfree(dc.Ap); dfree(dc.phi0);
     dfree(dc.lap_diag); dfree(dc.lap_off); dfree(dc.jac_inv); dfree(dc.st);
@@ -881,6 +882,13 @@ void GpuSolver::ensure_vecs32b(int K) {
         d_lane_add = dalloc<int>(dev::kMaxRhs);
         d_lane_sel = dalloc<int>(dev::kMaxRhs);
     }
+    if (!d_eis_partial) {
+        // one slot per block of every colour launch: colours x (32 resident blocks per SM)
+        int sms = 0;
+        cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "sm count");
+        eis_slots = std::max(1, n_colours()) * 32 * std::max(1, sms);
+        d_eis_partial = dalloc<double2>((size_t)eis_slots * dev::kMaxQ * dev::kMaxRhs);
+    }
     kv32b_K = K;
 }
 
@@ -904,6 +912,8 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     f.n_freq = c.n_freq;
     f.seg = seg32;
     f.row_kernels = c.row_kernels;
+    f.eis_partial = d_eis_partial;
+    f.eis_slots = eis_slots;
     return f;
 }
 
@@ -1068,10 +1078,17 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             cuda_ok(cudaMemcpyAsync(d_lane_map, map.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "map");
             cuda_ok(cudaMemcpyAsync(d_scale, sc.data(), sizeof(double) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "scale");
         };
-        // flushes lanes with add[j] set: x64 += scale * x32
-        auto flush = [&](const KrylovVecs<float>& v, int Kn) {
+        const bool eis = P.ssor_form == 1 && P.row_kernels == kRowsStaged;
+        // flushes lanes with add[j] set: x64 += scale * d32, d32 the x-space
+        // correction (x_hat mapped back by (D + U)^-1 in the Eisenstat form)
+        auto flush = [&](const KrylovCtx<float>& cc, const KrylovVecs<float>& v, int Kn) {
+            const float2* d = v.x;
+            if (eis) {
+                eis_finish(cc, v, v.sh);
+                d = v.sh;
+            }
             cuda_ok(cudaMemcpyAsync(d_lane_add, add.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "add");
-            k_add_f32_lanes<<<launch_grid((long)n_pad * Kn), 256, 0, stream>>>(x, K, v.x, Kn, d_lane_map, d_lane_add,
+            k_add_f32_lanes<<<launch_grid((long)n_pad * Kn), 256, 0, stream>>>(x, K, d, Kn, d_lane_map, d_lane_add,
                                                                            d_scale, (long)n_pad);
             ++launches;
         };
@@ -1091,7 +1108,8 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
         }
         cuda_ok(cudaMemcpyAsync(d_states, ls.data(), sizeof(BicgState) * Kc, cudaMemcpyHostToDevice, stream), "states");
         KrylovCtx<float> c32 = kctx32(Kc, fm.data());
-        bicg_init(c32, cur, d_states);
+        if (eis) eis_init(c32, cur, d_states);
+        else bicg_init(c32, cur, d_states);
         int it = 0;
         auto record = [&](int j) {   // lane j leaves the batch
             const int k = lanes[j];
@@ -1110,7 +1128,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 // finished lanes: add their corrections and record them
                 for (int j = 0; j < dev::kMaxRhs; ++j)
                     add[j] = (j < Kc && lanes[j] >= 0 && ls[j].status != kRunning) ? 1 : 0;
-                flush(cur, Kc);
+                flush(c32, cur, Kc);
                 std::vector<int> sel(dev::kMaxRhs, -1), nl(Kn, -1);
                 std::vector<BicgState> ns(Kn);
                 int q = 0;
@@ -1137,10 +1155,13 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 Kc = Kn;
                 c32 = kctx32(Kc, fm.data());
             }
-            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c32, cur, d_states);
+            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) {
+                if (eis) eis_iteration(c32, cur, d_states);
+                else bicg_iteration(c32, cur, d_states);
+            }
         }
         for (int j = 0; j < dev::kMaxRhs; ++j) add[j] = (j < Kc && lanes[j] >= 0) ? 1 : 0;
-        flush(cur, Kc);
+        flush(c32, cur, Kc);
         for (int j = 0; j < Kc; ++j) record(j);
         if (step > 0) ++stats.refinements;
     }

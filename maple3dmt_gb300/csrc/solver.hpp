@@ -133,6 +133,8 @@ private:
     KrylovVecs<float> kv32b{};    // second set for repacking the batch to fewer lanes
     int kv32b_K = 0;
     int *d_lane_map = nullptr, *d_lane_add = nullptr, *d_lane_sel = nullptr;   // [16] lane maps
+    double2* d_eis_partial = nullptr;   // block partial sums of the Eisenstat sweeps
+    int eis_slots = 0;
     void ensure_vecs32b(int K);
     double* d_scale = nullptr;    // [16] per-rhs residual norms of the refinement step
     // fields of the last forward solve: [n_pad][Kf], rhs 2f+p
