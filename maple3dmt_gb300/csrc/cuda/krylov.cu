@@ -755,6 +755,10 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
 // block, then once in block order by k_eis_reduce.
 // ---------------------------------------------------------------------------
 
+// Mode of the forward sweep and reduction for t = A_hat s whose |s|^2 comes
+// from the fused backward sweep (quantities |s|^2, (t, t), (t, s)).
+constexpr int kEisAsS = 5;
+
 // Per-block partial sums of NQ quantities per right-hand side (lane l on
 // rhs l % K): shuffle tree over the lanes of a right-hand side, warps in order;
 // written to dst[q * K + k].
@@ -779,14 +783,17 @@ __device__ __forceinline__ void block_partial_lanes(double2 (&acc)[NQ], double2*
 }
 
 // Backward sweep of one colour: w_i = (z_i - sum_{upper} a_ij w_j) / d_i.
-// FUSE_P: z is the new search direction, p = r + beta (p - omega v) (r on
-// the first iteration, 0 for right-hand sides not running), written back
-// to p (bicgstab.cpp:60-67).
-template <class R, int K, bool FUSE_P>
+// FUSE 0: z = z_in.  FUSE 1: z is the new search direction, p = r + beta
+// (p - omega v) (r on the first iteration, 0 for right-hand sides not
+// running), written back to p (bicgstab.cpp:60-67).  FUSE 2: z = s = r - alpha v
+// (0 when not running), written to `p`, and this block's partial |s|^2 in
+// slot q = 0 of a 3-quantity partial block (:89-94).
+template <class R, int K, int FUSE>
 __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
     k_eis_bwd_st(SegView<R> S, const int4* __restrict__ work, int count, DiagView<R> D, BatchView B,
                  const cplx<R>* __restrict__ z_in, cplx<R>* p, const cplx<R>* __restrict__ r,
-                 const cplx<R>* __restrict__ vv, const BicgState* __restrict__ st, cplx<R>* w) {
+                 const cplx<R>* __restrict__ vv, const BicgState* __restrict__ st, cplx<R>* w,
+                 double2* __restrict__ partial) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
@@ -795,14 +802,16 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
     bool run = true, first = false;
-    C be = cm<R>(0, 0), omg = cm<R>(0, 0);
-    if (FUSE_P) {
+    C be = cm<R>(0, 0), omg = cm<R>(0, 0), al = cm<R>(0, 0);
+    if (FUSE != 0) {
         const BicgState T = st[rhs];
         run = T.status == kRunning;
         first = T.iter == 0;
         be = from_d<C>(T.beta);
         omg = from_d<C>(T.omega);
+        al = from_d<C>(T.alpha);
     }
+    R ss = 0;
     slice_pipeline<2>(S.seg, work, count, S.stage_up, S.err, [&](const SegItem& it, const unsigned char* base) {
         SegRows<R> up;
         up.bind(base);
@@ -812,11 +821,15 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
             const int row = it.slice * kSlice + lr;
             const size_t i = (size_t)row * K + rhs;
             C z;
-            if (FUSE_P) {
+            if (FUSE == 1) {
                 if (!run) z = cm<R>(0, 0);
                 else if (first) z = r[i];
                 else z = cadd(r[i], cmul(be, csub(p[i], cmul(omg, vv[i]))));
                 p[i] = z;
+            } else if (FUSE == 2) {
+                z = run ? csub(r[i], cmul(al, vv[i])) : cm<R>(0, 0);
+                p[i] = z;
+                ss += z.x * z.x + z.y * z.y;
             } else {
                 z = z_in[i];
             }
@@ -825,6 +838,10 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
             w[i] = cmul(csub(z, s), inv_c(d));
         }
     });
+    if (FUSE == 2) {
+        double2 acc[3] = {make_double2((double)ss, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+        block_partial_lanes<3, K, Sh::NT>(acc, partial + (size_t)blockIdx.x * 3 * K);
+    }
 }
 
 // Forward sweep of one colour: y_i = ((z_i - d_i w_i) - sum_{lower} a_ij y_j) / d_i,
@@ -839,6 +856,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
     using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
     constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+    constexpr int NQW = (MODE == kEisAsS) ? 3 : NQ;   // quantities per partial block written
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int rhs = lane % K;
     const int lr0 = warp * RPW + lane / K;
@@ -870,26 +888,51 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v)
             }
         }
     });
-    double2 acc[NQ];
+    double2 acc[NQW];
+    acc[0] = make_double2(0.0, 0.0);
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) acc[q] = to_d(accR[q]);
-    block_partial_lanes<NQ, K, Sh::NT>(acc, partial + (size_t)blockIdx.x * NQ * K);
+    for (int q = 0; q < NQ; ++q) acc[NQW - NQ + q] = to_d(accR[q]);
+    block_partial_lanes<NQW, K, Sh::NT>(acc, partial + (size_t)blockIdx.x * NQW * K);
 }
 
-// Sums the block partials of all colour launches in slot order and runs the
-// scalar step: alpha (MODE Ap, bicgstab.cpp:79-87) or omega (MODE As, :116-125).
+// Sums the block partials of all colour launches and runs the scalar step:
+// alpha (MODE Ap, bicgstab.cpp:79-87) or omega (MODE As, :116-125).  Block b
+// sums slots [b * kEisSlotsPerBlock, ...) in a fixed order, the last block to
+// finish sums the block results in block order: deterministic, and no single
+// block walks thousands of slots.
+constexpr int kEisSlotsPerBlock = 64;
+
 template <int K, int MODE>
 __global__ void __launch_bounds__(kBlock) k_eis_reduce(const double2* __restrict__ partial, int slots,
-                                                       BicgState* st) {
-    constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+                                                       BicgState* st, RedScratch rs) {
+    constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kEisAsS) ? 3 : 2;
     constexpr int PK = NQ * K;
     constexpr int CH = kBlock / PK;
     __shared__ double2 chunk[kBlock];
     __shared__ double2 out[PK];
+    __shared__ bool am_last;
     const int p = threadIdx.x % PK, j = threadIdx.x / PK;
+    const int s0 = blockIdx.x * kEisSlotsPerBlock;
+    const int s1 = min(slots, s0 + kEisSlotsPerBlock);
     double2 s = make_double2(0.0, 0.0);
     if (j < CH)
-        for (int b = j; b < slots; b += CH) s = cadd(s, partial[(size_t)b * PK + p]);
+        for (int b = s0 + j; b < s1; b += CH) s = cadd(s, __ldcg(&partial[(size_t)b * PK + p]));
+    chunk[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x < PK) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int jj = 0; jj < CH; ++jj) t = cadd(t, chunk[jj * PK + threadIdx.x]);
+        __stcg(&rs.partial[(size_t)blockIdx.x * PK + threadIdx.x], t);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) am_last = atomicAdd(rs.counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    s = make_double2(0.0, 0.0);
+    if (j < CH)
+        for (int b = j; b < (int)gridDim.x; b += CH) s = cadd(s, __ldcg(&rs.partial[(size_t)b * PK + p]));
     chunk[threadIdx.x] = s;
     __syncthreads();
     if (threadIdx.x < PK) {
@@ -900,10 +943,17 @@ __global__ void __launch_bounds__(kBlock) k_eis_reduce(const double2* __restrict
     __syncthreads();
     if (threadIdx.x < K) {
         BicgState T = st[threadIdx.x];
-        if (MODE == kSpmvAp) ep_r0v(T, out, threadIdx.x, K);
-        else ep_omega(T, out, threadIdx.x, K);
+        if (MODE == kSpmvAp) {
+            ep_r0v(T, out, threadIdx.x, K);
+        } else if (MODE == kEisAsS) {
+            ep_s(T, out, threadIdx.x, K);
+            ep_omega(T, out + K, threadIdx.x, K);
+        } else {
+            ep_omega(T, out, threadIdx.x, K);
+        }
         st[threadIdx.x] = T;
     }
+    if (threadIdx.x == 0) *rs.counter = 0u;
 }
 
 // r = r0 = D y (the split right side b_hat = D (D + L)^-1 b), |b_hat|, (r0, r) -> start
@@ -945,22 +995,30 @@ int staged_grid(F* kernel, int nt, int stage_bytes, long items, int cap) {
     return (int)std::min<long>((long)wave_grid(kernel, cap, nt, smem), std::max<long>(items, 1));
 }
 
-// out = A_hat z over every colour; FUSE_P: z is the updated p (see k_eis_bwd_st).
-template <class R, int K, bool FUSE_P, int MODE>
+// out = A_hat z over every colour.  FUSE 1: z is the updated p; FUSE 2: z
+// is s = r - alpha v, stored in `p`, with |s|^2 reduced alongside (MODE
+// kEisAsS); see k_eis_bwd_st.  The backward sweeps of FUSE 2 take the first
+// partial slots, the forward sweeps the next; one reduction sums them all.
+template <class R, int K, int FUSE, int MODE>
 void eis_apply_k(const KrylovCtx<R>& c, const cplx<R>* z, cplx<R>* p, const cplx<R>* r, const cplx<R>* vv,
                  BicgState* st, cplx<R>* w, cplx<R>* y, cplx<R>* out, const cplx<R>* aux) {
     constexpr int NT = StagedShape<K>::NT;
-    constexpr int NQ = (MODE == kSpmvAp) ? 1 : 2;
+    constexpr int NQW = (MODE == kSpmvAp) ? 1 : (MODE == kEisAsS) ? 3 : 2;
     const int nc = (int)c.colour_ptr.size() - 1;
+    int slot = 0;
     for (int col = nc - 1; col >= 0; --col) {
         const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
-        launch_staged(k_eis_bwd_st<R, K, FUSE_P>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
-                      c.seg.work_col + s0, s1 - s0, c.D, c.B, z, p, r, vv, (const BicgState*)st, w);
+        auto kb = k_eis_bwd_st<R, K, FUSE>;
+        const int g = staged_grid(kb, NT, c.seg.stage_up, s1 - s0, 1 << 20);
+        if (FUSE == 2 && slot + g > c.eis_slots) throw std::runtime_error("Eisenstat partial-sum scratch too small");
+        kb<<<g, NT, 2 * c.seg.stage_up, c.stream>>>(c.seg, c.seg.work_col + s0, s1 - s0, c.D, c.B, z, p, r, vv,
+                                                      (const BicgState*)st, w,
+                                                      c.eis_partial + (size_t)slot * NQW * K);
         check_launch(c.launches);
+        if (FUSE == 2) slot += g;
     }
-    const cplx<R>* zz = FUSE_P ? (const cplx<R>*)p : z;
-    int slot = 0;
+    const cplx<R>* zz = FUSE != 0 ? (const cplx<R>*)p : z;
     for (int col = 0; col < nc; ++col) {
         const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
@@ -969,11 +1027,13 @@ void eis_apply_k(const KrylovCtx<R>& c, const cplx<R>* z, cplx<R>* p, const cplx
         if (slot + g > c.eis_slots) throw std::runtime_error("Eisenstat partial-sum scratch too small");
         kf<<<g, NT, 2 * c.seg.stage_lo, c.stream>>>(c.seg, c.seg.work_col + s0, s1 - s0, c.D, c.B, zz,
                                                       (const cplx<R>*)w, y, out, aux,
-                                                      c.eis_partial + (size_t)slot * NQ * K);
+                                                      c.eis_partial + (size_t)slot * NQW * K);
         check_launch(c.launches);
         slot += g;
     }
-    k_eis_reduce<K, MODE><<<1, kBlock, 0, c.stream>>>(c.eis_partial, slot, st);
+    const int gr = std::max(1, (slot + kEisSlotsPerBlock - 1) / kEisSlotsPerBlock);
+    if (gr > c.red.max_blocks) throw std::runtime_error("Eisenstat reduction grid beyond the reduction scratch");
+    k_eis_reduce<K, MODE><<<gr, kBlock, 0, c.stream>>>(c.eis_partial, slot, st, c.red);
     check_launch(c.launches);
 }
 
@@ -1001,15 +1061,12 @@ void eis_iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* s
     const double vb = (double)c.n_rows * K * sizeof(cplx<R>);
     // p update + v = A_hat p: matrix once, r, p (read, write), v (read, write), w (write, read), y
     int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + 9 * vb, K) : -1;
-    eis_apply_k<R, K, true, kSpmvAp>(c, nullptr, v.p, v.r, v.v, st, v.ph, v.y, v.v, v.r0);
+    eis_apply_k<R, K, 1, kSpmvAp>(c, nullptr, v.p, v.r, v.v, st, v.ph, v.y, v.v, v.r0);
     if (c.timer) c.timer->end(th);
-    th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
-    k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
-    check_launch(c.launches);
-    if (c.timer) c.timer->end(th);
-    // t = A_hat s: matrix once, s (twice), w (write, read), y, t, dot operand s
-    th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + 7 * vb, K) : -1;
-    eis_apply_k<R, K, false, kSpmvAs>(c, v.s, nullptr, nullptr, nullptr, st, v.ph, v.y, v.t, v.s);
+    // s = r - alpha v with |s|^2, and t = A_hat s: matrix once, r, v, s (write,
+    // read twice), w (write, read), y, t
+    th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + 9 * vb, K) : -1;
+    eis_apply_k<R, K, 2, kEisAsS>(c, nullptr, v.s, v.r, v.v, st, v.ph, v.y, v.t, v.s);
     if (c.timer) c.timer->end(th);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
     k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.p, v.s, v.s,
@@ -1025,9 +1082,10 @@ void eis_finish_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, cplx<R>* out) {
     for (int col = nc - 1; col >= 0; --col) {
         const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
-        launch_staged(k_eis_bwd_st<R, K, false>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+        launch_staged(k_eis_bwd_st<R, K, 0>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
                       c.seg.work_col + s0, s1 - s0, c.D, c.B, (const cplx<R>*)v.x, (cplx<R>*)nullptr,
-                      (const cplx<R>*)nullptr, (const cplx<R>*)nullptr, (const BicgState*)nullptr, out);
+                      (const cplx<R>*)nullptr, (const cplx<R>*)nullptr, (const BicgState*)nullptr, out,
+                      (double2*)nullptr);
         check_launch(c.launches);
     }
 }

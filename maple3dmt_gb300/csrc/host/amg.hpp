@@ -34,7 +34,7 @@ struct AmgHierarchy {
 struct AmgOptions {
     double theta = 0.08;      // strength threshold |a_ij| >= theta sqrt(a_ii a_jj)
     double omega_p = 2.0 / 3.0; // prolongator smoothing weight (times D^-1 A)
-    int max_coarse = 600;     // stop coarsening at or below this many rows
+    int max_coarse = 200;     // stop coarsening at or below this many rows
     int max_levels = 8;
 };
 

@@ -883,10 +883,11 @@ void GpuSolver::ensure_vecs32b(int K) {
         d_lane_sel = dalloc<int>(dev::kMaxRhs);
     }
     if (!d_eis_partial) {
-        // one slot per block of every colour launch: colours x (32 resident blocks per SM)
+        // one slot per block of every backward and forward colour launch of
+        // an operator application: 2 x colours x (32 resident blocks per SM)
         int sms = 0;
         cuda_ok(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "sm count");
-        eis_slots = std::max(1, n_colours()) * 32 * std::max(1, sms);
+        eis_slots = 2 * std::max(1, n_colours()) * 32 * std::max(1, sms);
         d_eis_partial = dalloc<double2>((size_t)eis_slots * dev::kMaxQ * dev::kMaxRhs);
     }
     kv32b_K = K;
