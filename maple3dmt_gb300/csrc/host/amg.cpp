@@ -1,10 +1,11 @@
-// Smoothed-aggregation AMG setup (see amg.hpp).  Aggregation follows Vanek,
+// Aggregation AMG setup (see amg.hpp).  Aggregation follows Vanek,
 // Mandel and Brezina, "Algebraic multigrid by smoothed aggregation for second
 // and fourth order elliptic problems", Computing 56 (1996): strength of
 // connection |a_ij| >= theta sqrt(a_ii a_jj), greedy aggregates around roots
 // whose strong neighbourhood is still free, leftovers attached to the
 // aggregate they are most strongly tied to; tentative prolongator piecewise
-// constant, smoothed by one damped Jacobi step; Galerkin coarse operators.
+// constant, optionally smoothed by one damped Jacobi step (omega_p > 0);
+// Galerkin coarse operators.
 #include "host/amg.hpp"
 
 #include <algorithm>

@@ -1,8 +1,10 @@
-// Smoothed-aggregation algebraic multigrid hierarchy for the node Laplacian
+// Aggregation algebraic multigrid hierarchy for the node Laplacian
 // of the divergence correction (the Poisson operator of divcorr_poisson_,
 // src/forward/forward_solver_fv.cpp:623-722, built by build_div_laplacian,
 // src/octree/operators.cpp:952-1019).  Host-side setup only; the V-cycle runs
-// on the GPU (cuda/amg.cu).  The reference preconditions this PCG with
+// on the GPU (mg_apply in cuda/physics.cu).  The solver builds it with
+// piecewise-constant prolongation (omega_p = 0); the smoothed prolongator of
+// the option is kept for the setup tests.  The reference preconditions this PCG with
 // Jacobi; the multigrid V-cycle is a stronger symmetric positive-definite
 // preconditioner for the same system and the same stopping rule.
 #pragma once
