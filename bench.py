@@ -61,6 +61,10 @@ def parse():
                     help="divergence-correction PCG: 0 Jacobi (the reference's), 1 aggregation multigrid")
     ap.add_argument("--row-kernels", type=int, default=1, choices=[0, 1],
                     help="0: CSR rows read by the lanes; 1: slice-staged rows (bulk copies to shared memory)")
+    ap.add_argument("--gradcorr", type=int, default=1, choices=[0, 1],
+                    help="1: gradient-space term (multigrid V-cycle on the divergence-correction Laplacian) in "
+                         "the FP32 inner solve's preconditioner for frequencies <= --gradcorr-fmax")
+    ap.add_argument("--gradcorr-fmax", type=float, default=1e30)
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -237,12 +241,12 @@ def run_ours(args, rank, world, local_rank):
     sv, obs, err = workload(args)
     if args.plain:
         args.precision, args.forward, args.row_kernels, args.divcorr_precond = "fp64", "reference", 0, 0
-        args.ssor_form = 0
+        args.ssor_form, args.gradcorr = 0, 0
     s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=args.maxiter,
                           precision=1 if args.precision == "mixed" else 0,
                           forward_interleaved=1 if args.forward == "interleaved" else 0,
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
-                          ssor_form=args.ssor_form)
+                          ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -337,6 +341,8 @@ def run_ours(args, rank, world, local_rank):
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
                    "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
+                   "gradcorr": (f"multigrid gradient-space term, f <= {args.gradcorr_fmax:g} Hz"
+                                if args.gradcorr else "off"),
                    "arm": "plain (per frequency, complex128)" if args.plain else "batched",
                    "l2": "inputs larger than L2 (matrix alone 260 MB)",
                    "parallelism": f"replica x{world}"},

@@ -118,6 +118,13 @@ typedef struct m3d_params {
                                  reference's), 1 aggregation multigrid V-cycle */
     int ssor_form;            /* mixed-precision inner solve: 0 right-preconditioned SSOR-BiCGStab
                                  as the reference, 1 Eisenstat split form (staged rows) */
+    int gradcorr;             /* 1: the mixed-precision inner solve adds a gradient-space term
+                                 G (i omega L)^-1 G^T (one multigrid V-cycle on the divergence-
+                                 correction Laplacian L) to the SSOR preconditioner of the
+                                 right-hand sides with f <= gradcorr_fmax; needs div_correction.
+                                 Batches with such a right-hand side run the right-preconditioned
+                                 form.  0: SSOR alone (the reference's preconditioner) */
+    double gradcorr_fmax;     /* Hz */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -240,7 +247,7 @@ int m3d_timer_start(m3d_solver* s);
 int m3d_timer_stop(m3d_solver* s, double* ms);
 
 /* Kernel classes: 0 SpMV, 1 SSOR apply (all colour sweeps), 2 Krylov vector
- * updates, 3 divergence correction, 4 other.  bytes = algorithmic bytes
+ * updates, 3 divergence correction, 4 gradient-space term of the preconditioner.  bytes = algorithmic bytes
  * (matrix entries, diagonals and vector streams each counted once). */
 typedef struct m3d_kernel_times {
     long long launches[5];

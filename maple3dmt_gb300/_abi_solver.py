@@ -27,6 +27,8 @@ class Params(C.Structure):
         ("row_kernels", C.c_int),
         ("divcorr_precond", C.c_int),
         ("ssor_form", C.c_int),
+        ("gradcorr", C.c_int),
+        ("gradcorr_fmax", C.c_double),
     ]
 
 
@@ -63,7 +65,7 @@ class KernelTimes(C.Structure):
     ]
 
 
-KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "other")
+KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "gradcorr")
 
 SOLVER_SYMBOLS = [
     "m3d_params_default", "m3d_solver_create", "m3d_solver_destroy", "m3d_last_error",

@@ -23,7 +23,8 @@ LIB = os.path.join(LIB_DIR, "libm3d_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRCS = ["host/octree_build.cpp", "host/mesh_capi.cpp", "host/layout.cpp", "host/layout_capi.cpp", "host/amg.cpp"]
-CUDA_SRCS = ["cuda/krylov.cu", "cuda/physics.cu", "cuda/dot.cu", "solver.cu", "capi.cu", "noalloc.cu"]
+CUDA_SRCS = ["cuda/krylov.cu", "cuda/physics.cu", "cuda/gradcorr.cu", "cuda/dot.cu", "solver.cu", "capi.cu",
+             "noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,78 @@
+// Gradient-space correction of the SSOR preconditioner (auxiliary nodal
+// space) for the complex-FP32 inner solve.
+//
+// At low frequency A = C^T Mf^-1 C + i omega Me is nearly singular on
+// discrete gradients: C G = 0, so for a gradient g = G phi on the free edges
+// A g = i omega Me g, and G~^T A G~ = i omega L, where G~ is the edge-node
+// gradient of build_gradient (src/octree/operators.cpp) restricted to free
+// edges (rows that are not identity rows of the eliminated system) and to
+// the nodes that are not Dirichlet nodes of the divergence correction, and L
+// is exactly the Poisson operator of divcorr_poisson_
+// (src/forward/forward_solver_fv.cpp:623-722, build_div_laplacian
+// src/octree/operators.cpp:952-1019) with its Dirichlet rows.  SSOR damps
+// the curl part of the error but barely moves the gradient part, which is
+// why the reference interleaves divergence corrections between BiCGStab
+// bursts.  Here the preconditioner itself gets the gradient-space term:
+//
+//     B r = M_ssor^-1 r + G~ (i omega L)^-1 G~^T r,
+//
+// the additive two-level form of Hiptmair's hybrid smoother, with (L)^-1
+// replaced by one V-cycle of the aggregation multigrid that already
+// preconditions the divergence-correction PCG (host/amg.cpp).  B is a
+// different preconditioner for the same system, so the converged solution
+// and the FP64 true-residual test are unchanged; only the iteration count
+// drops (at 0.01 Hz by an order of magnitude).
+//
+// The V-cycle runs in FP32 on [n][K] complex node vectors, reading the FP64
+// level operators of the device hierarchy (level 0 through the node
+// incidence of the divergence-correction Laplacian, coarser levels CSR), so
+// a conductivity update that refreshes the hierarchy refreshes it here too.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "krylov.cuh"
+#include "physics.cuh"
+
+namespace m3d {
+
+struct GcLevel {
+    int n = 0;
+    const int *ptr = nullptr, *col = nullptr;   // A_l in CSR (levels >= 1)
+    const double* val = nullptr;
+    const double* dinv = nullptr;               // Jacobi scale 1 / a_ii
+    const int* agg = nullptr;                   // [n] aggregate in level l+1 (-1: none)
+    const int *rptr = nullptr, *rcol = nullptr; // members of each aggregate of level l+1
+    float2 *b = nullptr, *x = nullptr, *y = nullptr;   // [n][kMaxRhs] right side, pre-, post-smoothed
+};
+
+struct GcDev {
+    int n_levels = 0;          // 0: correction unavailable
+    int nn = 0;
+    // level 0 = the divergence-correction Laplacian in incidence form
+    const int *inc_ptr = nullptr, *inc_other = nullptr;
+    const double *lap_off = nullptr, *lap_diag = nullptr;
+    // restriction G~^T (per incidence entry) and prolongation G~ (per
+    // permuted edge row, two entries), zero on masked edges / nodes
+    const int* inc_edge = nullptr;
+    const float* inc_g = nullptr;
+    const int* e_node = nullptr;
+    const float* e_g = nullptr;
+    GcLevel lv[phys::kAmgMaxLevels];
+    int n_coarse = 0;
+    const double* coarse_inv = nullptr;   // [n_coarse][n_coarse]
+    float omega = 2.0f / 3.0f;            // smoother damping
+    double omega_max = 0.0;               // lanes with angular frequency <= omega_max are corrected
+    long inc_entries = 0;                 // incidence entries (algorithmic bytes)
+};
+
+// Masked FP32 restriction / prolongation weights (once per mesh).
+void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s);
+
+// out += G~ V(G~^T in) / (i omega_k) on the lanes k of B with
+// 0 < omega_k <= g.omega_max; in and out are [n_pad][B.K] complex FP32.
+template <int K>
+void gc_apply_k(const GcDev& g, const BatchView& B, int n_pad, int n_rows, const float2* in, float2* out,
+                cudaStream_t s, long long* launches, KernelTimer* timer);
+
+}  // namespace m3d

@@ -1,11 +1,14 @@
 // Batched SSOR-BiCGStab kernels.  See krylov.cuh for what they restate.
 #include "krylov.cuh"
 
+#include "gradcorr.cuh"
+
 #include <algorithm>
 #include <map>
 #include <mutex>
 #include <stdexcept>
 #include <tuple>
+#include <type_traits>
 #include <utility>
 
 namespace m3d {
@@ -725,6 +728,15 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) 
     if (c.timer) c.timer->end(th);
 }
 
+// out += G~ V(G~^T in) / (i omega): the gradient-space term of the
+// preconditioner (complex FP32 only)
+template <class R, int K>
+void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* out) {
+    if constexpr (std::is_same<R, float>::value) {
+        if (c.gc) gc_apply_k<K>(*c.gc, c.B, c.n_pad, c.n_rows, in, out, c.stream, c.launches, c.timer);
+    }
+}
+
 template <class R, int K>
 void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     const long n = (long)c.n_pad * K;
@@ -735,12 +747,14 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.p, v.y, v.ph);
+    gc_term<R, K>(c, v.p, v.ph);
     spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
     k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.s, v.y, v.sh);
+    gc_term<R, K>(c, v.s, v.sh);
     spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
     k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);

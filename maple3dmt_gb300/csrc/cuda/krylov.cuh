@@ -71,7 +71,7 @@ struct BatchView {
 };
 
 // Optional CUDA-event timing of kernel classes on the solver's stream.
-enum KernelClass : int { kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsOther = 4, kNumCls = 5 };
+enum KernelClass : int { kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsGradcorr = 4, kNumCls = 5 };
 struct KernelTimer {
     bool on = false;
     cudaStream_t stream = nullptr;
@@ -92,6 +92,8 @@ struct KernelTimer {
     void reset();
     ~KernelTimer();
 };
+
+struct GcDev;   // gradient-space correction of the preconditioner (gradcorr.cuh)
 
 // Everything one launch of the batched solver needs.
 template <class R>
@@ -120,6 +122,9 @@ struct KrylovCtx {
     // partial sums of the sweeps' dot products, summed by one reduction kernel
     double2* eis_partial = nullptr;   // [eis_slots][kMaxQ * kMaxRhs]
     int eis_slots = 0;
+    // right-preconditioned form only (complex FP32): when set, each SSOR
+    // apply is followed by the gradient-space term of the preconditioner
+    const GcDev* gc = nullptr;
 };
 
 enum RowKernels : int { kRowsDirect = 0, kRowsStaged = 1 };

@@ -608,7 +608,7 @@ void GpuSolver::ensure_sigma_device() {
         phys::dc_build_laplacian(md, d_me_dc, dc, stream);
         ++launches;
         lap_built = true;
-        if (P.divcorr_precond == 1) build_amg();
+        if (want_amg()) build_amg();
     }
 }
 
@@ -618,6 +618,63 @@ void GpuSolver::free_amg() {
     amg_mem.clear();
     amg = phys::AmgDev{};
     amg_ok = false;
+    for (void* p : gc_mem) cudaFree(p);
+    gc_mem.clear();
+    gc = GcDev{};
+    gc_ok = false;
+}
+
+// Gradient-space correction over the device hierarchy just built: level 0
+// reads the divergence-correction Laplacian through the node incidence, the
+// coarser levels the hierarchy's CSR operators (both refreshed in place for
+// a new conductivity); FP32 work vectors for up to 16 right-hand sides.
+void GpuSolver::build_gc() {
+    if (!amg_ok || P.gradcorr != 1 || P.precision != 1) return;
+    auto zeros2 = [&](size_t n) {
+        float2* p = dalloc_zero<float2>(n, stream);
+        gc_mem.push_back((void*)p);
+        return p;
+    };
+    const long n_inc = (long)h_inc_other.size();
+    float* inc_g = dalloc<float>((size_t)std::max<long>(1, n_inc));
+    gc_mem.push_back((void*)inc_g);
+    float* e_g = dalloc<float>(2 * (size_t)n_pad);
+    gc_mem.push_back((void*)e_g);
+    gc_weights(md, inc_g, e_g, stream);
+    ++launches;
+    gc.n_levels = amg.n_levels;
+    gc.nn = L.nn;
+    gc.inc_ptr = md.inc_ptr;
+    gc.inc_other = md.inc_other;
+    gc.inc_edge = md.inc_edge;
+    gc.lap_off = dc.lap_off;
+    gc.lap_diag = dc.lap_diag;
+    gc.inc_g = inc_g;
+    gc.e_node = md.e_node;
+    gc.e_g = e_g;
+    for (int l = 0; l < amg.n_levels; ++l) {
+        const phys::AmgLevelDev& a = amg.lv[l];
+        GcLevel& g = gc.lv[l];
+        g.n = a.n;
+        g.ptr = a.ptr;
+        g.col = a.col;
+        g.val = a.val;
+        g.dinv = a.dinv;
+        g.agg = a.agg;
+        g.rptr = a.rptr;
+        g.rcol = a.rcol;
+        const size_t n = (size_t)a.n * dev::kMaxRhs;
+        g.b = zeros2(n);
+        g.x = zeros2(n);
+        g.y = zeros2(n);
+    }
+    gc.n_coarse = amg.n_coarse;
+    gc.coarse_inv = amg.coarse_inv;
+    gc.omega = (float)amg.omega;
+    gc.omega_max = 2.0 * kPi * P.gradcorr_fmax;
+    gc.inc_entries = n_inc;
+    sync();
+    gc_ok = true;
 }
 
 // Aggregation multigrid hierarchy of the node Laplacian just built on the
@@ -722,6 +779,7 @@ void GpuSolver::build_amg() {
     amg.coarse_inv = up(H.coarse_inv);
     amg_ok = true;
     sync();
+    build_gc();
     amg_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -1079,7 +1137,16 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             cuda_ok(cudaMemcpyAsync(d_lane_map, map.data(), sizeof(int) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "map");
             cuda_ok(cudaMemcpyAsync(d_scale, sc.data(), sizeof(double) * dev::kMaxRhs, cudaMemcpyHostToDevice, stream), "scale");
         };
-        const bool eis = P.ssor_form == 1 && P.row_kernels == kRowsStaged;
+        // the gradient-space term needs the right-preconditioned form: a
+        // batch with a corrected right-hand side runs that form throughout
+        bool use_gc = false;
+        if (gc_ok && P.gradcorr == 1)
+            for (int j = 0; j < Kc; ++j)
+                if (lanes[j] >= 0) {
+                    const double om = 2.0 * kPi * fz_freqs[fmap[lanes[j]]];
+                    use_gc |= om > 0.0 && om <= gc.omega_max;
+                }
+        const bool eis = !use_gc && P.ssor_form == 1 && P.row_kernels == kRowsStaged;
         // flushes lanes with add[j] set: x64 += scale * d32, d32 the x-space
         // correction (x_hat mapped back by (D + U)^-1 in the Eisenstat form)
         auto flush = [&](const KrylovCtx<float>& cc, const KrylovVecs<float>& v, int Kn) {
@@ -1109,6 +1176,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
         }
         cuda_ok(cudaMemcpyAsync(d_states, ls.data(), sizeof(BicgState) * Kc, cudaMemcpyHostToDevice, stream), "states");
         KrylovCtx<float> c32 = kctx32(Kc, fm.data());
+        if (use_gc) c32.gc = &gc;
         if (eis) eis_init(c32, cur, d_states);
         else bicg_init(c32, cur, d_states);
         int it = 0;
@@ -1155,6 +1223,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 std::swap(cur_cap, other_cap);
                 Kc = Kn;
                 c32 = kctx32(Kc, fm.data());
+                if (use_gc) c32.gc = &gc;
             }
             for (int i = 0; i < chunk && it < maxiter; ++i, ++it) {
                 if (eis) eis_iteration(c32, cur, d_states);

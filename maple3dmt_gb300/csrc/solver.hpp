@@ -12,6 +12,7 @@
 #include "host/layout.hpp"
 #include "cuda/krylov.cuh"
 #include "cuda/physics.cuh"
+#include "cuda/gradcorr.cuh"
 
 namespace m3d {
 
@@ -105,6 +106,13 @@ private:
     void build_amg();
     void free_amg();
     const phys::AmgDev* amg_or_null() const { return (amg_ok && P.divcorr_precond == 1) ? &amg : nullptr; }
+    // gradient-space term of the FP32 inner solve's preconditioner, on the
+    // same hierarchy (FP32 work vectors, masked transfer weights)
+    GcDev gc{};
+    bool gc_ok = false;
+    std::vector<void*> gc_mem;
+    void build_gc();
+    bool want_amg() const { return P.divcorr_precond == 1 || (P.gradcorr == 1 && P.precision == 1); }
     int* d_lap_qpos = nullptr;    // incidence -> value slot in dc.lap_seg
     void build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs, const std::vector<int>& ecol,
                         const std::vector<double>& eval);

@@ -41,12 +41,15 @@ def g_small(lib):
     return load_golden("small_block")
 
 
+@pytest.mark.parametrize("gradcorr", [0, 1])
 @pytest.mark.parametrize("row_kernels", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("interleaved", [0, 1])
-def test_forward_matches_oracle(g_small, precision, interleaved, row_kernels):
+def test_forward_matches_oracle(g_small, precision, interleaved, row_kernels, gradcorr):
+    if precision == 0 and gradcorr == 1:
+        pytest.skip("the gradient-space term is part of the mixed-precision solve only")
     g = g_small
-    s = _gpu(g, precision=precision, forward_interleaved=interleaved, row_kernels=row_kernels)
+    s = _gpu(g, precision=precision, forward_interleaved=interleaved, row_kernels=row_kernels, gradcorr=gradcorr)
     o = _oracle(g)
     for fr in g["freqs"]:
         Zg = s.compute_single_frequency(fr)
@@ -121,19 +124,24 @@ def test_jv_pieces_match_oracle(g_small):
         assert rel(s.extract_delta_impedance_complex(xo, pol), o.delta_impedance(xo, pol)) < 1e-8
 
 
+@pytest.mark.parametrize("gradcorr", [0, 1])
 @pytest.mark.parametrize("ssor_form", [0, 1])
 @pytest.mark.parametrize("divcorr_precond", [0, 1])
 @pytest.mark.parametrize("precision", [0, 1])
-def test_gradient_batch_matches_reference(g_small, precision, divcorr_precond, ssor_form):
+def test_gradient_batch_matches_reference(g_small, precision, divcorr_precond, ssor_form, gradcorr):
     """Against the reference's own outputs; both PCG preconditioners of the
     divergence correction (Jacobi as the reference, aggregation multigrid)
     stop at the same 1e-10 relative residual, and both forms of the FP32
-    SSOR-BiCGStab (right-preconditioned as the reference, Eisenstat split)
-    are driven to the same FP64 true residual."""
-    if precision == 0 and ssor_form == 1:
-        pytest.skip("the split form is used by the mixed-precision solve only")
+    SSOR-BiCGStab (right-preconditioned as the reference, Eisenstat split),
+    with and without the gradient-space term of the preconditioner, are
+    driven to the same FP64 true residual."""
+    if precision == 0 and (ssor_form == 1 or gradcorr == 1):
+        pytest.skip("the split form and the gradient-space term belong to the mixed-precision solve")
+    if gradcorr == 1 and ssor_form == 1:
+        pytest.skip("batches with the gradient-space term run the right-preconditioned form")
     g = g_small
-    s = _gpu(g, precision=precision, forward_interleaved=1, divcorr_precond=divcorr_precond, ssor_form=ssor_form)
+    s = _gpu(g, precision=precision, forward_interleaved=1, divcorr_precond=divcorr_precond, ssor_form=ssor_form,
+             gradcorr=gradcorr)
     Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
     ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
     assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
@@ -215,6 +223,30 @@ def test_c2_scale_divcorr_preconditioners_agree(lib):
         assert all(t <= 1e-7 for t in st["true_residual"][:4]), st
         s.close()
     assert rel(Zs[1], Zs[0]) < 1e-5
+
+
+def test_c2_scale_gradient_correction_low_frequency(lib):
+    """Full-size mesh at 0.01 Hz, both polarisations: with the gradient-space
+    term the reference's forward strategy (BiCGStab to 1e-7, then the
+    divergence correction) converges in a small fraction of the iterations
+    that SSOR alone needs with interleaved corrections, and the impedances of
+    the two agree to 1e-5 relative (both solves stop at the 1e-7 FP64 true
+    residual)."""
+    from maple3dmt_gb300 import mesh
+    from maple3dmt_gb300.solver import solver_for_survey
+    sv = mesh.layered_block_survey(min_level=6)
+    runs = []
+    for gc, inter in ((0, 1), (1, 0)):
+        s = solver_for_survey(sv, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1, forward_interleaved=inter,
+                              gradcorr=gc)
+        Z = s.forward_batch(sv.freqs[:1])
+        st = s.stats()
+        assert all(t <= 1e-7 for t in st["true_residual"][:2]), st
+        runs.append((Z, st["iterations"][:2]))
+        s.close()
+    (Z0, it0), (Z1, it1) = runs
+    assert max(it1) * 4 < min(it0), (it0, it1)
+    assert rel(Z1, Z0) < 1e-5
 
 
 @pytest.mark.parametrize("K", [1, 2, 4, 8, 16])
