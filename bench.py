@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--forward", default="interleaved", choices=["interleaved", "reference"])
+    ap.add_argument("--forward", default="reference", choices=["interleaved", "reference"])
     ap.add_argument("--min-level", type=int, default=6)
     ap.add_argument("--max-level", type=int, default=7)
     ap.add_argument("--nfreq", type=int, default=8)
@@ -65,6 +65,8 @@ def parse():
                     help="1: gradient-space term (multigrid V-cycle on the divergence-correction Laplacian) in "
                          "the FP32 inner solve's preconditioner for frequencies <= --gradcorr-fmax")
     ap.add_argument("--gradcorr-fmax", type=float, default=1e30)
+    ap.add_argument("--gradcorr-presmooth", type=int, default=0, choices=[0, 1],
+                    help="V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1)")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -246,7 +248,8 @@ def run_ours(args, rank, world, local_rank):
                           precision=1 if args.precision == "mixed" else 0,
                           forward_interleaved=1 if args.forward == "interleaved" else 0,
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
-                          ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax)
+                          ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
+                          gradcorr_presmooth=args.gradcorr_presmooth)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -341,8 +344,8 @@ def run_ours(args, rank, world, local_rank):
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
                    "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
-                   "gradcorr": (f"multigrid gradient-space term, f <= {args.gradcorr_fmax:g} Hz"
-                                if args.gradcorr else "off"),
+                   "gradcorr": (f"multigrid gradient-space term, V({args.gradcorr_presmooth},1), "
+                                f"f <= {args.gradcorr_fmax:g} Hz" if args.gradcorr else "off"),
                    "arm": "plain (per frequency, complex128)" if args.plain else "batched",
                    "l2": "inputs larger than L2 (matrix alone 260 MB)",
                    "parallelism": f"replica x{world}"},

@@ -125,6 +125,7 @@ typedef struct m3d_params {
                                  Batches with such a right-hand side run the right-preconditioned
                                  form.  0: SSOR alone (the reference's preconditioner) */
     double gradcorr_fmax;     /* Hz */
+    int gradcorr_presmooth;   /* V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1) */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;

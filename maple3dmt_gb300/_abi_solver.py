@@ -29,6 +29,7 @@ class Params(C.Structure):
         ("ssor_form", C.c_int),
         ("gradcorr", C.c_int),
         ("gradcorr_fmax", C.c_double),
+        ("gradcorr_presmooth", C.c_int),
     ]
 
 

@@ -54,11 +54,11 @@ struct XPlain {
     __device__ __forceinline__ float2 operator()(int j, int k, int K) const { return x[(size_t)j * K + k]; }
 };
 struct XProlonged {
-    const float2* x;
+    const float2* x;     // null: the level was not pre-smoothed (x = 0)
     const int* agg;
     const float2* xc;
     __device__ __forceinline__ float2 operator()(int j, int k, int K) const {
-        float2 v = x[(size_t)j * K + k];
+        float2 v = x ? x[(size_t)j * K + k] : f2(0.0f, 0.0f);
         const int a = __ldg(&agg[j]);
         if (a >= 0) {
             const float2 c = xc[(size_t)a * K + k];
@@ -125,12 +125,19 @@ __global__ void __launch_bounds__(kGcBlock) k_gc_restrict_edges(GcDev g, const f
         const int v = (int)(i / K), k = (int)(i % K);
         float2 acc = f2(0.0f, 0.0f);
         const int q0 = __ldg(&g.inc_ptr[v]), q1 = __ldg(&g.inc_ptr[v + 1]);
-        for (int q = q0; q < q1; ++q) {
-            const float w = __ldg(&g.inc_g[q]);
-            if (w == 0.0f) continue;
-            const float2 e = in[(size_t)__ldg(&g.inc_edge[q]) * K + k];
-            acc.x += w * e.x;
-            acc.y += w * e.y;
+        for (int q = q0; q < q1; q += 4) {
+            float w[4];
+            float2 e[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                w[u] = q + u < q1 ? __ldg(&g.inc_g[q + u]) : 0.0f;
+                e[u] = w[u] != 0.0f ? in[(size_t)__ldg(&g.inc_edge[q + u]) * K + k] : f2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                acc.x += w[u] * e[u].x;
+                acc.y += w[u] * e[u].y;
+            }
         }
         L.b[i] = acc;
         if (presmooth) {
@@ -140,21 +147,40 @@ __global__ void __launch_bounds__(kGcBlock) k_gc_restrict_edges(GcDev g, const f
     }
 }
 
-// b_{l+1}[I] = sum over members i of aggregate I of (b - A_l x)_i, and the
-// pre-smoothed x_{l+1} = omega D^-1 b_{l+1} unless l+1 is the coarsest level
+// r_l = b - A_l x, written to y (free until the up-sweep)
 template <int K, bool L0>
-__global__ void __launch_bounds__(kGcBlock) k_gc_down(GcDev g, GcLevel L, GcLevel N, int presmooth) {
-    const long n = (long)N.n * K;
+__global__ void __launch_bounds__(kGcBlock) k_gc_resid(GcDev g, GcLevel L) {
+    const long n = (long)L.n * K;
     const XPlain xf{L.x};
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int row = (int)(i / K), k = (int)(i % K);
+        const float2 ax = level_row<K, L0>(g, L, row, xf, k);
+        const float2 bv = L.b[i];
+        L.y[i] = f2(bv.x - ax.x, bv.y - ax.y);
+    }
+}
+
+// b_{l+1}[I] = sum of the level-l residual src over the members of aggregate
+// I (src = b_l when level l is not pre-smoothed), and the pre-smoothed
+// x_{l+1} = omega D^-1 b_{l+1} when level l+1 is
+template <int K>
+__global__ void __launch_bounds__(kGcBlock) k_gc_restrict(GcDev g, GcLevel L, GcLevel N, const float2* __restrict__ src,
+                                                          int presmooth) {
+    const long n = (long)N.n * K;
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const int I = (int)(i / K), k = (int)(i % K);
         float2 acc = f2(0.0f, 0.0f);
-        for (int m = __ldg(&L.rptr[I]); m < __ldg(&L.rptr[I + 1]); ++m) {
-            const int row = __ldg(&L.rcol[m]);
-            const float2 ax = level_row<K, L0>(g, L, row, xf, k);
-            const float2 bv = L.b[(size_t)row * K + k];
-            acc.x += bv.x - ax.x;
-            acc.y += bv.y - ax.y;
+        const int m0 = __ldg(&L.rptr[I]), m1 = __ldg(&L.rptr[I + 1]);
+        for (int m = m0; m < m1; m += 4) {
+            float2 r[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                r[u] = m + u < m1 ? src[(size_t)__ldg(&L.rcol[m + u]) * K + k] : f2(0.0f, 0.0f);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                acc.x += r[u].x;
+                acc.y += r[u].y;
+            }
         }
         N.b[i] = acc;
         if (presmooth) {
@@ -164,71 +190,51 @@ __global__ void __launch_bounds__(kGcBlock) k_gc_down(GcDev g, GcLevel L, GcLeve
     }
 }
 
-// coarsest level: x = A_c^-1 b (dense)
+// coarsest level: x = A_c^-1 b (dense); one block per row, thread t on
+// lane t % K and columns j = t / K (mod kGcBlock / K), summed in shared memory
 template <int K>
 __global__ void __launch_bounds__(kGcBlock) k_gc_coarse(int nc, const double* __restrict__ inv,
                                                         const float2* __restrict__ b, float2* __restrict__ x) {
-    const long n = (long)nc * K;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int row = (int)(i / K), k = (int)(i % K);
+    constexpr int G = kGcBlock / K;
+    __shared__ float2 part[kGcBlock];
+    const int k = threadIdx.x % K, grp = threadIdx.x / K;
+    for (int row = blockIdx.x; row < nc; row += gridDim.x) {
         float2 s = f2(0.0f, 0.0f);
-        for (int j = 0; j < nc; ++j) {
+        for (int j = grp; j < nc; j += G) {
             const float a = (float)__ldg(&inv[(size_t)row * nc + j]);
             const float2 v = b[(size_t)j * K + k];
             s.x += a * v.x;
             s.y += a * v.y;
         }
-        x[i] = s;
+        part[threadIdx.x] = s;
+        __syncthreads();
+        if (grp == 0) {
+            float2 t = f2(0.0f, 0.0f);
+            for (int q = 0; q < G; ++q) {
+                const float2 p = part[q * K + k];
+                t.x += p.x;
+                t.y += p.y;
+            }
+            x[(size_t)row * K + k] = t;
+        }
+        __syncthreads();
     }
 }
 
 // y_l = x~ + omega D^-1 (b - A_l x~), x~ = x_l + P xc (prolongation fused)
 template <int K, bool L0>
-__global__ void __launch_bounds__(kGcBlock) k_gc_up(GcDev g, GcLevel L, const float2* __restrict__ xc) {
+__global__ void __launch_bounds__(kGcBlock) k_gc_up(GcDev g, GcLevel L, const float2* __restrict__ xc,
+                                                    float2* __restrict__ out, int presmoothed) {
     const long n = (long)L.n * K;
-    const XProlonged xf{L.x, L.agg, xc};
+    const XProlonged xf{presmoothed ? L.x : nullptr, L.agg, xc};
     for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const int row = (int)(i / K), k = (int)(i % K);
         const float2 ax = level_row<K, L0>(g, L, row, xf, k);
         const float2 xt = xf(row, k, K);
         const float2 bv = L.b[i];
         const float sc = g.omega * (float)__ldg(&L.dinv[row]);
-        L.y[i] = f2(xt.x + sc * (bv.x - ax.x), xt.y + sc * (bv.y - ax.y));
+        out[i] = f2(xt.x + sc * (bv.x - ax.x), xt.y + sc * (bv.y - ax.y));
     }
-}
-
-struct LaneScale {
-    float s[kMaxRhs];
-};
-
-// out_e += (G~ y0)_e / (i omega_k) = s_k (g.y, -g.x), s_k = 1 / omega_k
-template <int K>
-__global__ void __launch_bounds__(kGcBlock) k_gc_prolong_edges(GcDev g, int n_pad, const float2* __restrict__ y0,
-                                                               float2* __restrict__ out, LaneScale ls) {
-    const long n = (long)n_pad * K;
-    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int r = (int)(i / K), k = (int)(i % K);
-        const float s = ls.s[k];
-        if (s == 0.0f) continue;
-        const float g0 = __ldg(&g.e_g[2 * r]), g1 = __ldg(&g.e_g[2 * r + 1]);
-        if (g0 == 0.0f && g1 == 0.0f) continue;
-        const float2 a = y0[(size_t)__ldg(&g.e_node[2 * r]) * K + k];
-        const float2 b = y0[(size_t)__ldg(&g.e_node[2 * r + 1]) * K + k];
-        const float gx = g0 * a.x + g1 * b.x, gy = g0 * a.y + g1 * b.y;
-        float2 o = out[i];
-        o.x += s * gy;
-        o.y -= s * gx;
-        out[i] = o;
-    }
-}
-
-LaneScale lane_scale(const GcDev& g, const BatchView& B) {
-    LaneScale ls{};
-    for (int k = 0; k < kMaxRhs; ++k) {
-        const double om = k < B.K ? B.omega[k] : 0.0;
-        ls.s[k] = (om > 0.0 && om <= g.omega_max) ? (float)(1.0 / om) : 0.0f;
-    }
-    return ls;
 }
 
 }  // namespace
@@ -239,58 +245,70 @@ void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s) {
     gc_check(nullptr);
 }
 
+GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which) {
+    GcRowTerm t;
+    t.ya = g.out0[which];
+    t.e_node = g.e_node;
+    t.e_g = g.e_g;
+    for (int k = 0; k < kMaxRhs; ++k) {
+        const double om = k < B.K ? B.omega[k] : 0.0;
+        t.s[k] = (om > 0.0 && om <= g.omega_max) ? (float)(1.0 / om) : 0.0f;
+    }
+    return t;
+}
+
 template <int K>
-void gc_apply_k(const GcDev& g, const BatchView& B, int n_pad, int n_rows, const float2* in, float2* out,
-                cudaStream_t s, long long* launches, KernelTimer* timer) {
+void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
+                KernelTimer* timer) {
     const int nl = g.n_levels;
     if (nl < 1) return;
-    const LaneScale ls = lane_scale(g, B);
-    // edge vectors: in read once, out read and written; level-0 node vectors
-    // b, x (written, read back), y (written, read by the prolongation); the
-    // Laplacian's incidence entries (value + column) twice; the transfer
-    // weights once
+    float2* out = g.out0[which];
+    // the edge vector gathered once; level-0 node vectors b, x (written, read
+    // back), the scratch residual (written, read by the restriction), the
+    // result (written); the Laplacian's incidence entries (value + column)
+    // twice; the restriction weights once
     const double eb = (double)n_rows * K * sizeof(float2), nb = (double)g.nn * K * sizeof(float2);
-    const double bytes = 3 * eb + 7 * nb + 2.0 * g.inc_entries * 12 + (double)g.inc_entries * 8 + (double)n_rows * 16;
+    const double bytes = eb + 7 * nb + 2.0 * g.inc_entries * 12 + (double)g.inc_entries * 8;
     const int th = timer ? timer->begin(kClsGradcorr, bytes, K) : -1;
-    k_gc_restrict_edges<K><<<gc_grid((long)g.nn * K), kGcBlock, 0, s>>>(g, in, nl > 1 ? 1 : 0);
+    const int pre = g.presmooth && nl > 1 ? 1 : 0;   // V(1,1) or V(0,1)
+    k_gc_restrict_edges<K><<<gc_grid((long)g.nn * K), kGcBlock, 0, s>>>(g, in, pre);
     gc_check(launches);
-    const float2* y0 = nullptr;
     if (nl == 1) {
-        k_gc_coarse<K><<<gc_grid((long)g.nn * K), kGcBlock, 0, s>>>(g.n_coarse, g.coarse_inv, g.lv[0].b, g.lv[0].y);
+        k_gc_coarse<K><<<std::max(1, g.n_coarse), kGcBlock, 0, s>>>(g.n_coarse, g.coarse_inv, g.lv[0].b, out);
         gc_check(launches);
-        y0 = g.lv[0].y;
     } else {
         for (int l = 0; l + 1 < nl; ++l) {
-            const int pre = (l + 1 < nl - 1) ? 1 : 0;
-            const long work = (long)g.lv[l + 1].n * K;
-            if (l == 0) k_gc_down<K, true><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], g.lv[l + 1], pre);
-            else k_gc_down<K, false><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], g.lv[l + 1], pre);
+            const int pre_next = (pre && l + 1 < nl - 1) ? 1 : 0;
+            const long rw = (long)g.lv[l].n * K;
+            const float2* src = g.lv[l].b;
+            if (pre) {   // residual of the pre-smoothed iterate, in y
+                if (l == 0) k_gc_resid<K, true><<<gc_grid(rw), kGcBlock, 0, s>>>(g, g.lv[l]);
+                else k_gc_resid<K, false><<<gc_grid(rw), kGcBlock, 0, s>>>(g, g.lv[l]);
+                gc_check(launches);
+                src = g.lv[l].y;
+            }
+            k_gc_restrict<K><<<gc_grid((long)g.lv[l + 1].n * K), kGcBlock, 0, s>>>(g, g.lv[l], g.lv[l + 1], src,
+                                                                                    pre_next);
             gc_check(launches);
         }
         const GcLevel& C = g.lv[nl - 1];
-        k_gc_coarse<K><<<gc_grid((long)C.n * K), kGcBlock, 0, s>>>(g.n_coarse, g.coarse_inv, C.b, C.x);
+        k_gc_coarse<K><<<std::max(1, g.n_coarse), kGcBlock, 0, s>>>(g.n_coarse, g.coarse_inv, C.b, C.x);
         gc_check(launches);
         for (int l = nl - 2; l >= 0; --l) {
             const float2* xc = (l + 1 == nl - 1) ? g.lv[l + 1].x : g.lv[l + 1].y;
+            float2* dst = l == 0 ? out : g.lv[l].y;
             const long work = (long)g.lv[l].n * K;
-            if (l == 0) k_gc_up<K, true><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc);
-            else k_gc_up<K, false><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc);
+            if (l == 0) k_gc_up<K, true><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc, dst, pre);
+            else k_gc_up<K, false><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc, dst, pre);
             gc_check(launches);
         }
-        y0 = g.lv[0].y;
     }
-    k_gc_prolong_edges<K><<<gc_grid((long)n_pad * K), kGcBlock, 0, s>>>(g, n_pad, y0, out, ls);
-    gc_check(launches);
     if (timer) timer->end(th);
 }
 
-template void gc_apply_k<2>(const GcDev&, const BatchView&, int, int, const float2*, float2*, cudaStream_t,
-                            long long*, KernelTimer*);
-template void gc_apply_k<4>(const GcDev&, const BatchView&, int, int, const float2*, float2*, cudaStream_t,
-                            long long*, KernelTimer*);
-template void gc_apply_k<8>(const GcDev&, const BatchView&, int, int, const float2*, float2*, cudaStream_t,
-                            long long*, KernelTimer*);
-template void gc_apply_k<16>(const GcDev&, const BatchView&, int, int, const float2*, float2*, cudaStream_t,
-                             long long*, KernelTimer*);
+template void gc_apply_k<2>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<4>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<8>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<16>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
 
 }  // namespace m3d

@@ -43,7 +43,7 @@ struct GcLevel {
     const double* dinv = nullptr;               // Jacobi scale 1 / a_ii
     const int* agg = nullptr;                   // [n] aggregate in level l+1 (-1: none)
     const int *rptr = nullptr, *rcol = nullptr; // members of each aggregate of level l+1
-    float2 *b = nullptr, *x = nullptr, *y = nullptr;   // [n][kMaxRhs] right side, pre-, post-smoothed
+    float2 *b = nullptr, *x = nullptr, *y = nullptr;   // [n][kMaxRhs] right side, pre-smoothed, scratch / post-smoothed
 };
 
 struct GcDev {
@@ -58,10 +58,12 @@ struct GcDev {
     const float* inc_g = nullptr;
     const int* e_node = nullptr;
     const float* e_g = nullptr;
+    float2* out0[2] = {nullptr, nullptr};   // [nn][kMaxRhs] V-cycle results for p and for s
     GcLevel lv[phys::kAmgMaxLevels];
     int n_coarse = 0;
     const double* coarse_inv = nullptr;   // [n_coarse][n_coarse]
     float omega = 2.0f / 3.0f;            // smoother damping
+    int presmooth = 0;                    // 1: V(1,1) cycle; 0: V(0,1) (post-smoothing only)
     double omega_max = 0.0;               // lanes with angular frequency <= omega_max are corrected
     long inc_entries = 0;                 // incidence entries (algorithmic bytes)
 };
@@ -69,10 +71,14 @@ struct GcDev {
 // Masked FP32 restriction / prolongation weights (once per mesh).
 void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s);
 
-// out += G~ V(G~^T in) / (i omega_k) on the lanes k of B with
-// 0 < omega_k <= g.omega_max; in and out are [n_pad][B.K] complex FP32.
+// g.out0[which] = V(G~^T in), one V-cycle on every lane; in is
+// [n_pad][K] complex FP32.  The term G~ out0 / (i omega) is added per row by
+// the SpMV and the x update (GcRowTerm).
 template <int K>
-void gc_apply_k(const GcDev& g, const BatchView& B, int n_pad, int n_rows, const float2* in, float2* out,
-                cudaStream_t s, long long* launches, KernelTimer* timer);
+void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
+                KernelTimer* timer);
+
+// Row term over g.out0[which] for the lanes k of B with 0 < omega_k <= g.omega_max.
+GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which);
 
 }  // namespace m3d

@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, Bat
                                                  const cplx<R>* __restrict__ x, cplx<R>* __restrict__ y,
                                                  const cplx<R>* __restrict__ aux,
                                                  cplx<R>* __restrict__ aux_out, BicgState* st,
-                                                 RedScratch rs) {
+                                                 RedScratch rs, GcRowTerm gt) {
     using C = cplx<R>;
     constexpr int RPW = Rpw<K>::v;
     constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kSpmvAs || MODE == kSpmvTrueRes) ? 2 : 3;
@@ -256,7 +256,13 @@ __global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, Bat
         const C s = row_dot<R, K>(A, A.rp[row], A.rp[row + 1], x, rhs);
         const size_t i = (size_t)row * K + rhs;
         const C d = diag_of(D, row, om);
-        const C yv = cadd(s, cmul(d, x[i]));
+        C yv = cadd(s, cmul(d, x[i]));
+        if ((MODE == kSpmvAp || MODE == kSpmvAs) && gt.ya && gt.s[rhs] != 0.0f) {
+            const float2 g = gc_grad_row(gt, gt.ya, row, rhs, K);
+            const R me = D.sm[row].y;
+            yv.x += me * (R)g.x;
+            yv.y += me * (R)g.y;
+        }
         if (MODE == kSpmvPlain) {
             y[i] = yv;
         } else if (MODE == kSpmvAp) {
@@ -357,7 +363,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
                                                                 cplx<R>* __restrict__ y,
                                                                 const cplx<R>* __restrict__ aux,
                                                                 cplx<R>* __restrict__ aux_out, BicgState* st,
-                                                                RedScratch rs) {
+                                                                RedScratch rs, GcRowTerm gt) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
@@ -367,6 +373,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
     const int rhs = lane % K;
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
+    const float2* gy = ((MODE == kSpmvAp || MODE == kSpmvAs) && gt.s[rhs] != 0.0f) ? gt.ya : nullptr;
     C accR[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) accR[q] = cm<R>(0, 0);
@@ -383,7 +390,13 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
             const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
             const C d = diag_of(D, row, om);
             const C s = seg_row_dot_lu<R, K>(lo, up, lr, x, rhs);
-            const C yv = cadd(s, cmul(d, xi));
+            C yv = cadd(s, cmul(d, xi));
+            if ((MODE == kSpmvAp || MODE == kSpmvAs) && gy) {
+                const float2 g = gc_grad_row(gt, gy, row, rhs, K);
+                const R me = D.sm[row].y;
+                yv.x += me * (R)g.x;
+                yv.y += me * (R)g.y;
+            }
             if (MODE == kSpmvPlain) {
                 y[i] = yv;
             } else if (MODE == kSpmvAp) {
@@ -547,7 +560,7 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
                                                       const cplx<R>* __restrict__ sh,
                                                       const cplx<R>* __restrict__ s,
                                                       const cplx<R>* __restrict__ t, BicgState* st,
-                                                      RedScratch rs) {
+                                                      RedScratch rs, GcRowTerm gt) {
     using C = cplx<R>;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
@@ -556,12 +569,29 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
     const bool run = S.status == kRunning;
     const bool pend = S.pend_x != 0;
     const C al = from_d<C>(S.alpha), om = from_d<C>(S.omega);
+    const bool term = gt.ya && gt.s[rhs] != 0.0f;
+    const R sc = (R)gt.s[rhs];
+    // c = G~ y / (i omega) = sc (g.y, -g.x)
+    auto corr = [&](const float2* y, long i) {
+        const float2 g = gc_grad_row(gt, y, (int)(i / K), rhs, K);
+        return cm<R>(sc * (R)g.y, -sc * (R)g.x);
+    };
     R rr = 0;
     C r0r = cm<R>(0, 0);
     for (long i = i0; i < n; i += stride) {
-        if (pend) { x[i] = cadd(x[i], cmul(al, ph[i])); continue; }
+        if (pend) {
+            C php = ph[i];
+            if (term) php = cadd(php, corr(gt.ya, i));
+            x[i] = cadd(x[i], cmul(al, php));
+            continue;
+        }
         if (!run) continue;
-        x[i] = cadd(x[i], cadd(cmul(al, ph[i]), cmul(om, sh[i])));
+        C php = ph[i], shs = sh[i];
+        if (term) {
+            php = cadd(php, corr(gt.ya, i));
+            shs = cadd(shs, corr(gt.yb, i));
+        }
+        x[i] = cadd(x[i], cadd(cmul(al, php), cmul(om, shs)));
         const C rv = csub(s[i], cmul(om, t[i]));
         r[i] = rv;
         rr += rv.x * rv.x + rv.y * rv.y;
@@ -604,7 +634,7 @@ double matrix_bytes(const KrylovCtx<R>& c) {
 
 template <class R, int K>
 void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
-                 cplx<R>* aux_out, BicgState* st) {
+                 cplx<R>* aux_out, BicgState* st, const GcRowTerm& gt) {
     constexpr int NT = StagedShape<K>::NT;
     const long ns = c.n_pad / kSlice;
     const int sb = c.seg.stage_spmv;
@@ -614,30 +644,30 @@ void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, 
     switch (mode) {
         case kSpmvPlain:
             launch_staged(k_spmv_st<R, K, kSpmvPlain>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red);
+                          aux_out, st, c.red, gt);
             break;
         case kSpmvAp:
             launch_staged(k_spmv_st<R, K, kSpmvAp>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red);
+                          aux_out, st, c.red, gt);
             break;
         case kSpmvAs:
             launch_staged(k_spmv_st<R, K, kSpmvAs>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red);
+                          aux_out, st, c.red, gt);
             break;
         case kSpmvInit:
             launch_staged(k_spmv_st<R, K, kSpmvInit>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red);
+                          aux_out, st, c.red, gt);
             break;
         default:
             launch_staged(k_spmv_st<R, K, kSpmvTrueRes>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red);
+                          aux_out, st, c.red, gt);
             break;
     }
 }
 
 template <class R, int K>
 void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
-            cplx<R>* aux_out, BicgState* st) {
+            cplx<R>* aux_out, BicgState* st, const GcRowTerm& gt = GcRowTerm{}) {
     const long warps = (long)c.A.n_pad / Rpw<K>::v;
     int grid;
     if (mode == kSpmvPlain) {
@@ -646,37 +676,39 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
         grid = c.grid_spmv;
     }
     const int streams = 2 + (aux ? 1 : 0) + (aux_out ? 1 : 0);
-    const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
+    // the gradient-space term: two node indices and weights per row
+    const double term = gt.ya ? (double)c.n_rows * 16 : 0.0;
+    const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) + term +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * streams, K) : -1;
     const int cap = c.red.max_blocks;
     if (c.row_kernels == kRowsStaged) {
-        spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st);
+        spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st, gt);
         check_launch(c.launches);
         if (c.timer) c.timer->end(th);
         return;
     }
     switch (mode) {
         case kSpmvPlain:
-            k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
             break;
         case kSpmvAp: {
             auto kf = k_spmv<R, K, kSpmvAp>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
             break;
         }
         case kSpmvAs: {
             auto kf = k_spmv<R, K, kSpmvAs>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
             break;
         }
         case kSpmvInit: {
             auto kf = k_spmv<R, K, kSpmvInit>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
             break;
         }
         default: {
             auto kf = k_spmv<R, K, kSpmvTrueRes>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
             break;
         }
     }
@@ -728,12 +760,13 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) 
     if (c.timer) c.timer->end(th);
 }
 
-// out += G~ V(G~^T in) / (i omega): the gradient-space term of the
-// preconditioner (complex FP32 only)
+// One V-cycle of the gradient-space term on G~^T in (complex FP32 only),
+// output in the node buffer `which` (0: for p, 1: for s); the SpMV and the x
+// update add the term per row (GcRowTerm).
 template <class R, int K>
-void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* out) {
+void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, int which) {
     if constexpr (std::is_same<R, float>::value) {
-        if (c.gc) gc_apply_k<K>(*c.gc, c.B, c.n_pad, c.n_rows, in, out, c.stream, c.launches, c.timer);
+        if (c.gc) gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.stream, c.launches, c.timer);
     }
 }
 
@@ -746,18 +779,25 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     k_update_p<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.p, v.v, st);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
+    GcRowTerm gp, gs, gx;
+    if (c.gc) {
+        gp = gc_row_term(*c.gc, c.B, 0);
+        gs = gc_row_term(*c.gc, c.B, 1);
+        gx = gp;
+        gx.yb = gs.ya;
+    }
     ssor_k<R, K>(c, v.p, v.y, v.ph);
-    gc_term<R, K>(c, v.p, v.ph);
-    spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
+    gc_term<R, K>(c, v.p, 0);
+    spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st, gp);
     th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
     k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
     ssor_k<R, K>(c, v.s, v.y, v.sh);
-    gc_term<R, K>(c, v.s, v.sh);
-    spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
-    th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
-    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
+    gc_term<R, K>(c, v.s, 1);
+    spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st, gs);
+    th = c.timer ? c.timer->begin(kClsVec, 8 * vb + (c.gc ? (double)c.n_rows * 16 : 0.0), K) : -1;
+    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red, gx);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
 }
@@ -1084,7 +1124,7 @@ void eis_iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* s
     if (c.timer) c.timer->end(th);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
     k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.p, v.s, v.s,
-                                                                              v.t, st, c.red);
+                                                                              v.t, st, c.red, GcRowTerm{});
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
 }

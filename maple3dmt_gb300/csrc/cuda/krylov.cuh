@@ -70,6 +70,30 @@ struct BatchView {
     double omega[dev::kMaxRhs];   // angular frequency of each right-hand side
 };
 
+// Per-row gradient-space term of the right-preconditioned FP32 iteration
+// (gradcorr.cuh): with y the node vector of one multigrid V-cycle and
+// c = G~ y / (i omega) the term added to the preconditioned vector,
+//  * the SpMV adds A c = i omega Me c = Me_i (G~ y)_i (A G~ = i omega Me G~,
+//    the curl of a gradient being zero), so c itself is never stored;
+//  * the x update adds alpha c_p + omega c_s.
+// G~ y at permuted row i = e_g[2i] y[e_node[2i]] + e_g[2i+1] y[e_node[2i+1]].
+struct GcRowTerm {
+    const float2* ya = nullptr;   // V-cycle output for p (SpMV: for the vector multiplied)
+    const float2* yb = nullptr;   // V-cycle output for s (x update only)
+    const int* e_node = nullptr;
+    const float* e_g = nullptr;
+    float s[dev::kMaxRhs] = {};   // 1 / omega of each lane; 0: no term on that lane
+};
+
+__device__ __forceinline__ float2 gc_grad_row(const GcRowTerm& t, const float2* __restrict__ y, int row, int rhs,
+                                              int K) {
+    const float g0 = __ldg(&t.e_g[2 * row]), g1 = __ldg(&t.e_g[2 * row + 1]);
+    if (g0 == 0.0f && g1 == 0.0f) return make_float2(0.0f, 0.0f);
+    const float2 a = y[(size_t)__ldg(&t.e_node[2 * row]) * K + rhs];
+    const float2 b = y[(size_t)__ldg(&t.e_node[2 * row + 1]) * K + rhs];
+    return make_float2(g0 * a.x + g1 * b.x, g0 * a.y + g1 * b.y);
+}
+
 // Optional CUDA-event timing of kernel classes on the solver's stream.
 enum KernelClass : int { kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsGradcorr = 4, kNumCls = 5 };
 struct KernelTimer {

@@ -668,9 +668,11 @@ void GpuSolver::build_gc() {
         g.x = zeros2(n);
         g.y = zeros2(n);
     }
+    for (int w = 0; w < 2; ++w) gc.out0[w] = zeros2((size_t)L.nn * dev::kMaxRhs);
     gc.n_coarse = amg.n_coarse;
     gc.coarse_inv = amg.coarse_inv;
     gc.omega = (float)amg.omega;
+    gc.presmooth = P.gradcorr_presmooth;
     gc.omega_max = 2.0 * kPi * P.gradcorr_fmax;
     gc.inc_entries = n_inc;
     sync();

@@ -62,6 +62,23 @@ def test_forward_matches_oracle(g_small, precision, interleaved, row_kernels, gr
         o.release()
 
 
+@pytest.mark.parametrize("presmooth", [0, 1])
+def test_gradient_correction_cycles_match_oracle(g_small, presmooth):
+    """Both V-cycles of the gradient-space term (V(1,1), V(0,1)) give the
+    oracle's impedances and fields at the 1e-10 solve."""
+    g = g_small
+    s = _gpu(g, precision=1, gradcorr=1, gradcorr_presmooth=presmooth)
+    o = _oracle(g)
+    for fr in g["freqs"]:
+        Zg = s.compute_single_frequency(fr)
+        st = s.stats()
+        assert all(t <= 1e-8 for t in st["true_residual"][:2]), st
+        assert rel(Zg, o.solve_frequency(fr)) < Z_TOL
+        for p in (0, 1):
+            assert rel(s.background_E(p), o.E(p)) < F_TOL
+        o.release()
+
+
 def test_forward_matches_reference_golden(g_small):
     g = g_small
     s = _gpu(g)
