@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--gradcorr-fmax", type=float, default=1e30)
     ap.add_argument("--gradcorr-presmooth", type=int, default=0, choices=[0, 1],
                     help="V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1)")
+    ap.add_argument("--divcorr-mixed", type=int, default=1, choices=[0, 1],
+                    help="1: divergence-correction Poisson solve as FP32 PCG inside FP64 refinement")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -243,13 +245,13 @@ def run_ours(args, rank, world, local_rank):
     sv, obs, err = workload(args)
     if args.plain:
         args.precision, args.forward, args.row_kernels, args.divcorr_precond = "fp64", "reference", 0, 0
-        args.ssor_form, args.gradcorr = 0, 0
+        args.ssor_form, args.gradcorr, args.divcorr_mixed = 0, 0, 0
     s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=args.maxiter,
                           precision=1 if args.precision == "mixed" else 0,
                           forward_interleaved=1 if args.forward == "interleaved" else 0,
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
                           ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
-                          gradcorr_presmooth=args.gradcorr_presmooth)
+                          gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -343,6 +345,7 @@ def run_ours(args, rank, world, local_rank):
                    "tol": 1e-7, "precision": args.precision, "forward": args.forward,
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
+                   "divcorr_solve": ["fp64 pcg", "fp32 pcg in fp64 refinement"][args.divcorr_mixed],
                    "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
                    "gradcorr": (f"multigrid gradient-space term, V({args.gradcorr_presmooth},1), "
                                 f"f <= {args.gradcorr_fmax:g} Hz" if args.gradcorr else "off"),

@@ -126,6 +126,10 @@ typedef struct m3d_params {
                                  form.  0: SSOR alone (the reference's preconditioner) */
     double gradcorr_fmax;     /* Hz */
     int gradcorr_presmooth;   /* V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1) */
+    int divcorr_mixed;        /* 1 (with precision 1, divcorr_precond 1): the divergence-correction Poisson solve runs as
+                                 complex-FP32 PCG (FP32 multigrid V(1,1) preconditioner) inside FP64
+                                 iterative refinement, stopped by the FP64 true residual at the
+                                 reference's 1e-10 |divJ|; 0: FP64 PCG */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;

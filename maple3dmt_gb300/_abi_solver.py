@@ -30,6 +30,7 @@ class Params(C.Structure):
         ("gradcorr", C.c_int),
         ("gradcorr_fmax", C.c_double),
         ("gradcorr_presmooth", C.c_int),
+        ("divcorr_mixed", C.c_int),
     ]
 
 

@@ -77,6 +77,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->gradcorr = 1;
     p->gradcorr_fmax = 1e30;
     p->gradcorr_presmooth = 0;
+    p->divcorr_mixed = 1;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -110,7 +111,8 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
         params->sigma_bg <= 0 || params->precision < 0 || params->precision > 1 || params->row_kernels < 0 ||
         params->row_kernels > 1 || params->divcorr_precond < 0 || params->divcorr_precond > 1 ||
         params->ssor_form < 0 || params->ssor_form > 1 || params->gradcorr < 0 || params->gradcorr > 1 ||
-        !(params->gradcorr_fmax >= 0.0) || params->gradcorr_presmooth < 0 || params->gradcorr_presmooth > 1)
+        !(params->gradcorr_fmax >= 0.0) || params->gradcorr_presmooth < 0 || params->gradcorr_presmooth > 1 ||
+        params->divcorr_mixed < 0 || params->divcorr_mixed > 1)
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
 }

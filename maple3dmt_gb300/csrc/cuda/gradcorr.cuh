@@ -46,6 +46,13 @@ struct GcLevel {
     float2 *b = nullptr, *x = nullptr, *y = nullptr;   // [n][kMaxRhs] right side, pre-smoothed, scratch / post-smoothed
 };
 
+// Per right-hand side state of the FP32 PCG of the mixed-precision
+// divergence-correction solve.
+struct GcPcgState {
+    double rho, tol, rz, alpha, beta;
+    int run, iter, ref, pad_;
+};
+
 struct GcDev {
     int n_levels = 0;          // 0: correction unavailable
     int nn = 0;
@@ -66,6 +73,9 @@ struct GcDev {
     int presmooth = 0;                    // 1: V(1,1) cycle; 0: V(0,1) (post-smoothing only)
     double omega_max = 0.0;               // lanes with angular frequency <= omega_max are corrected
     long inc_entries = 0;                 // incidence entries (algorithmic bytes)
+    // FP32 PCG work of the mixed-precision divergence-correction solve, [nn][kMaxRhs]
+    float2 *dc_x = nullptr, *dc_r = nullptr, *dc_z = nullptr, *dc_p = nullptr, *dc_ap = nullptr;
+    GcPcgState* dc_st = nullptr;          // [kMaxRhs]
 };
 
 // Masked FP32 restriction / prolongation weights (once per mesh).
@@ -77,6 +87,16 @@ void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s);
 template <int K>
 void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
                 KernelTimer* timer);
+
+// Solves L phi = divJ for the right-hand sides of w with cg_run set (the
+// PCG stage of divcorr_poisson_, forward_solver_fv.cpp:668-710): FP64
+// iterative refinement around FP32 PCG solves preconditioned by the FP32
+// V(1,1) cycle, until |divJ - L phi| < 1e-10 |divJ| in FP64.  Leaves phi in
+// w.phi, clears cg_run, adds the FP32 iterations to each cg_iter and the
+// batched iterations to *sweeps.  Returns the kernel launches.
+template <int K>
+long long dc_poisson_mixed_k(const GcDev& g, int nn, phys::DcWork w, dev::RedScratch red, cudaStream_t s,
+                             long long* sweeps);
 
 // Row term over g.out0[which] for the lanes k of B with 0 < omega_k <= g.omega_max.
 GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which);

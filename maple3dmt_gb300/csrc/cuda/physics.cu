@@ -1,6 +1,7 @@
 // Non-Krylov kernels of the solve path.  See physics.cuh for the reference
 // code each launcher restates.
 #include "physics.cuh"
+#include "gradcorr.cuh"
 #include "staged.cuh"
 
 #include <algorithm>
@@ -1123,7 +1124,7 @@ void dc_phi0(const MeshDev& m, VecK rhs, const RhsInfo& info, DcWork w, cudaStre
 template <int K>
 long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
                     double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
-                    DcCounters* counters, const AmgDev* amg) {
+                    DcCounters* counters, const AmgDev* amg, const GcDev* mixed) {
     if (counters) counters->calls += 1;
     long long launches = 0;
     std::vector<DcState> hs(K);
@@ -1148,6 +1149,21 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
         bool any = false;
         for (int k = 0; k < K; ++k) any |= (hs[k].active && !hs[k].done);
         if (!any) break;
+        if (mixed) {
+            long long sweeps = 0;
+            launches += dc_poisson_mixed_k<K>(*mixed, m.nn, w, red, s, &sweeps);
+            cudaMemcpyAsync(hs.data(), w.st, sizeof(DcState) * K, cudaMemcpyDeviceToHost, s);
+            cudaStreamSynchronize(s);
+            if (counters) {
+                counters->outer += 1;
+                counters->cg_sweeps += sweeps;
+                for (int k = 0; k < K; ++k) if (hs[k].active && !hs[k].done) counters->cg_iterations += hs[k].cg_iter;
+            }
+            k_dc_grad<<<ge, kBlock, 0, s>>>(m, E, w);
+            k_dc_outer_done<<<1, 32, 0, s>>>(K, w);
+            ck(); launches += 2;
+            continue;
+        }
         if (amg) {
             // z = M^-1 divJ, rz, p = z
             k_mg_cg_init<K><<<g_p, kBlock, 0, s>>>(m.nn, w);
@@ -1199,12 +1215,12 @@ long long divcorr_k(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0
 
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w, int max_outer,
                   double tol, const int* active_host, RedScratch red, cudaStream_t s, int cg_chunk,
-                  DcCounters* counters, const AmgDev* amg) {
+                  DcCounters* counters, const AmgDev* amg, const GcDev* mixed) {
     switch (E.K) {
-        case 2: return divcorr_k<2>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
-        case 4: return divcorr_k<4>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
-        case 8: return divcorr_k<8>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
-        case 16: return divcorr_k<16>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg);
+        case 2: return divcorr_k<2>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg, mixed);
+        case 4: return divcorr_k<4>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg, mixed);
+        case 8: return divcorr_k<8>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg, mixed);
+        case 16: return divcorr_k<16>(m, me_dc, E, use_phi0, w, max_outer, tol, active_host, red, s, cg_chunk, counters, amg, mixed);
         default: throw std::runtime_error("divergence correction batch must be 2, 4, 8 or 16");
     }
 }

@@ -12,6 +12,8 @@
 
 namespace m3d {
 
+struct GcDev;   // FP32 node multigrid (gradcorr.cuh)
+
 // Row flags (permuted edge rows).
 enum : unsigned char {
     kFlagConstrained = 1,   // identity row in A (solve BC or dead)   forward_solver_fv.cpp:214-217
@@ -170,9 +172,12 @@ struct AmgDev {
     double omega = 2.0 / 3.0;             // smoother damping
 };
 
+// With `mixed` set, the Poisson solve of each round is the mixed-precision
+// one of gradcorr.cuh (FP32 PCG inside FP64 refinement, same stopping rule).
 long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, DcWork w,
                   int max_outer, double tol, const int* active_host, dev::RedScratch red,
-                  cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr, const AmgDev* amg = nullptr);
+                  cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr, const AmgDev* amg = nullptr,
+                  const GcDev* mixed = nullptr);
 
 // ---- stations (forward_solver_fv.cpp:1490-1727, :1804-2065) ----
 // Z and H cache per (frequency f, station); E1 = rhs 2f, E2 = rhs 2f+1 of E.

@@ -629,7 +629,7 @@ void GpuSolver::free_amg() {
 // coarser levels the hierarchy's CSR operators (both refreshed in place for
 // a new conductivity); FP32 work vectors for up to 16 right-hand sides.
 void GpuSolver::build_gc() {
-    if (!amg_ok || P.gradcorr != 1 || P.precision != 1) return;
+    if (!amg_ok || P.precision != 1 || (P.gradcorr != 1 && P.divcorr_mixed != 1)) return;
     auto zeros2 = [&](size_t n) {
         float2* p = dalloc_zero<float2>(n, stream);
         gc_mem.push_back((void*)p);
@@ -669,11 +669,17 @@ void GpuSolver::build_gc() {
         g.y = zeros2(n);
     }
     for (int w = 0; w < 2; ++w) gc.out0[w] = zeros2((size_t)L.nn * dev::kMaxRhs);
+    if (P.divcorr_mixed == 1) {
+        for (float2** q : {&gc.dc_x, &gc.dc_r, &gc.dc_z, &gc.dc_p, &gc.dc_ap}) *q = zeros2((size_t)L.nn * dev::kMaxRhs);
+        GcPcgState* st = dalloc_zero<GcPcgState>(dev::kMaxRhs, stream);
+        gc_mem.push_back((void*)st);
+        gc.dc_st = st;
+    }
     gc.n_coarse = amg.n_coarse;
     gc.coarse_inv = amg.coarse_inv;
     gc.omega = (float)amg.omega;
     gc.presmooth = P.gradcorr_presmooth;
-    gc.omega_max = 2.0 * kPi * P.gradcorr_fmax;
+    gc.omega_max = P.gradcorr == 1 ? 2.0 * kPi * P.gradcorr_fmax : 0.0;
     gc.inc_entries = n_inc;
     sync();
     gc_ok = true;
@@ -1142,7 +1148,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
         // the gradient-space term needs the right-preconditioned form: a
         // batch with a corrected right-hand side runs that form throughout
         bool use_gc = false;
-        if (gc_ok && P.gradcorr == 1)
+        if (gc_ok && P.gradcorr == 1 && gc.omega_max > 0.0)
             for (int j = 0; j < Kc; ++j)
                 if (lanes[j] >= 0) {
                     const double om = 2.0 * kPi * fz_freqs[fmap[lanes[j]]];
@@ -1312,7 +1318,7 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
         ensure_dc(K);
         const int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
         launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
-                                  red, stream, 25, &dcc, amg_or_null());
+                                  red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
         timer.end(th);
     }
     phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
@@ -1389,7 +1395,7 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
     ++launches;
     int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
     launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                              active.data(), red, stream, 25, &dcc, amg_or_null());
+                              active.data(), red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
     timer.end(th);
     std::vector<int> done(K, 0);
     std::vector<double> prev(K, 1e30);
@@ -1422,7 +1428,7 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
         if (!anyd) break;
         th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
         launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                                  dca.data(), red, stream, 25, &dcc, amg_or_null());
+                                  dca.data(), red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
         timer.end(th);
         std::vector<BicgState> hs(K);
         for (int k = 0; k < K; ++k) {

@@ -112,7 +112,13 @@ private:
     bool gc_ok = false;
     std::vector<void*> gc_mem;
     void build_gc();
-    bool want_amg() const { return P.divcorr_precond == 1 || (P.gradcorr == 1 && P.precision == 1); }
+    bool want_amg() const {
+        return P.divcorr_precond == 1 || (P.precision == 1 && (P.gradcorr == 1 || P.divcorr_mixed == 1));
+    }
+    const GcDev* mixed_or_null() const {
+        return (gc_ok && P.divcorr_mixed == 1 && P.divcorr_precond == 1 && P.precision == 1 && gc.dc_st) ? &gc
+                                                                                                     : nullptr;
+    }
     int* d_lap_qpos = nullptr;    // incidence -> value slot in dc.lap_seg
     void build_segments(const std::vector<int>& op_rp, const std::vector<int>& op_rs, const std::vector<int>& ecol,
                         const std::vector<double>& eval);

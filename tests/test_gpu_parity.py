@@ -79,6 +79,20 @@ def test_gradient_correction_cycles_match_oracle(g_small, presmooth):
         o.release()
 
 
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_divcorr_mixed_matches_reference(g_small, mixed):
+    """The divergence-correction Poisson solve as FP64 PCG and as FP32 PCG
+    inside FP64 refinement (both stopped at the FP64 residual 1e-10 |divJ|)
+    give the reference's impedances and gradient."""
+    g = g_small
+    s = _gpu(g, precision=1, forward_interleaved=1, divcorr_precond=1, divcorr_mixed=mixed)
+    Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
+    ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
+    assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
+    assert rel(grad, g["ref_grad"]) < G_TOL
+    assert s.stats()["divcorr_calls"] > 0
+
+
 def test_forward_matches_reference_golden(g_small):
     g = g_small
     s = _gpu(g)
