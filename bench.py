@@ -69,6 +69,8 @@ def parse():
                     help="V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1)")
     ap.add_argument("--divcorr-mixed", type=int, default=1, choices=[0, 1],
                     help="1: divergence-correction Poisson solve as FP32 PCG inside FP64 refinement")
+    ap.add_argument("--inner-tol-floor", type=float, default=1e-5,
+                    help="smallest relative residual asked of one complex-FP32 inner solve")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -251,7 +253,8 @@ def run_ours(args, rank, world, local_rank):
                           forward_interleaved=1 if args.forward == "interleaved" else 0,
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
                           ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
-                          gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed)
+                          gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
+                          inner_tol_floor=args.inner_tol_floor)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -342,7 +345,8 @@ def run_ours(args, rank, world, local_rank):
         "config": {"workload": f"layered+block earth, octree levels {args.min_level}/{args.max_level} "
                                f"({s.ne} edges, {s.nc} cells), 121 stations, {nf} freqs 0.01-100 Hz, "
                                f"forward+adjoint+sensitivity gradient step ({solves_per_step} solves)",
-                   "tol": 1e-7, "precision": args.precision, "forward": args.forward,
+                   "tol": 1e-7, "precision": args.precision, "inner_tol_floor": args.inner_tol_floor,
+                   "forward": args.forward,
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
                    "divcorr_solve": ["fp64 pcg", "fp32 pcg in fp64 refinement"][args.divcorr_mixed],

@@ -31,6 +31,7 @@ class Params(C.Structure):
         ("gradcorr_fmax", C.c_double),
         ("gradcorr_presmooth", C.c_int),
         ("divcorr_mixed", C.c_int),
+        ("inner_tol_floor", C.c_double),
     ]
 
 

@@ -49,6 +49,14 @@ __global__ void k_gc_weights(MeshDev m, float* __restrict__ inc_g, float* __rest
     }
 }
 
+__global__ void k_gc_pack0(GcDev g) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.nn) return;
+    g.lap_diag32[v] = (float)g.lap_diag[v];
+    for (int q = g.inc_ptr[v]; q < g.inc_ptr[v + 1]; ++q)
+        g.lap_pk[q] = make_int2(g.inc_other[q], __float_as_int((float)g.lap_off[q]));
+}
+
 // x~_j of the up-sweep: level iterate plus the prolonged coarse correction
 struct XPlain {
     const float2* x;
@@ -75,22 +83,22 @@ template <int K, bool L0, class XF>
 __device__ __forceinline__ float2 level_row(const GcDev& g, const GcLevel& L, int row, const XF& xf, int k) {
     float2 s = f2(0.0f, 0.0f);
     if (L0) {
-        const float dg = (float)__ldg(&g.lap_diag[row]);
+        const float dg = __ldg(&g.lap_diag32[row]);
         const float2 xr = xf(row, k, K);
         s.x = dg * xr.x;
         s.y = dg * xr.y;
         const int q0 = __ldg(&g.inc_ptr[row]), q1 = __ldg(&g.inc_ptr[row + 1]);
-        for (int q = q0; q < q1; q += 4) {
-            float a[4];
-            float2 xv[4];
+        for (int q = q0; q < q1; q += 8) {
+            float a[8];
+            float2 xv[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const bool ok = q + u < q1;
-                a[u] = ok ? (float)__ldg(&g.lap_off[q + u]) : 0.0f;
-                xv[u] = (ok && a[u] != 0.0f) ? xf(__ldg(&g.inc_other[q + u]), k, K) : f2(0.0f, 0.0f);
+            for (int u = 0; u < 8; ++u) {
+                const int2 e = q + u < q1 ? __ldg(&g.lap_pk[q + u]) : make_int2(0, 0);
+                a[u] = __int_as_float(e.y);
+                xv[u] = a[u] != 0.0f ? xf(e.x, k, K) : f2(0.0f, 0.0f);
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 s.x += a[u] * xv[u].x;
                 s.y += a[u] * xv[u].y;
             }
@@ -291,6 +299,12 @@ void vcycle_k(const GcDev& g, int pre, float2* out, cudaStream_t s, long long* l
 void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s) {
     const long n = std::max<long>(m.nn, m.n_pad);
     k_gc_weights<<<gc_grid(n), kGcBlock, 0, s>>>(m, inc_g, e_g);
+    gc_check(nullptr);
+}
+
+void gc_pack_level0(const GcDev& g, cudaStream_t s) {
+    if (g.n_levels < 1 || !g.lap_pk) return;
+    k_gc_pack0<<<(g.nn + kGcBlock - 1) / kGcBlock, kGcBlock, 0, s>>>(g);
     gc_check(nullptr);
 }
 

@@ -59,6 +59,10 @@ struct GcDev {
     // level 0 = the divergence-correction Laplacian in incidence form
     const int *inc_ptr = nullptr, *inc_other = nullptr;
     const double *lap_off = nullptr, *lap_diag = nullptr;
+    // FP32 copy read by the V-cycle and the FP32 PCG: (other node, value bits)
+    // per incidence entry, and the diagonal; refreshed with the Laplacian
+    int2* lap_pk = nullptr;
+    float* lap_diag32 = nullptr;
     // restriction G~^T (per incidence entry) and prolongation G~ (per
     // permuted edge row, two entries), zero on masked edges / nodes
     const int* inc_edge = nullptr;
@@ -80,6 +84,8 @@ struct GcDev {
 
 // Masked FP32 restriction / prolongation weights (once per mesh).
 void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s);
+// FP32 level-0 copy (lap_pk, lap_diag32) of the current Laplacian.
+void gc_pack_level0(const GcDev& g, cudaStream_t s);
 
 // g.out0[which] = V(G~^T in), one V-cycle on every lane; in is
 // [n_pad][K] complex FP32.  The term G~ out0 / (i omega) is added per row by

@@ -650,6 +650,12 @@ void GpuSolver::build_gc() {
     gc.lap_off = dc.lap_off;
     gc.lap_diag = dc.lap_diag;
     gc.inc_g = inc_g;
+    int2* pk = dalloc<int2>((size_t)std::max<long>(1, n_inc));
+    gc_mem.push_back((void*)pk);
+    float* d32 = dalloc<float>((size_t)L.nn);
+    gc_mem.push_back((void*)d32);
+    gc.lap_pk = pk;
+    gc.lap_diag32 = d32;
     gc.e_node = md.e_node;
     gc.e_g = e_g;
     for (int l = 0; l < amg.n_levels; ++l) {
@@ -681,6 +687,8 @@ void GpuSolver::build_gc() {
     gc.presmooth = P.gradcorr_presmooth;
     gc.omega_max = P.gradcorr == 1 ? 2.0 * kPi * P.gradcorr_fmax : 0.0;
     gc.inc_entries = n_inc;
+    gc_pack_level0(gc, stream);
+    ++launches;
     sync();
     gc_ok = true;
 }
@@ -732,6 +740,10 @@ void GpuSolver::build_amg() {
         }
         cuda_ok(cudaMemcpyAsync(const_cast<double*>(amg.coarse_inv), H.coarse_inv.data(),
                                 sizeof(double) * H.coarse_inv.size(), cudaMemcpyHostToDevice, stream), "mg values");
+        if (gc_ok) {
+            gc_pack_level0(gc, stream);
+            ++launches;
+        }
         sync();
         amg_setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         return;
@@ -1073,7 +1085,7 @@ void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<
 
 // Mixed precision: each step computes r = b - A x in FP64, solves A d = r
 // with the complex-FP32 batched BiCGStab (scaled to unit norm, relative
-// tolerance max(tol / ||r||_rel, 1e-5)), and adds d to x in FP64.  Steps repeat
+// tolerance max(tol / ||r||_rel, inner_tol_floor)), and adds d to x in FP64.  Steps repeat
 // until the FP64 true residual meets tol, the iteration budget is spent or a
 // step fails to reduce the residual by 10 %.
 //
@@ -1178,7 +1190,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             std::memset(&ls[j], 0, sizeof(BicgState));
             const int k = lanes[j];
             if (k < 0) { ls[j].status = kInactive; continue; }
-            ls[j].tol = std::min(0.5, std::max(tol / R.true_res[k], 1e-5));
+            ls[j].tol = std::min(0.5, std::max(tol / R.true_res[k], P.inner_tol_floor));
             ls[j].maxiter = std::max(1, maxiter - R.iters[k]);
             ls[j].status = kRunning;
         }
