@@ -71,6 +71,8 @@ def parse():
                     help="1: divergence-correction Poisson solve as FP32 PCG inside FP64 refinement")
     ap.add_argument("--inner-tol-floor", type=float, default=1e-5,
                     help="smallest relative residual asked of one complex-FP32 inner solve")
+    ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1],
+                    help="1: inner FP32 solve to the final tolerance with FP64 residual replacement")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -254,7 +256,7 @@ def run_ours(args, rank, world, local_rank):
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
                           ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
                           gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
-                          inner_tol_floor=args.inner_tol_floor)
+                          inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -298,7 +300,7 @@ def run_ours(args, rank, world, local_rank):
         iters.append(st["total_iterations"])
         solver_stats = {k: st[k] for k in ("forward_iterations", "adjoint_iterations", "refinements",
                                            "divcorr_calls", "divcorr_outer", "divcorr_cg_iterations",
-                                           "divcorr_cg_sweeps", "divcorr_setup_ms")}
+                                           "divcorr_cg_sweeps", "divcorr_setup_ms", "replacements")}
         solver_stats["iterations_per_rhs"] = st["iterations"]
         tr = st["true_residual"][:st["n_rhs"]]
         solver_stats["rhs_at_tol"] = sum(1 for t in tr if t <= 1e-7)
@@ -346,6 +348,7 @@ def run_ours(args, rank, world, local_rank):
                                f"({s.ne} edges, {s.nc} cells), 121 stations, {nf} freqs 0.01-100 Hz, "
                                f"forward+adjoint+sensitivity gradient step ({solves_per_step} solves)",
                    "tol": 1e-7, "precision": args.precision, "inner_tol_floor": args.inner_tol_floor,
+                   "residual_replacement": bool(args.residual_replacement),
                    "forward": args.forward,
                    "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
                    "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],

@@ -130,7 +130,12 @@ typedef struct m3d_params {
                                  complex-FP32 PCG (FP32 multigrid V(1,1) preconditioner) inside FP64
                                  iterative refinement, stopped by the FP64 true residual at the
                                  reference's 1e-10 |divJ|; 0: FP64 PCG */
-    double inner_tol_floor;   /* smallest relative residual asked of one complex-FP32 inner solve (1e-5) */
+    double inner_tol_floor;   /* smallest relative residual asked of one complex-FP32 inner solve (1e-5),
+                                 when residual_replacement is 0 */
+    int residual_replacement; /* 1: the complex-FP32 inner solve (right-preconditioned form) runs to the
+                                 final tolerance, its residual replaced by the FP64 true residual of the
+                                 accumulated solution each time it falls 1000x (no Krylov restart).
+                                 0 (default): restart per FP64 refinement, measured faster on C2 */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -152,6 +157,7 @@ typedef struct m3d_stats {
     long long adjoint_iterations;     /* ... of the adjoint phase */
     long long divcorr_cg_sweeps;      /* batched PCG iterations run (each serves every rhs of a batch) */
     double divcorr_setup_ms;          /* host time of the last multigrid setup of the PCG */
+    int replacements;                 /* residual replacements of the inner solves */
 } m3d_stats;
 
 void m3d_params_default(m3d_params* p);

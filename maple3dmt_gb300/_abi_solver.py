@@ -32,6 +32,7 @@ class Params(C.Structure):
         ("gradcorr_presmooth", C.c_int),
         ("divcorr_mixed", C.c_int),
         ("inner_tol_floor", C.c_double),
+        ("residual_replacement", C.c_int),
     ]
 
 
@@ -53,6 +54,7 @@ class Stats(C.Structure):
         ("adjoint_iterations", C.c_longlong),
         ("divcorr_cg_sweeps", C.c_longlong),
         ("divcorr_setup_ms", C.c_double),
+        ("replacements", C.c_int),
     ]
 
 

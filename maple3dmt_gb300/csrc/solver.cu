@@ -90,6 +90,52 @@ __global__ void k_add_f32_scaled(double2* __restrict__ x, const float2* __restri
 }
 
 
+// Residual replacement (reliable updating, van der Vorst and Ye 2000) of the
+// inner solve: on lanes with rep[j] set, r32 = y64[map[j]] / scale[j] (the
+// FP64 true residual of the accumulated FP64 solution, in the lane's
+// scaling) and x32 = 0 (its correction having been added to x64); rho =
+// (r0, r), beta and |r| are recomputed from the new residual so the
+// BiCGStab recurrence continues without a restart.
+template <int Kc>
+__global__ void __launch_bounds__(256) k_replace_lanes(const double2* __restrict__ y, int K, float2* __restrict__ r,
+                                                       float2* __restrict__ x, const float2* __restrict__ r0,
+                                                       const int* __restrict__ map, const int* __restrict__ rep,
+                                                       const double* __restrict__ scale, long n_rows, BicgState* st,
+                                                       dev::RedScratch rs) {
+    const long n = n_rows * Kc;
+    const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int j = (int)(i0 % Kc), m = map[j];
+    const bool on = m >= 0 && rep[j] && scale[j] > 0.0;
+    const double inv = on ? 1.0 / scale[j] : 0.0;
+    double2 acc[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    for (long i = i0; i < n && on; i += stride) {
+        const double2 w = y[(i / Kc) * K + m];
+        const float2 v = make_float2((float)(w.x * inv), (float)(w.y * inv));
+        r[i] = v;
+        x[i] = make_float2(0.0f, 0.0f);
+        const float2 a = r0[i];
+        acc[0].x += (double)a.x * v.x + (double)a.y * v.y;
+        acc[0].y += (double)a.x * v.y - (double)a.y * v.x;
+        acc[1].x += (double)v.x * v.x + (double)v.y * v.y;
+    }
+    __shared__ double2 out[2 * Kc];
+    if (dev::grid_reduce_lanes<2, Kc, 256>(acc, rs, out)) {
+        const int jj = threadIdx.x;
+        if (jj < Kc && map[jj] >= 0 && rep[jj] && scale[jj] > 0.0) {
+            BicgState S = st[jj];
+            if (S.status == kRunning) {
+                S.rnorm = sqrt(out[Kc + jj].x);
+                S.res = S.rnorm / S.bnorm;
+                S.rho = out[jj];
+                if (S.res < S.tol) S.status = kConverged;
+                else S.beta = dev::cmul(dev::cdiv(S.rho, S.rho_old), dev::cdiv(S.alpha, S.omega));
+                st[jj] = S;
+            }
+        }
+    }
+}
+
 // Compact layout of the mixed-precision inner solve: lane j of a K_c-wide
 // batch works on right-hand side map[j] of the K-wide FP64 batch (-1: padding).
 
@@ -1167,6 +1213,10 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                     use_gc |= om > 0.0 && om <= gc.omega_max;
                 }
         const bool eis = !use_gc && P.ssor_form == 1 && P.row_kernels == kRowsStaged;
+        // residual replacement needs the untransformed residual of the
+        // right-preconditioned form
+        const bool replace = P.residual_replacement == 1 && !eis;
+        std::vector<double> rep_level(dev::kMaxRhs, 1.0);
         // flushes lanes with add[j] set: x64 += scale * d32, d32 the x-space
         // correction (x_hat mapped back by (D + U)^-1 in the Eisenstat form)
         auto flush = [&](const KrylovCtx<float>& cc, const KrylovVecs<float>& v, int Kn) {
@@ -1180,6 +1230,25 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                                                                            d_scale, (long)n_pad);
             ++launches;
         };
+        auto replace_lanes = [&](int Kn, const KrylovVecs<float>& v) {
+            // d_lane_add holds the replaced lanes (uploaded by the flush)
+#define M3D_REPLACE(KC)                                                                                        \
+    {                                                                                                          \
+        auto kf = k_replace_lanes<KC>;                                                                         \
+        kf<<<wave_grid(kf, red.max_blocks, 256), 256, 0, stream>>>(kv.y, K, v.r, v.x, v.r0, d_lane_map,        \
+                                                                   d_lane_add, d_scale, (long)n_pad, d_states, \
+                                                                   red);                                       \
+    }
+            switch (Kn) {
+                case 2: M3D_REPLACE(2) break;
+                case 4: M3D_REPLACE(4) break;
+                case 8: M3D_REPLACE(8) break;
+                default: M3D_REPLACE(16) break;
+            }
+#undef M3D_REPLACE
+            cuda_ok(cudaGetLastError(), "replace");
+            ++launches;
+        };
         upload_lanes(Kc);
         k_to_f32_lanes<<<launch_grid((long)n_pad * Kc), 256, 0, stream>>>(kv.y, K, cur.b, Kc, d_lane_map, d_scale,
                                                                       (long)n_pad);
@@ -1190,7 +1259,10 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             std::memset(&ls[j], 0, sizeof(BicgState));
             const int k = lanes[j];
             if (k < 0) { ls[j].status = kInactive; continue; }
-            ls[j].tol = std::min(0.5, std::max(tol / R.true_res[k], P.inner_tol_floor));
+            // with residual replacement the inner solve runs to the final
+            // tolerance; without, to what complex FP32 reaches reliably
+            ls[j].tol = std::min(0.5, std::max(tol / R.true_res[k], replace ? 0.25 * tol / R.true_res[k]
+                                                                                    : P.inner_tol_floor));
             ls[j].maxiter = std::max(1, maxiter - R.iters[k]);
             ls[j].status = kRunning;
         }
@@ -1212,6 +1284,36 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             int nrun = 0;
             for (int j = 0; j < Kc; ++j) nrun += (lanes[j] >= 0 && ls[j].status == kRunning);
             if (nrun == 0 || it >= maxiter) break;
+            if (replace) {
+                // lanes whose recursive residual fell 1000x since the last
+                // replacement: flush x, FP64 true residual, replace r
+                std::vector<int> rep(dev::kMaxRhs, 0);
+                bool anyrep = false;
+                for (int j = 0; j < Kc; ++j)
+                    if (lanes[j] >= 0 && ls[j].status == kRunning && ls[j].res < 1e-3 * rep_level[j]) {
+                        rep[j] = 1;
+                        anyrep = true;
+                    }
+                if (anyrep) {
+                    add = rep;
+                    flush(c32, cur, Kc);
+                    std::vector<BicgState> ts(K);
+                    for (int k = 0; k < K; ++k) {
+                        std::memset(&ts[k], 0, sizeof(BicgState));
+                        ts[k].status = kInactive;
+                    }
+                    for (int j = 0; j < Kc; ++j)
+                        if (rep[j]) ts[lanes[j]].status = kConverged;
+                    cuda_ok(cudaMemcpyAsync(d_states2, ts.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice,
+                                            stream), "states");
+                    spmv(c64, kSpmvTrueRes, x, kv.y, b, nullptr, d_states2);
+                    replace_lanes(Kc, cur);
+                    for (int j = 0; j < Kc; ++j)
+                        if (rep[j]) rep_level[j] = ls[j].res;
+                    ++stats.replacements;
+                    continue;   // re-read the states
+                }
+            }
             const int Kn = pow2_at_least(nrun);
             if (Kn < Kc && Kn <= other_cap) {
                 // finished lanes: add their corrections and record them
@@ -1263,6 +1365,7 @@ void GpuSolver::begin_call() {
     stats.forward_iterations = 0;
     stats.adjoint_iterations = 0;
     stats.refinements = 0;
+    stats.replacements = 0;
     dcc = phys::DcCounters();
 }
 

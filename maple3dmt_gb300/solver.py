@@ -217,7 +217,8 @@ class ForwardSolverFV:
                     divcorr_calls=s.divcorr_calls, divcorr_outer=s.divcorr_outer,
                     divcorr_cg_iterations=s.divcorr_cg_iterations,
                     forward_iterations=s.forward_iterations, adjoint_iterations=s.adjoint_iterations,
-                    divcorr_cg_sweeps=s.divcorr_cg_sweeps, divcorr_setup_ms=s.divcorr_setup_ms)
+                    divcorr_cg_sweeps=s.divcorr_cg_sweeps, divcorr_setup_ms=s.divcorr_setup_ms,
+                    replacements=s.replacements)
 
 
 def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:

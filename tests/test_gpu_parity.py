@@ -93,6 +93,23 @@ def test_divcorr_mixed_matches_reference(g_small, mixed):
     assert s.stats()["divcorr_calls"] > 0
 
 
+@pytest.mark.parametrize("replacement", [0, 1])
+def test_residual_replacement_matches_reference(g_small, replacement):
+    """The FP32 inner solve restarted per FP64 refinement and run through with
+    FP64 residual replacement reach the same 1e-10 true residual and the
+    reference's impedances and gradient."""
+    g = g_small
+    s = _gpu(g, precision=1, forward_interleaved=1, residual_replacement=replacement)
+    Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
+    ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
+    assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
+    assert rel(grad, g["ref_grad"]) < G_TOL
+    st = s.stats()
+    assert all(t <= 1e-10 for t in st["true_residual"][:st["n_rhs"]]), st
+    if replacement:
+        assert st["replacements"] > 0
+
+
 def test_forward_matches_reference_golden(g_small):
     g = g_small
     s = _gpu(g)
