@@ -69,7 +69,7 @@ def parse():
                     help="V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1)")
     ap.add_argument("--divcorr-mixed", type=int, default=1, choices=[0, 1],
                     help="1: divergence-correction Poisson solve as FP32 PCG inside FP64 refinement")
-    ap.add_argument("--inner-tol-floor", type=float, default=1e-5,
+    ap.add_argument("--inner-tol-floor", type=float, default=3e-5,
                     help="smallest relative residual asked of one complex-FP32 inner solve")
     ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1],
                     help="1: inner FP32 solve to the final tolerance with FP64 residual replacement")

@@ -130,7 +130,7 @@ typedef struct m3d_params {
                                  complex-FP32 PCG (FP32 multigrid V(1,1) preconditioner) inside FP64
                                  iterative refinement, stopped by the FP64 true residual at the
                                  reference's 1e-10 |divJ|; 0: FP64 PCG */
-    double inner_tol_floor;   /* smallest relative residual asked of one complex-FP32 inner solve (1e-5),
+    double inner_tol_floor;   /* smallest relative residual asked of one complex-FP32 inner solve (3e-5),
                                  when residual_replacement is 0 */
     int residual_replacement; /* 1: the complex-FP32 inner solve (right-preconditioned form) runs to the
                                  final tolerance, its residual replaced by the FP64 true residual of the

@@ -78,7 +78,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->gradcorr_fmax = 1e30;
     p->gradcorr_presmooth = 0;
     p->divcorr_mixed = 1;
-    p->inner_tol_floor = 1e-5;
+    p->inner_tol_floor = 3e-5;
     p->residual_replacement = 0;
 }
 

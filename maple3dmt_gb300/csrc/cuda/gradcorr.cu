@@ -53,6 +53,7 @@ __global__ void k_gc_pack0(GcDev g) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.nn) return;
     g.lap_diag32[v] = (float)g.lap_diag[v];
+    g.lv[0].dinv32[v] = (float)g.lv[0].dinv[v];
     for (int q = g.inc_ptr[v]; q < g.inc_ptr[v + 1]; ++q)
         g.lap_pk[q] = make_int2(g.inc_other[q], __float_as_int((float)g.lap_off[q]));
 }
@@ -246,6 +247,35 @@ __global__ void __launch_bounds__(kGcBlock) k_gc_up(GcDev g, GcLevel L, const fl
     }
 }
 
+// t = x + P xc (x optional): the level-0 iterate after the coarse
+// correction, written out so the smoothing step gathers it directly
+template <int K>
+__global__ void __launch_bounds__(kGcBlock) k_gc_prolong0(GcDev g, const float2* __restrict__ xc,
+                                                          float2* __restrict__ t, int presmoothed) {
+    const GcLevel& L = g.lv[0];
+    const XProlonged xf{presmoothed ? L.x : nullptr, L.agg, xc};
+    const long n = (long)g.nn * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        t[i] = xf((int)(i / K), (int)(i % K), K);
+}
+
+// y0 = t + omega D^-1 (b0 - L t)
+template <int K>
+__global__ void __launch_bounds__(kGcBlock) k_gc_smooth0(GcDev g, const float2* __restrict__ t,
+                                                         float2* __restrict__ out) {
+    const GcLevel& L = g.lv[0];
+    const XPlain xf{t};
+    const long n = (long)g.nn * K;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int row = (int)(i / K), k = (int)(i % K);
+        const float2 ax = level_row<K, true>(g, L, row, xf, k);
+        const float2 xt = t[i];
+        const float2 bv = L.b[i];
+        const float sc = g.omega * __ldg(&L.dinv32[row]);
+        out[i] = f2(xt.x + sc * (bv.x - ax.x), xt.y + sc * (bv.y - ax.y));
+    }
+}
+
 // x0 = omega D^-1 b0 (pre-smoothing from zero, node-vector input)
 template <int K>
 __global__ void __launch_bounds__(kGcBlock) k_gc_pre0(GcDev g) {
@@ -288,8 +318,15 @@ void vcycle_k(const GcDev& g, int pre, float2* out, cudaStream_t s, long long* l
         const float2* xc = (l + 1 == nl - 1) ? g.lv[l + 1].x : g.lv[l + 1].y;
         float2* dst = l == 0 ? out : g.lv[l].y;
         const long work = (long)g.lv[l].n * K;
-        if (l == 0) k_gc_up<K, true><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc, dst, pre);
-        else k_gc_up<K, false><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc, dst, pre);
+        if (l == 0) {
+            // level 0 in two passes: prolongation into y (the level's scratch),
+            // then the smoothing step gathers it directly
+            k_gc_prolong0<K><<<gc_grid(work), kGcBlock, 0, s>>>(g, xc, g.lv[0].y, pre);
+            gc_check(launches);
+            k_gc_smooth0<K><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[0].y, dst);
+        } else {
+            k_gc_up<K, false><<<gc_grid(work), kGcBlock, 0, s>>>(g, g.lv[l], xc, dst, pre);
+        }
         gc_check(launches);
     }
 }

@@ -41,6 +41,7 @@ struct GcLevel {
     const int *ptr = nullptr, *col = nullptr;   // A_l in CSR (levels >= 1)
     const double* val = nullptr;
     const double* dinv = nullptr;               // Jacobi scale 1 / a_ii
+    float* dinv32 = nullptr;                    // its FP32 copy (level 0, refreshed with the Laplacian)
     const int* agg = nullptr;                   // [n] aggregate in level l+1 (-1: none)
     const int *rptr = nullptr, *rcol = nullptr; // members of each aggregate of level l+1
     float2 *b = nullptr, *x = nullptr, *y = nullptr;   // [n][kMaxRhs] right side, pre-smoothed, scratch / post-smoothed
@@ -69,7 +70,7 @@ struct GcDev {
     const float* inc_g = nullptr;
     const int* e_node = nullptr;
     const float* e_g = nullptr;
-    float2* out0[2] = {nullptr, nullptr};   // [nn][kMaxRhs] V-cycle results for p and for s
+    float2* out0[2] = {nullptr, nullptr};   // [nn][kMaxRhs] V-cycle results (the iteration uses out0[0])
     GcLevel lv[phys::kAmgMaxLevels];
     int n_coarse = 0;
     const double* coarse_inv = nullptr;   // [n_coarse][n_coarse]
@@ -89,7 +90,7 @@ void gc_pack_level0(const GcDev& g, cudaStream_t s);
 
 // g.out0[which] = V(G~^T in), one V-cycle on every lane; in is
 // [n_pad][K] complex FP32.  The term G~ out0 / (i omega) is added per row by
-// the SpMV and the x update (GcRowTerm).
+// the backward SSOR sweep (GcRowTerm).
 template <int K>
 void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
                 KernelTimer* timer);

@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, Bat
                                                  const cplx<R>* __restrict__ x, cplx<R>* __restrict__ y,
                                                  const cplx<R>* __restrict__ aux,
                                                  cplx<R>* __restrict__ aux_out, BicgState* st,
-                                                 RedScratch rs, GcRowTerm gt) {
+                                                 RedScratch rs) {
     using C = cplx<R>;
     constexpr int RPW = Rpw<K>::v;
     constexpr int NQ = (MODE == kSpmvAp) ? 1 : (MODE == kSpmvAs || MODE == kSpmvTrueRes) ? 2 : 3;
@@ -256,13 +256,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(OpView<R> A, DiagView<R> D, Bat
         const C s = row_dot<R, K>(A, A.rp[row], A.rp[row + 1], x, rhs);
         const size_t i = (size_t)row * K + rhs;
         const C d = diag_of(D, row, om);
-        C yv = cadd(s, cmul(d, x[i]));
-        if ((MODE == kSpmvAp || MODE == kSpmvAs) && gt.ya && gt.s[rhs] != 0.0f) {
-            const float2 g = gc_grad_row(gt, gt.ya, row, rhs, K);
-            const R me = D.sm[row].y;
-            yv.x += me * (R)g.x;
-            yv.y += me * (R)g.y;
-        }
+        const C yv = cadd(s, cmul(d, x[i]));
         if (MODE == kSpmvPlain) {
             y[i] = yv;
         } else if (MODE == kSpmvAp) {
@@ -363,7 +357,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
                                                                 cplx<R>* __restrict__ y,
                                                                 const cplx<R>* __restrict__ aux,
                                                                 cplx<R>* __restrict__ aux_out, BicgState* st,
-                                                                RedScratch rs, GcRowTerm gt) {
+                                                                RedScratch rs) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
@@ -373,7 +367,6 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
     const int rhs = lane % K;
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
-    const float2* gy = ((MODE == kSpmvAp || MODE == kSpmvAs) && gt.s[rhs] != 0.0f) ? gt.ya : nullptr;
     C accR[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) accR[q] = cm<R>(0, 0);
@@ -390,13 +383,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
             const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
             const C d = diag_of(D, row, om);
             const C s = seg_row_dot_lu<R, K>(lo, up, lr, x, rhs);
-            C yv = cadd(s, cmul(d, xi));
-            if ((MODE == kSpmvAp || MODE == kSpmvAs) && gy) {
-                const float2 g = gc_grad_row(gt, gy, row, rhs, K);
-                const R me = D.sm[row].y;
-                yv.x += me * (R)g.x;
-                yv.y += me * (R)g.y;
-            }
+            const C yv = cadd(s, cmul(d, xi));
             if (MODE == kSpmvPlain) {
                 y[i] = yv;
             } else if (MODE == kSpmvAp) {
@@ -468,10 +455,14 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
 }
 
 // SSOR backward sweep of one colour over slice-staged upper parts (ssor.h:69-78).
-template <class R, int K>
+// GC: the preconditioner's gradient-space term c = G~ y0 / (i omega) is added
+// to the written row, out_i = w_i + c_i; the sweep then keeps w in y (in
+// place of the forward result, read once per row before it is replaced) and
+// gathers the later colours' w from there.
+template <class R, int K, bool GC>
 __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_bwd_st(SegView<R> S, const int4* __restrict__ work,
                                                                     int count, DiagView<R> D, BatchView B,
-                                                                    const cplx<R>* __restrict__ y, cplx<R>* out) {
+                                                                    cplx<R>* y, cplx<R>* out, GcRowTerm gt) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
@@ -487,10 +478,29 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
             const int lr = ps * Sh::ROWS_PER_PASS + lr0;
             const int row = it.slice * kSlice + lr;
             const size_t i = (size_t)row * K + rhs;
+            // the term's node values are loaded ahead of the row's gathers
+            float g0 = 0.0f, g1 = 0.0f;
+            float2 ya = make_float2(0.0f, 0.0f), yb = ya;
+            if (GC) {
+                g0 = __ldg(&gt.e_g[2 * row]);
+                g1 = __ldg(&gt.e_g[2 * row + 1]);
+                const int n0 = __ldg(&gt.e_node[2 * row]), n1 = __ldg(&gt.e_node[2 * row + 1]);
+                ya = gt.ya[(size_t)n0 * K + rhs];
+                yb = gt.ya[(size_t)n1 * K + rhs];
+            }
             const C yv = y[i];
             const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], out, rhs, cm<R>(0, 0));
-            out[i] = csub(yv, cmul(s, inv_c(d)));
+            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], GC ? y : out, rhs,
+                                          cm<R>(0, 0));
+            const C w = csub(yv, cmul(s, inv_c(d)));
+            if (GC) {
+                y[i] = w;
+                const float sc = gt.s[rhs];
+                const float gx = g0 * ya.x + g1 * yb.x, gy = g0 * ya.y + g1 * yb.y;
+                out[i] = cm<R>(w.x + (R)(sc * gy), w.y - (R)(sc * gx));
+            } else {
+                out[i] = w;
+            }
         }
     });
 }
@@ -560,7 +570,7 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
                                                       const cplx<R>* __restrict__ sh,
                                                       const cplx<R>* __restrict__ s,
                                                       const cplx<R>* __restrict__ t, BicgState* st,
-                                                      RedScratch rs, GcRowTerm gt) {
+                                                      RedScratch rs) {
     using C = cplx<R>;
     const long i0 = (long)blockIdx.x * blockDim.x + threadIdx.x;
     const long stride = (long)gridDim.x * blockDim.x;
@@ -569,29 +579,12 @@ __global__ void __launch_bounds__(kBlock) k_update_xr(long n, cplx<R>* __restric
     const bool run = S.status == kRunning;
     const bool pend = S.pend_x != 0;
     const C al = from_d<C>(S.alpha), om = from_d<C>(S.omega);
-    const bool term = gt.ya && gt.s[rhs] != 0.0f;
-    const R sc = (R)gt.s[rhs];
-    // c = G~ y / (i omega) = sc (g.y, -g.x)
-    auto corr = [&](const float2* y, long i) {
-        const float2 g = gc_grad_row(gt, y, (int)(i / K), rhs, K);
-        return cm<R>(sc * (R)g.y, -sc * (R)g.x);
-    };
     R rr = 0;
     C r0r = cm<R>(0, 0);
     for (long i = i0; i < n; i += stride) {
-        if (pend) {
-            C php = ph[i];
-            if (term) php = cadd(php, corr(gt.ya, i));
-            x[i] = cadd(x[i], cmul(al, php));
-            continue;
-        }
+        if (pend) { x[i] = cadd(x[i], cmul(al, ph[i])); continue; }
         if (!run) continue;
-        C php = ph[i], shs = sh[i];
-        if (term) {
-            php = cadd(php, corr(gt.ya, i));
-            shs = cadd(shs, corr(gt.yb, i));
-        }
-        x[i] = cadd(x[i], cadd(cmul(al, php), cmul(om, shs)));
+        x[i] = cadd(x[i], cadd(cmul(al, ph[i]), cmul(om, sh[i])));
         const C rv = csub(s[i], cmul(om, t[i]));
         r[i] = rv;
         rr += rv.x * rv.x + rv.y * rv.y;
@@ -634,7 +627,7 @@ double matrix_bytes(const KrylovCtx<R>& c) {
 
 template <class R, int K>
 void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
-                 cplx<R>* aux_out, BicgState* st, const GcRowTerm& gt) {
+                 cplx<R>* aux_out, BicgState* st) {
     constexpr int NT = StagedShape<K>::NT;
     const long ns = c.n_pad / kSlice;
     const int sb = c.seg.stage_spmv;
@@ -644,30 +637,30 @@ void spmv_staged(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, 
     switch (mode) {
         case kSpmvPlain:
             launch_staged(k_spmv_st<R, K, kSpmvPlain>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red, gt);
+                          aux_out, st, c.red);
             break;
         case kSpmvAp:
             launch_staged(k_spmv_st<R, K, kSpmvAp>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red, gt);
+                          aux_out, st, c.red);
             break;
         case kSpmvAs:
             launch_staged(k_spmv_st<R, K, kSpmvAs>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red, gt);
+                          aux_out, st, c.red);
             break;
         case kSpmvInit:
             launch_staged(k_spmv_st<R, K, kSpmvInit>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red, gt);
+                          aux_out, st, c.red);
             break;
         default:
             launch_staged(k_spmv_st<R, K, kSpmvTrueRes>, NT, sb, ns, cap, c.stream, c.seg, ns, c.D, c.B, x, y, aux,
-                          aux_out, st, c.red, gt);
+                          aux_out, st, c.red);
             break;
     }
 }
 
 template <class R, int K>
 void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const cplx<R>* aux,
-            cplx<R>* aux_out, BicgState* st, const GcRowTerm& gt = GcRowTerm{}) {
+            cplx<R>* aux_out, BicgState* st) {
     const long warps = (long)c.A.n_pad / Rpw<K>::v;
     int grid;
     if (mode == kSpmvPlain) {
@@ -676,39 +669,37 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
         grid = c.grid_spmv;
     }
     const int streams = 2 + (aux ? 1 : 0) + (aux_out ? 1 : 0);
-    // the gradient-space term: two node indices and weights per row
-    const double term = gt.ya ? (double)c.n_rows * 16 : 0.0;
-    const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) + term +
+    const int th = c.timer ? c.timer->begin(kClsSpmv, matrix_bytes(c) +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * streams, K) : -1;
     const int cap = c.red.max_blocks;
     if (c.row_kernels == kRowsStaged) {
-        spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st, gt);
+        spmv_staged<R, K>(c, mode, x, y, aux, aux_out, st);
         check_launch(c.launches);
         if (c.timer) c.timer->end(th);
         return;
     }
     switch (mode) {
         case kSpmvPlain:
-            k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
+            k_spmv<R, K, kSpmvPlain><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
         case kSpmvAp: {
             auto kf = k_spmv<R, K, kSpmvAp>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
         }
         case kSpmvAs: {
             auto kf = k_spmv<R, K, kSpmvAs>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
         }
         case kSpmvInit: {
             auto kf = k_spmv<R, K, kSpmvInit>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
         }
         default: {
             auto kf = k_spmv<R, K, kSpmvTrueRes>;
-            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red, gt);
+            kf<<<wave_grid(kf, cap), kBlock, 0, c.stream>>>(c.A, c.D, c.B, x, y, aux, aux_out, st, c.red);
             break;
         }
     }
@@ -716,13 +707,30 @@ void spmv_k(const KrylovCtx<R>& c, int mode, const cplx<R>* x, cplx<R>* y, const
     if (c.timer) c.timer->end(th);
 }
 
+// out_i += G~ y0 / (i omega) = s (g.y, -g.x) on the lanes with s != 0
 template <class R, int K>
-void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
+__global__ void __launch_bounds__(kBlock) k_add_gc_term(long n, cplx<R>* __restrict__ out, GcRowTerm gt) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int rhs = (int)(i % K);
+    const float sc = gt.s[rhs];
+    if (sc == 0.0f) return;
+    const float2 g = gc_grad_row(gt, gt.ya, (int)(i / K), rhs, K);
+    cplx<R> o = out[i];
+    o.x += (R)(sc * g.y);
+    o.y -= (R)(sc * g.x);
+    out[i] = o;
+}
+
+template <class R, int K>
+void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, const GcRowTerm& gt = GcRowTerm{}) {
     constexpr int G = kSlice / Rpw<K>::v;   // row-group tasks per slice
     const int nc = (int)c.colour_ptr.size() - 1;
     // whole apply: matrix once (lower forward, upper backward), vectors in,
-    // y (written, read back), out
-    const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) +
+    // y (written, read back), out; with the gradient-space term y written
+    // back once more and two node indices and weights per row
+    const double gcb = gt.ya ? (double)c.n_rows * (K * sizeof(cplx<R>) + 16) : 0.0;
+    const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + gcb +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * 4, K) : -1;
     if (c.row_kernels == kRowsStaged) {
         constexpr int NT = StagedShape<K>::NT;
@@ -736,8 +744,12 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) 
         for (int col = nc - 1; col >= 0; --col) {
             const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
             if (s1 <= s0) continue;
-            launch_staged(k_ssor_bwd_st<R, K>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
-                          c.seg.work_col + s0, s1 - s0, c.D, c.B, (const cplx<R>*)y, out);
+            if (gt.ya)
+                launch_staged(k_ssor_bwd_st<R, K, true>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+                              c.seg.work_col + s0, s1 - s0, c.D, c.B, y, out, gt);
+            else
+                launch_staged(k_ssor_bwd_st<R, K, false>, NT, c.seg.stage_up, s1 - s0, 1 << 20, c.stream, c.seg,
+                              c.seg.work_col + s0, s1 - s0, c.D, c.B, y, out, gt);
             check_launch(c.launches);
         }
         if (c.timer) c.timer->end(th);
@@ -757,12 +769,17 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) 
         k_ssor_bwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, c.colour_list + s0, s1 - s0, y, out);
         check_launch(c.launches);
     }
+    if (gt.ya) {   // CSR rows: the gradient-space term in a pass of its own
+        const long n = (long)c.n_pad * K;
+        k_add_gc_term<R, K><<<blocks_for(n, kBlock, 1 << 20), kBlock, 0, c.stream>>>(n, out, gt);
+        check_launch(c.launches);
+    }
     if (c.timer) c.timer->end(th);
 }
 
 // One V-cycle of the gradient-space term on G~^T in (complex FP32 only),
-// output in the node buffer `which` (0: for p, 1: for s); the SpMV and the x
-// update add the term per row (GcRowTerm).
+// output in the node buffer `which`; the backward SSOR sweep adds the term
+// per row (GcRowTerm).
 template <class R, int K>
 void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, int which) {
     if constexpr (std::is_same<R, float>::value) {
@@ -779,25 +796,22 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     k_update_p<R, K><<<gv, kBlock, 0, c.stream>>>(n, v.r, v.p, v.v, st);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
-    GcRowTerm gp, gs, gx;
-    if (c.gc) {
-        gp = gc_row_term(*c.gc, c.B, 0);
-        gs = gc_row_term(*c.gc, c.B, 1);
-        gx = gp;
-        gx.yb = gs.ya;
-    }
-    ssor_k<R, K>(c, v.p, v.y, v.ph);
+    // the gradient-space term: V-cycle first, added to the preconditioned
+    // vector by the backward sweep
+    GcRowTerm gt;
+    if (c.gc) gt = gc_row_term(*c.gc, c.B, 0);
     gc_term<R, K>(c, v.p, 0);
-    spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st, gp);
+    ssor_k<R, K>(c, v.p, v.y, v.ph, gt);
+    spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
     k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
-    ssor_k<R, K>(c, v.s, v.y, v.sh);
-    gc_term<R, K>(c, v.s, 1);
-    spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st, gs);
-    th = c.timer ? c.timer->begin(kClsVec, 8 * vb + (c.gc ? (double)c.n_rows * 16 : 0.0), K) : -1;
-    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red, gx);
+    gc_term<R, K>(c, v.s, 0);
+    ssor_k<R, K>(c, v.s, v.y, v.sh, gt);
+    spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
+    th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
+    k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.ph, v.sh, v.s, v.t, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
 }
@@ -1124,7 +1138,7 @@ void eis_iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* s
     if (c.timer) c.timer->end(th);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;
     k_update_xr<R, K><<<wave_grid(k_update_xr<R, K>, gv), kBlock, 0, c.stream>>>(n, v.x, v.r, v.r0, v.p, v.s, v.s,
-                                                                              v.t, st, c.red, GcRowTerm{});
+                                                                              v.t, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
 }

@@ -71,15 +71,12 @@ struct BatchView {
 };
 
 // Per-row gradient-space term of the right-preconditioned FP32 iteration
-// (gradcorr.cuh): with y the node vector of one multigrid V-cycle and
-// c = G~ y / (i omega) the term added to the preconditioned vector,
-//  * the SpMV adds A c = i omega Me c = Me_i (G~ y)_i (A G~ = i omega Me G~,
-//    the curl of a gradient being zero), so c itself is never stored;
-//  * the x update adds alpha c_p + omega c_s.
-// G~ y at permuted row i = e_g[2i] y[e_node[2i]] + e_g[2i+1] y[e_node[2i+1]].
+// (gradcorr.cuh): with y the node vector of one multigrid V-cycle, the
+// preconditioned vector gets c = G~ y / (i omega) added by the backward SSOR
+// sweep as it writes each row; G~ y at permuted row i =
+// e_g[2i] y[e_node[2i]] + e_g[2i+1] y[e_node[2i+1]].
 struct GcRowTerm {
-    const float2* ya = nullptr;   // V-cycle output for p (SpMV: for the vector multiplied)
-    const float2* yb = nullptr;   // V-cycle output for s (x update only)
+    const float2* ya = nullptr;   // V-cycle output (null: no term)
     const int* e_node = nullptr;
     const float* e_g = nullptr;
     float s[dev::kMaxRhs] = {};   // 1 / omega of each lane; 0: no term on that lane

@@ -702,6 +702,8 @@ void GpuSolver::build_gc() {
     gc_mem.push_back((void*)d32);
     gc.lap_pk = pk;
     gc.lap_diag32 = d32;
+    float* dv32 = dalloc<float>((size_t)L.nn);
+    gc_mem.push_back((void*)dv32);
     gc.e_node = md.e_node;
     gc.e_g = e_g;
     for (int l = 0; l < amg.n_levels; ++l) {
@@ -712,6 +714,7 @@ void GpuSolver::build_gc() {
         g.col = a.col;
         g.val = a.val;
         g.dinv = a.dinv;
+        if (l == 0) g.dinv32 = dv32;
         g.agg = a.agg;
         g.rptr = a.rptr;
         g.rcol = a.rcol;
