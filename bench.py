@@ -73,6 +73,8 @@ def parse():
                     help="smallest relative residual asked of one complex-FP32 inner solve")
     ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1],
                     help="1: inner FP32 solve to the final tolerance with FP64 residual replacement")
+    ap.add_argument("--gradcorr-overlap", type=int, default=1, choices=[0, 1],
+                    help="1: V-cycles of the gradient-space term on a second stream, overlapping the SSOR sweep")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -256,7 +258,8 @@ def run_ours(args, rank, world, local_rank):
                           row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
                           ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
                           gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
-                          inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement)
+                          inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
+                          gradcorr_overlap=args.gradcorr_overlap)
     nf = len(sv.freqs)
     solves_per_step = 4 * nf
     dist = None
@@ -355,7 +358,9 @@ def run_ours(args, rank, world, local_rank):
                    "divcorr_solve": ["fp64 pcg", "fp32 pcg in fp64 refinement"][args.divcorr_mixed],
                    "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
                    "gradcorr": (f"multigrid gradient-space term, V({args.gradcorr_presmooth},1), "
-                                f"f <= {args.gradcorr_fmax:g} Hz" if args.gradcorr else "off"),
+                                f"f <= {args.gradcorr_fmax:g} Hz"
+                                + (", V-cycle on a second stream" if args.gradcorr_overlap else "")
+                                if args.gradcorr else "off"),
                    "arm": "plain (per frequency, complex128)" if args.plain else "batched",
                    "l2": "inputs larger than L2 (matrix alone 260 MB)",
                    "parallelism": f"replica x{world}"},

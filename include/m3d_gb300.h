@@ -136,6 +136,8 @@ typedef struct m3d_params {
                                  final tolerance, its residual replaced by the FP64 true residual of the
                                  accumulated solution each time it falls 1000x (no Krylov restart).
                                  0 (default): restart per FP64 refinement, measured faster on C2 */
+    int gradcorr_overlap;     /* 1: the V-cycles of the gradient-space term run on a second CUDA stream,
+                                 overlapping the forward SSOR sweep (same arithmetic); 0: one stream */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;

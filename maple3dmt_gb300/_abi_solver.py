@@ -33,6 +33,7 @@ class Params(C.Structure):
         ("divcorr_mixed", C.c_int),
         ("inner_tol_floor", C.c_double),
         ("residual_replacement", C.c_int),
+        ("gradcorr_overlap", C.c_int),
     ]
 
 

@@ -80,6 +80,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->divcorr_mixed = 1;
     p->inner_tol_floor = 3e-5;
     p->residual_replacement = 0;
+    p->gradcorr_overlap = 1;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -115,7 +116,8 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
         params->ssor_form < 0 || params->ssor_form > 1 || params->gradcorr < 0 || params->gradcorr > 1 ||
         !(params->gradcorr_fmax >= 0.0) || params->gradcorr_presmooth < 0 || params->gradcorr_presmooth > 1 ||
         params->divcorr_mixed < 0 || params->divcorr_mixed > 1 || !(params->inner_tol_floor > 0.0) ||
-        params->inner_tol_floor >= 1.0 || params->residual_replacement < 0 || params->residual_replacement > 1)
+        params->inner_tol_floor >= 1.0 || params->residual_replacement < 0 || params->residual_replacement > 1 ||
+        params->gradcorr_overlap < 0 || params->gradcorr_overlap > 1)
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
 }

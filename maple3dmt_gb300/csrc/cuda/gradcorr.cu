@@ -369,12 +369,12 @@ void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStr
     // twice; the restriction weights once
     const double eb = (double)n_rows * K * sizeof(float2), nb = (double)g.nn * K * sizeof(float2);
     const double bytes = eb + 7 * nb + 2.0 * g.inc_entries * 12 + (double)g.inc_entries * 8;
-    const int th = timer ? timer->begin(kClsGradcorr, bytes, K) : -1;
+    const int th = timer ? timer->begin(kClsGradcorr, bytes, K, s) : -1;
     const int pre = g.presmooth && nl > 1 ? 1 : 0;   // V(1,1) or V(0,1)
     k_gc_restrict_edges<K><<<gc_grid((long)g.nn * K), kGcBlock, 0, s>>>(g, in, pre);
     gc_check(launches);
     vcycle_k<K>(g, pre, out, s, launches);
-    if (timer) timer->end(th);
+    if (timer) timer->end(th, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -47,18 +47,18 @@ cudaEvent_t KernelTimer::get() {
     return e;
 }
 
-int KernelTimer::begin(int cls, double algorithmic_bytes, int K) {
+int KernelTimer::begin(int cls, double algorithmic_bytes, int K, cudaStream_t s) {
     if (!on) return -1;
     const int kb = K == 2 ? 0 : K == 4 ? 1 : K == 8 ? 2 : K == 16 ? 3 : 4;
     Pair p{cls, kb, get(), get(), algorithmic_bytes};
-    cudaEventRecord(p.a, stream);
+    cudaEventRecord(p.a, s ? s : stream);
     open.push_back(p);
     return (int)open.size() - 1;
 }
 
-void KernelTimer::end(int h) {
+void KernelTimer::end(int h, cudaStream_t s) {
     if (h < 0) return;
-    cudaEventRecord(open[h].b, stream);
+    cudaEventRecord(open[h].b, s ? s : stream);
 }
 
 void KernelTimer::collect() {
@@ -732,6 +732,7 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
     const double gcb = gt.ya ? (double)c.n_rows * (K * sizeof(cplx<R>) + 16) : 0.0;
     const int th = c.timer ? c.timer->begin(kClsSsor, matrix_bytes(c) + gcb +
                                             (double)c.n_rows * K * sizeof(cplx<R>) * 4, K) : -1;
+    const bool join = gt.ya && c.gc_stream;   // the V-cycle of the term runs on the side stream
     if (c.row_kernels == kRowsStaged) {
         constexpr int NT = StagedShape<K>::NT;
         for (int col = 0; col < nc; ++col) {
@@ -741,6 +742,7 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
                           c.seg.work_col + s0, s1 - s0, c.D, c.B, in, y);
             check_launch(c.launches);
         }
+        if (join) cudaStreamWaitEvent(c.stream, c.gc_join, 0);
         for (int col = nc - 1; col >= 0; --col) {
             const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
             if (s1 <= s0) continue;
@@ -762,6 +764,7 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
         k_ssor_fwd<R, K><<<grid, kBlock, 0, c.stream>>>(c.A, c.D, c.B, c.colour_list + s0, s1 - s0, in, y);
         check_launch(c.launches);
     }
+    if (join) cudaStreamWaitEvent(c.stream, c.gc_join, 0);
     for (int col = nc - 1; col >= 0; --col) {
         const int s0 = c.colour_ptr[col], s1 = c.colour_ptr[col + 1];
         if (s1 <= s0) continue;
@@ -783,7 +786,15 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
 template <class R, int K>
 void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, int which) {
     if constexpr (std::is_same<R, float>::value) {
-        if (c.gc) gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.stream, c.launches, c.timer);
+        if (!c.gc) return;
+        if (c.gc_stream) {
+            cudaEventRecord(c.gc_fork, c.stream);
+            cudaStreamWaitEvent(c.gc_stream, c.gc_fork, 0);
+            gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.gc_stream, c.launches, c.timer);
+            cudaEventRecord(c.gc_join, c.gc_stream);
+        } else {
+            gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.stream, c.launches, c.timer);
+        }
     }
 }
 

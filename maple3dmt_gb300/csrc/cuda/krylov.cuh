@@ -107,8 +107,10 @@ struct KernelTimer {
     double ms_k[kNumCls][kNumKBins] = {};
     double bytes_k[kNumCls][kNumKBins] = {};
     cudaEvent_t get();
-    int begin(int cls, double algorithmic_bytes, int K = 0);   // returns handle or -1
-    void end(int handle);
+    // events on the timer's stream, or on `s` for work launched on another
+    // stream that the timer's stream joins before collect()
+    int begin(int cls, double algorithmic_bytes, int K = 0, cudaStream_t s = nullptr);   // handle or -1
+    void end(int handle, cudaStream_t s = nullptr);
     void collect();   // synchronises and folds finished pairs into the totals
     void reset();
     ~KernelTimer();
@@ -146,6 +148,10 @@ struct KrylovCtx {
     // right-preconditioned form only (complex FP32): when set, each SSOR
     // apply is followed by the gradient-space term of the preconditioner
     const GcDev* gc = nullptr;
+    // when set, the V-cycle runs on gc_stream, forked after the p / s update
+    // and joined before the backward sweep, overlapping the forward sweep
+    cudaStream_t gc_stream = nullptr;
+    cudaEvent_t gc_fork = nullptr, gc_join = nullptr;
 };
 
 enum RowKernels : int { kRowsDirect = 0, kRowsStaged = 1 };

@@ -234,6 +234,9 @@ void GpuSolver::free_all() {
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
     dfree(d_host_stage); dfree(d_stage_real); dfree(d_states); dfree(d_states2);
+    if (gc_stream) { cudaStreamDestroy(gc_stream); gc_stream = nullptr; }
+    if (gc_fork) { cudaEventDestroy(gc_fork); gc_fork = nullptr; }
+    if (gc_join) { cudaEventDestroy(gc_join); gc_join = nullptr; }
     if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
     kv_K = 0; fwd_cap = 0; dc_K = 0; hc_cap = 0; obs_cap = 0; diag_cap = 0;
     ready = false; have_sigma = false; lap_built = false; stations_set = false;
@@ -738,8 +741,24 @@ void GpuSolver::build_gc() {
     gc.inc_entries = n_inc;
     gc_pack_level0(gc, stream);
     ++launches;
+    if (!gc_stream) {
+        cuda_ok(cudaStreamCreateWithFlags(&gc_stream, cudaStreamNonBlocking), "stream");
+        cuda_ok(cudaEventCreateWithFlags(&gc_fork, cudaEventDisableTiming), "event");
+        cuda_ok(cudaEventCreateWithFlags(&gc_join, cudaEventDisableTiming), "event");
+    }
     sync();
     gc_ok = true;
+}
+
+// The gradient-space term on a FP32 batch context; with gradcorr_overlap its
+// V-cycles run on the side stream, overlapping the forward SSOR sweeps.
+void GpuSolver::attach_gc(KrylovCtx<float>& c) {
+    c.gc = &gc;
+    if (P.gradcorr_overlap == 1) {
+        c.gc_stream = gc_stream;
+        c.gc_fork = gc_fork;
+        c.gc_join = gc_join;
+    }
 }
 
 // Aggregation multigrid hierarchy of the node Laplacian just built on the
@@ -1271,7 +1290,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
         }
         cuda_ok(cudaMemcpyAsync(d_states, ls.data(), sizeof(BicgState) * Kc, cudaMemcpyHostToDevice, stream), "states");
         KrylovCtx<float> c32 = kctx32(Kc, fm.data());
-        if (use_gc) c32.gc = &gc;
+        if (use_gc) attach_gc(c32);
         if (eis) eis_init(c32, cur, d_states);
         else bicg_init(c32, cur, d_states);
         int it = 0;
@@ -1348,7 +1367,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 std::swap(cur_cap, other_cap);
                 Kc = Kn;
                 c32 = kctx32(Kc, fm.data());
-                if (use_gc) c32.gc = &gc;
+                if (use_gc) attach_gc(c32);
             }
             for (int i = 0; i < chunk && it < maxiter; ++i, ++it) {
                 if (eis) eis_iteration(c32, cur, d_states);

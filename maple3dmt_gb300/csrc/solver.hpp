@@ -112,6 +112,9 @@ private:
     bool gc_ok = false;
     std::vector<void*> gc_mem;
     void build_gc();
+    cudaStream_t gc_stream = nullptr;
+    cudaEvent_t gc_fork = nullptr, gc_join = nullptr;
+    void attach_gc(KrylovCtx<float>& c);
     bool want_amg() const {
         return P.divcorr_precond == 1 || (P.precision == 1 && (P.gradcorr == 1 || P.divcorr_mixed == 1));
     }
