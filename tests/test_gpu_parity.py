@@ -62,12 +62,13 @@ def test_forward_matches_oracle(g_small, precision, interleaved, row_kernels, gr
         o.release()
 
 
-@pytest.mark.parametrize("presmooth", [0, 1])
-def test_gradient_correction_cycles_match_oracle(g_small, presmooth):
-    """Both V-cycles of the gradient-space term (V(1,1), V(0,1)) give the
-    oracle's impedances and fields at the 1e-10 solve."""
+@pytest.mark.parametrize("presmooth,overlap", [(0, 1), (1, 1), (0, 0)])
+def test_gradient_correction_cycles_match_oracle(g_small, presmooth, overlap):
+    """Both V-cycles of the gradient-space term (V(1,1), V(0,1)), on the side
+    stream or on the solver's stream, give the oracle's impedances and fields
+    at the 1e-10 solve."""
     g = g_small
-    s = _gpu(g, precision=1, gradcorr=1, gradcorr_presmooth=presmooth)
+    s = _gpu(g, precision=1, gradcorr=1, gradcorr_presmooth=presmooth, gradcorr_overlap=overlap)
     o = _oracle(g)
     for fr in g["freqs"]:
         Zg = s.compute_single_frequency(fr)
