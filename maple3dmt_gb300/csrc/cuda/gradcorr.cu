@@ -89,17 +89,17 @@ __device__ __forceinline__ float2 level_row(const GcDev& g, const GcLevel& L, in
         s.x = dg * xr.x;
         s.y = dg * xr.y;
         const int q0 = __ldg(&g.inc_ptr[row]), q1 = __ldg(&g.inc_ptr[row + 1]);
-        for (int q = q0; q < q1; q += 8) {
-            float a[8];
-            float2 xv[8];
+        for (int q = q0; q < q1; q += 4) {
+            float a[4];
+            float2 xv[4];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < 4; ++u) {
                 const int2 e = q + u < q1 ? __ldg(&g.lap_pk[q + u]) : make_int2(0, 0);
                 a[u] = __int_as_float(e.y);
                 xv[u] = a[u] != 0.0f ? xf(e.x, k, K) : f2(0.0f, 0.0f);
             }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
+            for (int u = 0; u < 4; ++u) {
                 s.x += a[u] * xv[u].x;
                 s.y += a[u] * xv[u].y;
             }
