@@ -345,9 +345,9 @@ void gc_pack_level0(const GcDev& g, cudaStream_t s) {
     gc_check(nullptr);
 }
 
-GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which) {
+GcRowTerm gc_row_term(const GcDev& g, const BatchView& B) {
     GcRowTerm t;
-    t.ya = g.out0[which];
+    t.ya = g.out0;
     t.e_node = g.e_node;
     t.e_g = g.e_g;
     for (int k = 0; k < kMaxRhs; ++k) {
@@ -358,11 +358,11 @@ GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which) {
 }
 
 template <int K>
-void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
+void gc_apply_k(const GcDev& g, int n_rows, const float2* in, cudaStream_t s, long long* launches,
                 KernelTimer* timer) {
     const int nl = g.n_levels;
     if (nl < 1) return;
-    float2* out = g.out0[which];
+    float2* out = g.out0;
     // the edge vector gathered once; level-0 node vectors b, x (written, read
     // back), the scratch residual (written, read by the restriction), the
     // result (written); the Laplacian's incidence entries (value + column)
@@ -714,9 +714,9 @@ template long long dc_poisson_mixed_k<4>(const GcDev&, int, DcWork, RedScratch, 
 template long long dc_poisson_mixed_k<8>(const GcDev&, int, DcWork, RedScratch, cudaStream_t, long long*);
 template long long dc_poisson_mixed_k<16>(const GcDev&, int, DcWork, RedScratch, cudaStream_t, long long*);
 
-template void gc_apply_k<2>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
-template void gc_apply_k<4>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
-template void gc_apply_k<8>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
-template void gc_apply_k<16>(const GcDev&, int, const float2*, int, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<2>(const GcDev&, int, const float2*, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<4>(const GcDev&, int, const float2*, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<8>(const GcDev&, int, const float2*, cudaStream_t, long long*, KernelTimer*);
+template void gc_apply_k<16>(const GcDev&, int, const float2*, cudaStream_t, long long*, KernelTimer*);
 
 }  // namespace m3d

@@ -70,7 +70,7 @@ struct GcDev {
     const float* inc_g = nullptr;
     const int* e_node = nullptr;
     const float* e_g = nullptr;
-    float2* out0[2] = {nullptr, nullptr};   // [nn][kMaxRhs] V-cycle results (the iteration uses out0[0])
+    float2* out0 = nullptr;               // [nn][kMaxRhs] V-cycle result of the current half iteration
     GcLevel lv[phys::kAmgMaxLevels];
     int n_coarse = 0;
     const double* coarse_inv = nullptr;   // [n_coarse][n_coarse]
@@ -88,11 +88,11 @@ void gc_weights(const MeshDev& m, float* inc_g, float* e_g, cudaStream_t s);
 // FP32 level-0 copy (lap_pk, lap_diag32) of the current Laplacian.
 void gc_pack_level0(const GcDev& g, cudaStream_t s);
 
-// g.out0[which] = V(G~^T in), one V-cycle on every lane; in is
+// g.out0 = V(G~^T in), one V-cycle on every lane; in is
 // [n_pad][K] complex FP32.  The term G~ out0 / (i omega) is added per row by
 // the backward SSOR sweep (GcRowTerm).
 template <int K>
-void gc_apply_k(const GcDev& g, int n_rows, const float2* in, int which, cudaStream_t s, long long* launches,
+void gc_apply_k(const GcDev& g, int n_rows, const float2* in, cudaStream_t s, long long* launches,
                 KernelTimer* timer);
 
 // Solves L phi = divJ for the right-hand sides of w with cg_run set (the
@@ -105,7 +105,7 @@ template <int K>
 long long dc_poisson_mixed_k(const GcDev& g, int nn, phys::DcWork w, dev::RedScratch red, cudaStream_t s,
                              long long* sweeps);
 
-// Row term over g.out0[which] for the lanes k of B with 0 < omega_k <= g.omega_max.
-GcRowTerm gc_row_term(const GcDev& g, const BatchView& B, int which);
+// Row term over g.out0 for the lanes k of B with 0 < omega_k <= g.omega_max.
+GcRowTerm gc_row_term(const GcDev& g, const BatchView& B);
 
 }  // namespace m3d

@@ -790,19 +790,19 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
 }
 
 // One V-cycle of the gradient-space term on G~^T in (complex FP32 only),
-// output in the node buffer `which`; the backward SSOR sweep adds the term
+// output in the node buffer g.out0; the backward SSOR sweep adds the term
 // per row (GcRowTerm).
 template <class R, int K>
-void gc_term(const KrylovCtx<R>& c, const cplx<R>* in, int which) {
+void gc_term(const KrylovCtx<R>& c, const cplx<R>* in) {
     if constexpr (std::is_same<R, float>::value) {
         if (!c.gc) return;
         if (c.gc_stream) {
             cudaEventRecord(c.gc_fork, c.stream);
             cudaStreamWaitEvent(c.gc_stream, c.gc_fork, 0);
-            gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.gc_stream, c.launches, c.timer);
+            gc_apply_k<K>(*c.gc, c.n_rows, in, c.gc_stream, c.launches, c.timer);
             cudaEventRecord(c.gc_join, c.gc_stream);
         } else {
-            gc_apply_k<K>(*c.gc, c.n_rows, in, which, c.stream, c.launches, c.timer);
+            gc_apply_k<K>(*c.gc, c.n_rows, in, c.stream, c.launches, c.timer);
         }
     }
 }
@@ -819,15 +819,15 @@ void iteration_k(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     // the gradient-space term: V-cycle first, added to the preconditioned
     // vector by the backward sweep
     GcRowTerm gt;
-    if (c.gc) gt = gc_row_term(*c.gc, c.B, 0);
-    gc_term<R, K>(c, v.p, 0);
+    if (c.gc) gt = gc_row_term(*c.gc, c.B);
+    gc_term<R, K>(c, v.p);
     ssor_k<R, K>(c, v.p, v.y, v.ph, gt);
     spmv_k<R, K>(c, kSpmvAp, v.ph, v.v, v.r0, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 3 * vb, K) : -1;
     k_update_s<R, K><<<wave_grid(k_update_s<R, K>, gv), kBlock, 0, c.stream>>>(n, v.r, v.v, v.s, st, c.red);
     check_launch(c.launches);
     if (c.timer) c.timer->end(th);
-    gc_term<R, K>(c, v.s, 0);
+    gc_term<R, K>(c, v.s);
     ssor_k<R, K>(c, v.s, v.y, v.sh, gt);
     spmv_k<R, K>(c, kSpmvAs, v.sh, v.t, v.s, nullptr, st);
     th = c.timer ? c.timer->begin(kClsVec, 8 * vb, K) : -1;

@@ -726,7 +726,7 @@ void GpuSolver::build_gc() {
         g.x = zeros2(n);
         g.y = zeros2(n);
     }
-    for (int w = 0; w < 2; ++w) gc.out0[w] = zeros2((size_t)L.nn * dev::kMaxRhs);
+    gc.out0 = zeros2((size_t)L.nn * dev::kMaxRhs);
     if (P.divcorr_mixed == 1) {
         for (float2** q : {&gc.dc_x, &gc.dc_r, &gc.dc_z, &gc.dc_p, &gc.dc_ap}) *q = zeros2((size_t)L.nn * dev::kMaxRhs);
         GcPcgState* st = dalloc_zero<GcPcgState>(dev::kMaxRhs, stream);
