@@ -225,6 +225,23 @@ int m3d_forward_batch(m3d_solver* s, const double* freqs, int n_freqs, double* Z
 int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const double* obs_Z,
                        const double* obs_err, double* Z_out, double* grad);
 
+/* GN-CG product out = J^T W^2 J dsigma for all frequencies in two batched
+ * solves: the data term of ImplicitJtJOperatorFV::Mult
+ * (src/inversion/implicit_jtj_fv.cpp:78-192); the regularisation term
+ * lambda W^T W x and the log-sigma / active-cell mapping stay with the caller.
+ * Per frequency f and polarisation p: build_perturbation_rhs(p+1, dsigma) on
+ * the background field, solve_rhs, extract_delta_impedance(p+1), weighting by
+ * w^2 = 1/err^2 (0 where err <= 0), build_adjoint_rhs_from_residual (source
+ * of polarisation p), adjoint_solve, compute_sensitivity with the background
+ * field, summed.  Inner solves stop at relative residual inner_tol (the
+ * reference uses 1e-4, implicit_jtj_fv.cpp:113).  The background fields are
+ * those the last m3d_forward_batch left on the device (the reference's
+ * cache_background_fields, :37-56): freqs must be the same n_freqs <= 8
+ * frequencies, else M3D_ERR_STATE.  dsigma, out [n_cells]; obs_err
+ * [n_stations][n_freqs][4]. */
+int m3d_jtjv_batch(m3d_solver* s, const double* freqs, int n_freqs, const double* dsigma,
+                   const double* obs_err, double inner_tol, double* out);
+
 /* Batched Hermitian inner products out[k] = sum_i conj(x[i][k]) * y[i][k] of
  * K interleaved complex-FP64 DEVICE vectors x, y ([n][K] complex; K in
  * {1, 2, 4, 8, 16}); out is a device pointer to K complex values.  The

@@ -128,6 +128,15 @@ public:
         return g;
     }
 
+    // ---- GN-CG J^T W^2 J v (ImplicitJtJOperatorFV::Mult, data term) ----
+    // after forward_batch(freqs) (the cached background fields); err: [station][freq][4]
+    RealVec jtjv(const RealVec& freqs, const RealVec& dsigma, const RealVec& err, double inner_tol = 1e-4) {
+        RealVec y(nc_, 0.0);
+        check(m3d_jtjv_batch(h_, freqs.data(), (int)freqs.size(), dsigma.data(), err.data(), inner_tol, y.data()),
+              "jtjv");
+        return y;
+    }
+
     m3d_stats last_stats() const {
         m3d_stats s{};
         m3d_get_stats(h_, &s);

@@ -230,6 +230,16 @@ extern "C" int m3d_forward_batch(m3d_solver* h, const double* freqs, int nf, dou
     return guarded(h, [&](m3d::GpuSolver& s) { s.forward_batch(freqs, nf, Z_out, E_out); });
 }
 
+extern "C" int m3d_jtjv_batch(m3d_solver* h, const double* freqs, int nf, const double* dsigma,
+                              const double* obs_err, double inner_tol, double* out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!freqs || nf < 1 || !dsigma || !obs_err || !out) return fail(h, M3D_ERR_ARG, "null buffer");
+    if (nf > 8) return fail(h, M3D_ERR_ARG, "at most 8 frequencies per call");
+    if (!(inner_tol > 0.0) || inner_tol >= 1.0) return fail(h, M3D_ERR_ARG, "inner_tol must be in (0, 1)");
+    for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.jtjv_batch(freqs, nf, dsigma, obs_err, inner_tol, out); });
+}
+
 extern "C" int m3d_gradient_batch(m3d_solver* h, const double* freqs, int nf, const double* obs_Z,
                                   const double* obs_err, double* Z_out, double* grad) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");

@@ -1241,6 +1241,46 @@ void weighted_residual(int ns, int nf, int nf_total, int f0, const double2* obs,
     ck();
 }
 
+// JtJ.v weighting (ImplicitJtJOperatorFV::Mult, implicit_jtj_fv.cpp:137-150):
+// lane k = 2f + p of dZ ([K][ns][4]) times w^2, w = 1 / err (0 where err <= 0),
+// into wr_p[f] ([nf][ns][4], not conjugated, as the reference passes it).
+__global__ void k_jtj_weight(int ns, int nf, const double* __restrict__ err, const double2* __restrict__ dz,
+                             double2* __restrict__ wr0, double2* __restrict__ wr1) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * nf * ns * 4) return;
+    const int k = i / (ns * 4), s = (i / 4) % ns, c = i % 4;
+    const int f = k / 2, p = k % 2;
+    const double e = err[((size_t)s * nf + f) * 4 + c];
+    double2 v = zero2();
+    if (e > 0.0) {
+        const double w2 = 1.0 / (e * e);
+        const double2 d = dz[((size_t)k * ns + s) * 4 + c];
+        v = make_double2(w2 * d.x, w2 * d.y);
+    }
+    (p == 0 ? wr0 : wr1)[((size_t)f * ns + s) * 4 + c] = v;
+}
+
+// out lane 2f from a (pol 1 source of wr_0), lane 2f + 1 from b (pol 2 source of wr_1)
+__global__ void k_pick_pol_lanes(long n, int K, const double2* __restrict__ a, const double2* __restrict__ b,
+                                 double2* __restrict__ out) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = ((i % K) % 2 == 0) ? a[i] : b[i];
+}
+
+void jtj_weight(int ns, int nf, const double* err, const double2* dz, double2* wr0, double2* wr1, cudaStream_t s) {
+    const int n = 2 * nf * ns * 4;
+    if (n == 0) return;
+    k_jtj_weight<<<(n + kBlock - 1) / kBlock, kBlock, 0, s>>>(ns, nf, err, dz, wr0, wr1);
+    ck();
+}
+
+void pick_pol_lanes(long n_pad, int K, const double2* a, const double2* b, double2* out, cudaStream_t s) {
+    const long n = n_pad * K;
+    k_pick_pol_lanes<<<(int)((n + kBlock - 1) / kBlock), kBlock, 0, s>>>(n, K, a, b, out);
+    ck();
+}
+
 void adjoint_rhs(const StationDev& st, const MeshDev& m, const double2* wr, const HCache* hc,
                  const double* omegas, int nf, VecK out, cudaStream_t s) {
     (void)m;

@@ -179,6 +179,12 @@ long long divcorr(const MeshDev& m, const double* me_dc, VecK E, bool use_phi0, 
                   cudaStream_t s, int cg_chunk, DcCounters* counters = nullptr, const AmgDev* amg = nullptr,
                   const GcDev* mixed = nullptr);
 
+// ---- GN-CG J^T W^2 J v pieces (implicit_jtj_fv.cpp:78-192) ----
+// w^2 dZ of lane 2f + p into wr_p[f] (err [ns][nf][4], dz [2 nf][ns][4], wr_p [nf][ns][4]).
+void jtj_weight(int ns, int nf, const double* err, const double2* dz, double2* wr0, double2* wr1, cudaStream_t s);
+// out = lane 2f of a, lane 2f + 1 of b ([n_pad][K]).
+void pick_pol_lanes(long n_pad, int K, const double2* a, const double2* b, double2* out, cudaStream_t s);
+
 // ---- stations (forward_solver_fv.cpp:1490-1727, :1804-2065) ----
 // Z and H cache per (frequency f, station); E1 = rhs 2f, E2 = rhs 2f+1 of E.
 void station_impedance(const StationDev& st, VecK E, const double* omegas, int nf, HCache* hc,

@@ -233,6 +233,8 @@ void GpuSolver::free_all() {
     dc.lap_work = nullptr; dc.lap_qpos = nullptr;
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
+    dfree(d_jtj_rhs); dfree(d_jtj_dE); dfree(d_jtj_a); dfree(d_jtj_b); dfree(d_jtj_dz); dfree(d_jtj_wr0);
+    dfree(d_jtj_wr1); dfree(d_jtj_ds); dfree(d_jtj_err);
     dfree(d_host_stage); dfree(d_stage_real); dfree(d_states); dfree(d_states2);
     if (gc_stream) { cudaStreamDestroy(gc_stream); gc_stream = nullptr; }
     if (gc_fork) { cudaEventDestroy(gc_fork); gc_fork = nullptr; }
@@ -1723,6 +1725,99 @@ void GpuSolver::forward_batch(const double* freqs, int nf, double* Z_out, double
         }
     }
     stats.total_iterations = (int)it_total;
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    end_call();
+}
+
+// ImplicitJtJOperatorFV::Mult (implicit_jtj_fv.cpp:78-192) without the
+// regularisation term, for the frequencies whose background fields are
+// resident: every perturbation solve of the product in one batched solve and
+// every adjoint solve in a second, at the relaxed tolerance of :113.
+void GpuSolver::jtjv_batch(const double* freqs, int nf, const double* dsigma, const double* err, double inner_tol,
+                           double* out) {
+    if (E_nf != nf || (int)fz_freqs.size() != nf || E_K < 2 * nf || !d_hc)
+        throw std::logic_error("no resident background fields for these frequencies (m3d_forward_batch first)");
+    for (int f = 0; f < nf; ++f)
+        if (fz_freqs[f] != freqs[f])
+            throw std::logic_error("no resident background fields for these frequencies (m3d_forward_batch first)");
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call();
+    const int ns = sd.ns;
+    const int K = E_K;
+    const size_t nv = (size_t)n_pad * dev::kMaxRhs;
+    if (!d_jtj_rhs) {
+        d_jtj_rhs = dalloc<double2>(nv); d_jtj_dE = dalloc<double2>(nv);
+        d_jtj_a = dalloc<double2>(nv); d_jtj_b = dalloc<double2>(nv);
+        d_jtj_dz = dalloc<double2>((size_t)dev::kMaxRhs * std::max(1, ns) * 4);
+        d_jtj_wr0 = dalloc<double2>((size_t)8 * std::max(1, ns) * 4);
+        d_jtj_wr1 = dalloc<double2>((size_t)8 * std::max(1, ns) * 4);
+        d_jtj_ds = dalloc<double>((size_t)L.nc);
+        d_jtj_err = dalloc<double>((size_t)8 * std::max(1, ns) * 4);
+    }
+    ensure_fields(K);
+    cuda_ok(cudaMemcpyAsync(d_jtj_ds, dsigma, sizeof(double) * L.nc, cudaMemcpyHostToDevice, stream), "dsigma");
+    cuda_ok(cudaMemcpyAsync(d_jtj_err, err, sizeof(double) * (size_t)ns * nf * 4, cudaMemcpyHostToDevice, stream),
+            "err");
+    cuda_ok(cudaMemsetAsync(d_grad, 0, sizeof(double) * L.nc, stream), "memset");
+    const double tol_saved = tol_override;
+    tol_override = inner_tol;
+    struct Restore {
+        double& t;
+        double v;
+        ~Restore() { t = v; }
+    } restore{tol_override, tol_saved};
+    std::vector<int> fmap(K, 0), pol(K, -1), active(K, 0);
+    for (int k = 0; k < 2 * nf; ++k) { fmap[k] = k / 2; active[k] = 1; }
+    std::vector<double> fr(freqs, freqs + nf);
+    RhsInfo info = rhs_info(K, fmap, pol, fr);
+    current_omega = 2.0 * kPi * fr[0];
+    long long it_total = 0;
+    std::vector<int> all_it, all_st;
+    std::vector<double> all_tr;
+    auto keep = [&]() {
+        for (int k = 0; k < stats.n_rhs && k < 64; ++k) {
+            all_it.push_back(stats.iterations[k]);
+            all_st.push_back(stats.status[k]);
+            all_tr.push_back(stats.true_residual[k]);
+        }
+    };
+    // J.v: perturbation right-hand sides (:127-130) and their solves (:133)
+    cuda_ok(cudaMemsetAsync(d_jtj_rhs, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    for (int k = 0; k < 2 * nf; ++k)
+        phys::perturbation_rhs(md, d_sigma, d_jtj_ds, VecK{d_E, E_K}, k, 2.0 * kPi * fr[k / 2],
+                               VecK{d_jtj_rhs, K}, k, stream);
+    launches += 2 * nf;
+    run_adjoint(K, fmap.data(), info, d_jtj_rhs, d_jtj_dE, active);
+    it_total += stats.total_iterations;
+    keep();
+    // delta Z (:136) and its weighting (:139-150)
+    for (int k = 0; k < 2 * nf; ++k)
+        phys::delta_impedance(sd, VecK{d_jtj_dE, K}, k, d_hc + (size_t)(k / 2) * ns, k % 2 + 1,
+                              d_jtj_dz + (size_t)k * ns * 4, stream);
+    phys::jtj_weight(ns, nf, d_jtj_err, d_jtj_dz, d_jtj_wr0, d_jtj_wr1, stream);
+    launches += 2 * nf + 1;
+    // J^T: adjoint source of polarisation p from the weighted dZ of
+    // perturbation p (:154-164), adjoint solve, sensitivity (:167-175)
+    cuda_ok(cudaMemsetAsync(d_jtj_a, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    cuda_ok(cudaMemsetAsync(d_jtj_b, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+    phys::adjoint_rhs(sd, md, d_jtj_wr0, d_hc, d_omegas, nf, VecK{d_jtj_a, K}, stream);
+    phys::adjoint_rhs(sd, md, d_jtj_wr1, d_hc, d_omegas, nf, VecK{d_jtj_b, K}, stream);
+    phys::pick_pol_lanes(n_pad, K, d_jtj_a, d_jtj_b, d_adj, stream);
+    launches += 3;
+    run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
+    it_total += stats.total_iterations;
+    keep();
+    phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, nf, 2, d_grad, stream);
+    ++launches;
+    cuda_ok(cudaMemcpyAsync(out, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "out");
+    sync();
+    stats.total_iterations = (int)it_total;
+    stats.n_rhs = (int)all_it.size();
+    for (size_t k = 0; k < all_it.size() && k < 64; ++k) {
+        stats.iterations[k] = all_it[k];
+        stats.status[k] = all_st[k];
+        stats.true_residual[k] = all_tr[k];
+    }
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     end_call();
 }

@@ -51,6 +51,12 @@ public:
 
     // ---- batched ----
     void forward_batch(const double* freqs, int nf, double* Z_out, double* E_out);
+    void jtjv_batch(const double* freqs, int nf, const double* dsigma, const double* err, double inner_tol,
+                    double* out);
+    double2 *d_jtj_rhs = nullptr, *d_jtj_dE = nullptr, *d_jtj_a = nullptr, *d_jtj_b = nullptr;
+    double2 *d_jtj_dz = nullptr, *d_jtj_wr0 = nullptr, *d_jtj_wr1 = nullptr;
+    double* d_jtj_ds = nullptr;
+    double* d_jtj_err = nullptr;
     void gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,
                         double* grad);
     // batched Hermitian dot of caller-owned device vectors on the solver's

@@ -182,6 +182,18 @@ class ForwardSolverFV:
                                              Z.ctypes.data_as(c_double_p), g.ctypes.data_as(c_double_p)))
         return Z, g
 
+    def jtjv_batch(self, freqs, dsigma, obs_err, inner_tol=1e-4):
+        """J^T W^2 J dsigma summed over freqs (ImplicitJtJOperatorFV::Mult without
+        the regularisation term); needs the background fields of the same
+        frequencies from forward_batch."""
+        f, pf = _d(freqs)
+        ds, pds = _d(dsigma)
+        oe, poe = _d(obs_err)
+        out = np.zeros(self.nc)
+        self._ck(self.lib.m3d_jtjv_batch(self.h, pf, int(f.shape[0]), pds, poe, float(inner_tol),
+                                         out.ctypes.data_as(c_double_p)))
+        return out
+
     def dot_batched(self, x_ptr: int, y_ptr: int, n: int, K: int, out_ptr: int):
         """Hermitian dots of K interleaved complex128 device vectors ([n][K]);
         writes K complex values at device address out_ptr."""
