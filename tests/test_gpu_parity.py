@@ -235,6 +235,28 @@ def test_jtjv_batch_matches_oracle(g_small):
     assert ex.value.code == 2
 
 
+def test_sigma_update_matches_fresh_solver(g_small):
+    """Line-search trial steps (inversion_fv.cpp:427-436): a conductivity
+    update keeps the layout, colouring, segments and multigrid aggregates and
+    re-assembles only the values; its impedances match a solver set up from
+    scratch for the new conductivity, and the original conductivity set
+    again reproduces the first result."""
+    g = g_small
+    s = _gpu(g, precision=1)
+    Z1 = s.forward_batch(g["freqs"])
+    earth = g["cell_type"] == 0
+    sig2 = np.where(earth, g["sigma"] * np.exp(0.3 * np.random.default_rng(7).normal(size=g["sigma"].shape)),
+                    g["sigma"])
+    s.set_sigma(sig2)
+    Z2 = s.forward_batch(g["freqs"])
+    f = _gpu(g, precision=1)
+    f.set_sigma(sig2)
+    assert rel(Z2, f.forward_batch(g["freqs"])) < Z_TOL
+    assert rel(Z2, Z1) > 10 * Z_TOL
+    s.set_sigma(g["sigma"])
+    assert rel(s.forward_batch(g["freqs"]), Z1) < Z_TOL
+
+
 def test_batch_equals_single_frequency(g_small):
     g = g_small
     s = _gpu(g)
