@@ -225,6 +225,35 @@ int m3d_forward_batch(m3d_solver* s, const double* freqs, int n_freqs, double* Z
 int m3d_gradient_batch(m3d_solver* s, const double* freqs, int n_freqs, const double* obs_Z,
                        const double* obs_err, double* Z_out, double* grad);
 
+/* ---------------------------------------------------------------------- */
+/* Octree model regularisation (RegularizationOctree,                      */
+/* src/inversion/regularization_octree.cpp) on the solver's mesh.          */
+/* ---------------------------------------------------------------------- */
+
+/* RegParamsOctree (include/maple3dmt/inversion/regularization_octree.h:25-32);
+ * alpha_r (reference damping) is not used by the operators below. */
+typedef struct m3d_reg_params {
+    double alpha_s, alpha_x, alpha_y, alpha_z;
+    int n_smooth;
+} m3d_reg_params;
+
+/* RegularizationOctree::setup (:24-172): active (earth) cells, W^T W from
+ * face adjacency, neighbour lists, unit average diagonal.  Host setup once
+ * per mesh, operators on the GPU.  After m3d_solver_setup. */
+int m3d_reg_setup(m3d_solver* s, const m3d_reg_params* p);
+/* n_active (); active_to_global [n_active] */
+int m3d_reg_num_active(const m3d_solver* s, int* n_active);
+int m3d_reg_active_to_global(const m3d_solver* s, int* a2g);
+/* apply_WtW (:229-231), apply_CmCmT (:251-281), diagonal_WtW (:236-246):
+ * active-space vectors [n_active] */
+int m3d_reg_apply_wtw(m3d_solver* s, const double* x, double* y);
+int m3d_reg_apply_cmcmt(m3d_solver* s, const double* x, double* y);
+int m3d_reg_diagonal_wtw(m3d_solver* s, double* d);
+/* evaluate (:183-201) and gradient (:206-224): params = ln(sigma) per cell
+ * [n_cells], ref [n_active] (nullable: zero reference model); value
+ * nullable; grad nullable [n_cells] */
+int m3d_reg_evaluate(m3d_solver* s, const double* params, const double* ref, double* value, double* grad);
+
 /* GN-CG product out = J^T W^2 J dsigma for all frequencies in two batched
  * solves: the data term of ImplicitJtJOperatorFV::Mult
  * (src/inversion/implicit_jtj_fv.cpp:78-192); the regularisation term

@@ -137,6 +137,34 @@ public:
         return y;
     }
 
+    // ---- octree regularisation (RegularizationOctree) ----
+    int reg_setup(double alpha_s, double alpha_x, double alpha_y, double alpha_z, int n_smooth) {
+        m3d_reg_params p{alpha_s, alpha_x, alpha_y, alpha_z, n_smooth};
+        check(m3d_reg_setup(h_, &p), "reg_setup");
+        int n = 0;
+        check(m3d_reg_num_active(h_, &n), "reg_num_active");
+        n_active_ = n;
+        return n;
+    }
+    RealVec reg_apply_WtW(const RealVec& x) {
+        RealVec y(n_active_, 0.0);
+        check(m3d_reg_apply_wtw(h_, x.data(), y.data()), "reg_apply_wtw");
+        return y;
+    }
+    RealVec reg_apply_CmCmT(const RealVec& x) {
+        RealVec y(n_active_, 0.0);
+        check(m3d_reg_apply_cmcmt(h_, x.data(), y.data()), "reg_apply_cmcmt");
+        return y;
+    }
+    // ln(sigma) per cell; ref per active cell (empty: zero); returns the objective, fills grad [n_cells]
+    double reg_evaluate(const RealVec& log_sigma, const RealVec& ref, RealVec* grad = nullptr) {
+        double v = 0.0;
+        if (grad) grad->assign(nc_, 0.0);
+        check(m3d_reg_evaluate(h_, log_sigma.data(), ref.empty() ? nullptr : ref.data(), &v,
+                               grad ? grad->data() : nullptr), "reg_evaluate");
+        return v;
+    }
+
     m3d_stats last_stats() const {
         m3d_stats s{};
         m3d_get_stats(h_, &s);
@@ -146,7 +174,7 @@ public:
 
 private:
     m3d_solver* h_ = nullptr;
-    int ne_ = 0, nc_ = 0, ns_ = 0;
+    int ne_ = 0, nc_ = 0, ns_ = 0, n_active_ = 0;
     static double* d(ComplexVec& v) { return reinterpret_cast<double*>(v.data()); }
     static const double* cd(const ComplexVec& v) { return reinterpret_cast<const double*>(v.data()); }
     void check(int rc, const char* what) const {

@@ -71,6 +71,14 @@ class KernelTimes(C.Structure):
     ]
 
 
+class RegParams(C.Structure):
+    """struct m3d_reg_params."""
+    _fields_ = [
+        ("alpha_s", C.c_double), ("alpha_x", C.c_double), ("alpha_y", C.c_double), ("alpha_z", C.c_double),
+        ("n_smooth", C.c_int),
+    ]
+
+
 KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "gradcorr")
 
 SOLVER_SYMBOLS = [
@@ -80,7 +88,8 @@ SOLVER_SYMBOLS = [
     "m3d_factorize_frequency", "m3d_release_factorization", "m3d_background_E",
     "m3d_set_background_fields", "m3d_build_adjoint_rhs", "m3d_adjoint_solve", "m3d_solve_rhs",
     "m3d_compute_sensitivity", "m3d_build_perturbation_rhs", "m3d_extract_delta_impedance",
-    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_dot_batched", "m3d_dot_batched_noalloc", "m3d_get_stats",
+    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
+    "m3d_reg_apply_wtw", "m3d_reg_apply_cmcmt", "m3d_reg_diagonal_wtw", "m3d_reg_evaluate", "m3d_dot_batched", "m3d_dot_batched_noalloc", "m3d_get_stats",
     "m3d_timer_start", "m3d_timer_stop", "m3d_set_kernel_timing", "m3d_get_kernel_times",
 ]
 
@@ -112,6 +121,13 @@ def declare(lib) -> None:
     _fn(lib, "m3d_gradient_batch", C.c_int,
         [vp, c_double_p, C.c_int, c_double_p, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_jtjv_batch", C.c_int, [vp, c_double_p, C.c_int, c_double_p, c_double_p, C.c_double, c_double_p])
+    _fn(lib, "m3d_reg_setup", C.c_int, [vp, C.POINTER(RegParams)])
+    _fn(lib, "m3d_reg_num_active", C.c_int, [vp, c_int_p])
+    _fn(lib, "m3d_reg_active_to_global", C.c_int, [vp, c_int_p])
+    _fn(lib, "m3d_reg_apply_wtw", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_reg_apply_cmcmt", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_reg_diagonal_wtw", C.c_int, [vp, c_double_p])
+    _fn(lib, "m3d_reg_evaluate", C.c_int, [vp, c_double_p, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_dot_batched", C.c_int, [vp, vp, vp, C.c_longlong, C.c_int, vp])
     _fn(lib, "m3d_dot_batched_noalloc", C.c_int, [vp, vp, C.c_longlong, C.c_int, vp, vp])
     _fn(lib, "m3d_get_stats", C.c_int, [vp, C.POINTER(Stats)])

@@ -22,9 +22,10 @@ OBJ_DIR = os.path.join(HERE, "_lib", "obj")
 LIB = os.path.join(LIB_DIR, "libm3d_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-HOST_SRCS = ["host/octree_build.cpp", "host/mesh_capi.cpp", "host/layout.cpp", "host/layout_capi.cpp", "host/amg.cpp"]
-CUDA_SRCS = ["cuda/krylov.cu", "cuda/physics.cu", "cuda/gradcorr.cu", "cuda/dot.cu", "solver.cu", "capi.cu",
-             "noalloc.cu"]
+HOST_SRCS = ["host/octree_build.cpp", "host/mesh_capi.cpp", "host/layout.cpp", "host/layout_capi.cpp", "host/amg.cpp",
+             "host/regularization.cpp"]
+CUDA_SRCS = ["cuda/krylov.cu", "cuda/physics.cu", "cuda/gradcorr.cu", "cuda/regularization.cu", "cuda/dot.cu",
+             "solver.cu", "capi.cu", "noalloc.cu"]
 
 
 def _nvcc() -> str:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <algorithm>
 #include <new>
 #include <stdexcept>
 #include <string>
@@ -228,6 +229,55 @@ extern "C" int m3d_forward_batch(m3d_solver* h, const double* freqs, int nf, dou
     if (!freqs || nf < 1) return fail(h, M3D_ERR_ARG, "need frequencies");
     for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
     return guarded(h, [&](m3d::GpuSolver& s) { s.forward_batch(freqs, nf, Z_out, E_out); });
+}
+
+extern "C" int m3d_reg_setup(m3d_solver* h, const m3d_reg_params* p) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!p || p->n_smooth < 0) return fail(h, M3D_ERR_ARG, "invalid regularisation parameters");
+    m3d::RegParams q;
+    q.alpha_s = p->alpha_s; q.alpha_x = p->alpha_x; q.alpha_y = p->alpha_y; q.alpha_z = p->alpha_z;
+    q.n_smooth = p->n_smooth;
+    return guarded(h, [&](m3d::GpuSolver& s) { s.reg_setup(q); });
+}
+
+extern "C" int m3d_reg_num_active(const m3d_solver* h, int* n) {
+    if (!ready(h) || !h->s->reg_ok) return M3D_ERR_STATE;
+    if (!n) return M3D_ERR_ARG;
+    *n = h->s->reg.na;
+    return M3D_OK;
+}
+
+extern "C" int m3d_reg_active_to_global(const m3d_solver* h, int* a2g) {
+    if (!ready(h) || !h->s->reg_ok) return M3D_ERR_STATE;
+    if (!a2g) return M3D_ERR_ARG;
+    const auto& v = h->s->reg_host.a2g;
+    std::copy(v.begin(), v.end(), a2g);
+    return M3D_OK;
+}
+
+extern "C" int m3d_reg_apply_wtw(m3d_solver* h, const double* x, double* y) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!x || !y) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.reg_apply(0, x, y); });
+}
+
+extern "C" int m3d_reg_apply_cmcmt(m3d_solver* h, const double* x, double* y) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!x || !y) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.reg_apply(1, x, y); });
+}
+
+extern "C" int m3d_reg_diagonal_wtw(m3d_solver* h, double* d) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!d) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.reg_apply(2, nullptr, d); });
+}
+
+extern "C" int m3d_reg_evaluate(m3d_solver* h, const double* params, const double* ref, double* value,
+                                double* grad) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!params) return fail(h, M3D_ERR_ARG, "null buffer");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.reg_evaluate(params, ref, value, grad); });
 }
 
 extern "C" int m3d_jtjv_batch(m3d_solver* h, const double* freqs, int nf, const double* dsigma,

@@ -160,7 +160,10 @@ void build_layout(const LeafInput& in, HostLayout& L) {
 
     // ---- faces (staggered_grid.cpp:128-224) ----
     std::vector<double> fx, fy, fz;
-    std::vector<int> fnorm, fcm, fcp;
+    std::vector<int>& fnorm = L.fnorm;
+    std::vector<int>& fcm = L.fcm;
+    std::vector<int>& fcp = L.fcp;
+    fnorm.clear(); fcm.clear(); fcp.clear();
     std::vector<std::array<int, 4>> fedge;
     std::vector<int> fnedge;
     KeyMap fm((size_t)nc * 4);

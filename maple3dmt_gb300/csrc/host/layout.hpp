@@ -43,6 +43,7 @@ struct HostLayout {
     std::vector<std::array<int, 3>> hp;  // hanging pairs: coarse, child1, child2
     // faces
     std::vector<double> farea, fdual;
+    std::vector<int> fnorm, fcm, fcp;    // normal direction, minus / plus cell (after the hanging fix-up)
     std::vector<char> dead_f;
     // curl after hanging-face handling: faces x edges
     std::vector<int> ce_ptr, ce_idx;

@@ -230,6 +230,7 @@ void GpuSolver::free_all() {
     dfree(dc.lap_seg); dfree(d_lap_work); dfree(d_lap_qpos);
     free_amg();
     amg_host = AmgHierarchy{};
+    reg_free();
     dc.lap_work = nullptr; dc.lap_qpos = nullptr;
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
     dfree(d_hc); dfree(d_Z); dfree(d_wr); dfree(d_obs); dfree(d_err); dfree(d_grad);
@@ -1820,6 +1821,86 @@ void GpuSolver::jtjv_batch(const double* freqs, int nf, const double* dsigma, co
     }
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     end_call();
+}
+
+// ---------------------------------------------------------------------------
+// octree model regularisation (regularization_octree.cpp)
+// ---------------------------------------------------------------------------
+
+void GpuSolver::reg_free() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : reg_mem) cudaFree(p);
+    reg_mem.clear();
+    reg = RegDev{};
+    reg_ok = false;
+    d_reg_in = d_reg_out = d_reg_ref = nullptr;
+}
+
+void GpuSolver::reg_setup(const RegParams& p) {
+    if (!ready) throw std::logic_error("solver not set up");
+    reg_free();
+    reg_build(L, p, reg_host);
+    const RegHost& R = reg_host;
+    auto up = [&](const auto& v) {
+        auto* q = dupload(v, stream);
+        reg_mem.push_back((void*)q);
+        return q;
+    };
+    auto scratch = [&](size_t n) {
+        double* q = dalloc<double>(std::max<size_t>(1, n));
+        reg_mem.push_back((void*)q);
+        return q;
+    };
+    reg.nc = R.nc;
+    reg.na = R.na;
+    reg.n_smooth = p.n_smooth;
+    reg.alpha_s = p.alpha_s;
+    reg.a2g = up(R.a2g);
+    reg.ptr = up(R.ptr);
+    reg.idx = up(R.idx);
+    reg.val = up(R.val);
+    reg.aptr = up(R.aptr);
+    reg.aidx = up(R.aidx);
+    reg.aw = up(R.aw);
+    reg.diagw = up(R.diagw);
+    reg.t0 = scratch(R.na);
+    reg.t1 = scratch(R.na);
+    reg.t2 = scratch(R.na);
+    reg.dot = scratch(1);
+    const size_t nio = (size_t)std::max(R.na, R.nc);
+    d_reg_in = scratch(nio);
+    d_reg_out = scratch(nio);
+    d_reg_ref = scratch(R.na);
+    sync();
+    reg_ok = true;
+}
+
+void GpuSolver::reg_apply(int op, const double* x, double* y) {
+    if (!reg_ok) throw std::logic_error("regularisation not set up (m3d_reg_setup)");
+    const size_t nb = sizeof(double) * (size_t)reg.na;
+    if (op != 2) cuda_ok(cudaMemcpyAsync(d_reg_in, x, nb, cudaMemcpyHostToDevice, stream), "x");
+    if (op == 0) reg_apply_wtw(reg, d_reg_in, d_reg_out, stream);
+    else if (op == 1) reg_apply_cmcmt(reg, d_reg_in, d_reg_out, stream);
+    else reg_diagonal(reg, d_reg_out, stream);
+    ++launches;
+    cuda_ok(cudaMemcpyAsync(y, d_reg_out, nb, cudaMemcpyDeviceToHost, stream), "y");
+    sync();
+}
+
+void GpuSolver::reg_evaluate(const double* params, const double* ref, double* value, double* grad) {
+    if (!reg_ok) throw std::logic_error("regularisation not set up (m3d_reg_setup)");
+    cuda_ok(cudaMemcpyAsync(d_reg_in, params, sizeof(double) * (size_t)reg.nc, cudaMemcpyHostToDevice, stream),
+            "params");
+    if (ref)
+        cuda_ok(cudaMemcpyAsync(d_reg_ref, ref, sizeof(double) * (size_t)reg.na, cudaMemcpyHostToDevice, stream),
+                "ref");
+    m3d::reg_evaluate(reg, d_reg_in, ref ? d_reg_ref : nullptr, grad ? d_reg_out : nullptr, stream);
+    launches += 3;
+    if (value) cuda_ok(cudaMemcpyAsync(value, reg.dot, sizeof(double), cudaMemcpyDeviceToHost, stream), "value");
+    if (grad)
+        cuda_ok(cudaMemcpyAsync(grad, d_reg_out, sizeof(double) * (size_t)reg.nc, cudaMemcpyDeviceToHost, stream),
+                "grad");
+    sync();
 }
 
 void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, const double* err, double* Z_out,

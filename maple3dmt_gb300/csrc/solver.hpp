@@ -9,10 +9,12 @@
 
 #include "m3d_gb300.h"
 #include "host/amg.hpp"
+#include "host/regularization.hpp"
 #include "host/layout.hpp"
 #include "cuda/krylov.cuh"
 #include "cuda/physics.cuh"
 #include "cuda/gradcorr.cuh"
+#include "cuda/regularization.cuh"
 
 namespace m3d {
 
@@ -53,6 +55,16 @@ public:
     void forward_batch(const double* freqs, int nf, double* Z_out, double* E_out);
     void jtjv_batch(const double* freqs, int nf, const double* dsigma, const double* err, double inner_tol,
                     double* out);
+    // octree model regularisation (RegularizationOctree) on this mesh
+    RegHost reg_host;
+    RegDev reg{};
+    bool reg_ok = false;
+    std::vector<void*> reg_mem;
+    double *d_reg_in = nullptr, *d_reg_out = nullptr, *d_reg_ref = nullptr;
+    void reg_setup(const RegParams& p);
+    void reg_free();
+    void reg_apply(int op, const double* x, double* y);   // op 0: W^T W, 1: CmCm^T, 2: diagonal (x unused)
+    void reg_evaluate(const double* params, const double* ref, double* value, double* grad);
     double2 *d_jtj_rhs = nullptr, *d_jtj_dE = nullptr, *d_jtj_a = nullptr, *d_jtj_b = nullptr;
     double2 *d_jtj_dz = nullptr, *d_jtj_wr0 = nullptr, *d_jtj_wr1 = nullptr;
     double* d_jtj_ds = nullptr;

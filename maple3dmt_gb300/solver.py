@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _loader, mesh
 from ._abi import c_double_p, c_int_p
-from ._abi_solver import KERNEL_CLASSES, KernelTimes, Params, Stats
+from ._abi_solver import KERNEL_CLASSES, KernelTimes, Params, RegParams, Stats
 
 ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "OOM", 5: "NO_DEVICE", 6: "TOO_LARGE", 7: "NUMERIC"}
 
@@ -193,6 +193,45 @@ class ForwardSolverFV:
         self._ck(self.lib.m3d_jtjv_batch(self.h, pf, int(f.shape[0]), pds, poe, float(inner_tol),
                                          out.ctypes.data_as(c_double_p)))
         return out
+
+    # -- octree regularisation (RegularizationOctree) --------------------
+    def reg_setup(self, alpha_s=1.0, alpha_x=1.0, alpha_y=1.0, alpha_z=1.0, n_smooth=2):
+        p = RegParams(float(alpha_s), float(alpha_x), float(alpha_y), float(alpha_z), int(n_smooth))
+        self._ck(self.lib.m3d_reg_setup(self.h, C.byref(p)))
+        n = C.c_int()
+        self._ck(self.lib.m3d_reg_num_active(self.h, C.byref(n)))
+        self.n_active = n.value
+        return self.n_active
+
+    def reg_active_to_global(self):
+        out = np.zeros(self.n_active, np.int32)
+        self._ck(self.lib.m3d_reg_active_to_global(self.h, out.ctypes.data_as(c_int_p)))
+        return out
+
+    def reg_apply_wtw(self, x):
+        a, pa = _d(x)
+        y = np.zeros(self.n_active)
+        self._ck(self.lib.m3d_reg_apply_wtw(self.h, pa, y.ctypes.data_as(c_double_p)))
+        return y
+
+    def reg_apply_cmcmt(self, x):
+        a, pa = _d(x)
+        y = np.zeros(self.n_active)
+        self._ck(self.lib.m3d_reg_apply_cmcmt(self.h, pa, y.ctypes.data_as(c_double_p)))
+        return y
+
+    def reg_diagonal_wtw(self):
+        d = np.zeros(self.n_active)
+        self._ck(self.lib.m3d_reg_diagonal_wtw(self.h, d.ctypes.data_as(c_double_p)))
+        return d
+
+    def reg_evaluate(self, log_sigma, ref=None):
+        p, pp = _d(log_sigma)
+        r, pr = _d(ref) if ref is not None else (None, None)
+        v = C.c_double()
+        g = np.zeros(self.nc)
+        self._ck(self.lib.m3d_reg_evaluate(self.h, pp, pr, C.byref(v), g.ctypes.data_as(c_double_p)))
+        return v.value, g
 
     def dot_batched(self, x_ptr: int, y_ptr: int, n: int, K: int, out_ptr: int):
         """Hermitian dots of K interleaved complex128 device vectors ([n][K]);

@@ -145,14 +145,14 @@ def _read_m3da(path: str) -> dict:
     return out
 
 
-def run_ref(case: Case, *, layout=True, forward=True, adjoint=True, log_level=4) -> dict:
+def run_ref(case: Case, *, layout=True, forward=True, adjoint=True, regularization=False, log_level=4) -> dict:
     """Run the reference's own ForwardSolverFV on `case` (see ref_driver.cpp)."""
     if not os.path.exists(REF_SO):
         raise RuntimeError("oracle/_ref/libm3d_ref.so not built (reference tree absent?)")
     lib = C.CDLL(REF_SO)
     lib.ref_run.restype = C.c_int
     lib.ref_run.argtypes = [C.POINTER(CaseStruct), C.c_char_p, C.c_int, C.c_int]
-    flags = (1 if layout else 0) | (2 if forward else 0) | (4 if adjoint else 0)
+    flags = (1 if layout else 0) | (2 if forward else 0) | (4 if adjoint else 0) | (8 if regularization else 0)
     with tempfile.TemporaryDirectory() as td:
         path = os.path.join(td, "out.m3da")
         rc = lib.ref_run(C.byref(case.struct), path.encode(), flags, int(log_level))
@@ -196,6 +196,14 @@ def load_oracle():
             "m3d_oracle_get_edges": (C.c_int, [vp, dp, dp, ip, dp, ip, ip, ip]),
             "m3d_oracle_gradient": (C.c_int, [vp, dp, C.c_int, dp, dp, dp, dp]),
             "m3d_oracle_time_iterations": (C.c_double, [vp, C.c_double, C.c_int, dp]),
+            "m3d_oracle_reg_create": (vp, [vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),
+            "m3d_oracle_reg_destroy": (None, [vp]),
+            "m3d_oracle_reg_num_active": (C.c_int, [vp]),
+            "m3d_oracle_reg_active_to_global": (None, [vp, ip]),
+            "m3d_oracle_reg_apply_wtw": (None, [vp, dp, dp]),
+            "m3d_oracle_reg_diagonal": (None, [vp, dp]),
+            "m3d_oracle_reg_apply_cmcmt": (None, [vp, dp, dp]),
+            "m3d_oracle_reg_evaluate": (C.c_double, [vp, dp, dp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -325,3 +333,50 @@ class Oracle:
         g = np.zeros(self.nc)
         self.lib.m3d_oracle_gradient(self.h, _p(fr), len(fr), _p(oz), _p(oe), _p(Z), _p(g))
         return Z, g
+
+
+class Regularization:
+    """RegularizationOctree (src/inversion/regularization_octree.cpp) restated
+    in C on the mesh of an Oracle."""
+
+    def __init__(self, orc: "Oracle", alpha_s=1.0, alpha_x=1.0, alpha_y=1.0, alpha_z=1.0, n_smooth=2):
+        self.lib = orc.lib
+        self.orc = orc
+        self.h = self.lib.m3d_oracle_reg_create(orc.h, float(alpha_s), float(alpha_x), float(alpha_y),
+                                                float(alpha_z), int(n_smooth))
+        self.na = self.lib.m3d_oracle_reg_num_active(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.m3d_oracle_reg_destroy(self.h)
+            self.h = None
+
+    def active_to_global(self):
+        out = np.zeros(self.na, np.int32)
+        self.lib.m3d_oracle_reg_active_to_global(self.h, _p(out, ip))
+        return out
+
+    def apply_wtw(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.na)
+        self.lib.m3d_oracle_reg_apply_wtw(self.h, _p(x), _p(y))
+        return y
+
+    def diagonal(self):
+        d = np.zeros(self.na)
+        self.lib.m3d_oracle_reg_diagonal(self.h, _p(d))
+        return d
+
+    def apply_cmcmt(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.na)
+        self.lib.m3d_oracle_reg_apply_cmcmt(self.h, _p(x), _p(y))
+        return y
+
+    def evaluate(self, params, ref=None):
+        p = np.ascontiguousarray(params, np.float64)
+        r = None if ref is None else np.ascontiguousarray(ref, np.float64)
+        g = np.zeros(len(p))
+        v = self.lib.m3d_oracle_reg_evaluate(self.h, _p(p), _p(r) if r is not None else None, _p(g))
+        return v, g
+

@@ -1,5 +1,5 @@
 #!/usr/bin/env bash
-# Compile the reference's own forward-solver sources, unmodified and read in
+# Compile the reference's own forward-solver (and octree regularisation) sources, unmodified and read in
 # place from the reference tree, into a shared library that the tests use as
 # a checker (oracle/_ref/libm3d_ref.so).  Three small shims stand in for what
 # the reference tree lacks (p8est-backed OctreeMesh, the missing MT data
@@ -23,6 +23,7 @@ SRCS=(
   "$REF/src/forward/bicgstab.cpp"
   "$REF/src/utils/logger.cpp"
   "$REF/src/model/conductivity_model.cpp"
+  "$REF/src/inversion/regularization_octree.cpp"
   "$HERE/ref_driver.cpp"
 )
 CXXFLAGS=(-std=c++17 -O2 -fPIC -ffp-contract=off -DMAPLE3DMT_USE_OCTREE

@@ -1889,3 +1889,181 @@ double m3d_oracle_time_iterations(m3d_oracle* S, double freq, int n_iter, double
     free(is_bc); free(isc); free(bc1); free(rhs); free(Ep); free(AEp); free(x);
     return t2 - t1;
 }
+
+/* ------------------------------------------------------------------------ */
+/* octree regularisation  (src/inversion/regularization_octree.cpp)         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { int row, col, ord; double val; } rcoo_t;
+
+static int rcoo_cmp(const void* a, const void* b) {
+    const rcoo_t* x = (const rcoo_t*)a; const rcoo_t* y = (const rcoo_t*)b;
+    if (x->row != y->row) return x->row < y->row ? -1 : 1;
+    if (x->col != y->col) return x->col < y->col ? -1 : 1;
+    return x->ord < y->ord ? -1 : (x->ord > y->ord ? 1 : 0);
+}
+
+struct m3d_oracle_reg {
+    int nc, na;
+    int *a2g, *g2a;
+    int *ptr, *idx;  double* val;           /* W^T W, columns sorted */
+    int *aptr, *aidx; double* aw;           /* neighbours per active cell, face order */
+    double* diagw;
+    double alpha_s;
+    int n_smooth;
+};
+
+/* RegularizationOctree::setup  regularization_octree.cpp:24-172 */
+m3d_oracle_reg* m3d_oracle_reg_create(const m3d_oracle* S, double alpha_s, double alpha_x, double alpha_y,
+                                      double alpha_z, int n_smooth) {
+    const mesh_t* m = &S->m;
+    const grid_t* G = &S->G;
+    const int nc = S->nc;
+    m3d_oracle_reg* R = (m3d_oracle_reg*)xcalloc(1, sizeof(m3d_oracle_reg));
+    R->nc = nc; R->alpha_s = alpha_s; R->n_smooth = n_smooth;
+    R->g2a = (int*)xcalloc((size_t)nc + 1, sizeof(int));
+    R->a2g = (int*)xcalloc((size_t)nc + 1, sizeof(int));
+    for (int c = 0; c < nc; ++c) {
+        R->g2a[c] = -1;
+        if (m->type[c] == 0) { R->g2a[c] = R->na; R->a2g[R->na++] = c; }
+    }
+    const int na = R->na;
+    double* vol = (double*)xcalloc((size_t)nc + 1, sizeof(double));
+    for (int c = 0; c < nc; ++c) { double dx, dy, dz; cell_size_xyz(m, c, &dx, &dy, &dz); vol[c] = dx * dy * dz; }
+    rcoo_t* q = (rcoo_t*)xcalloc((size_t)4 * G->nf + 1, sizeof(rcoo_t));
+    int nq = 0;
+    /* neighbour lists: two passes (count, fill) keep the face order */
+    int* acount = (int*)xcalloc((size_t)na + 1, sizeof(int));
+    int* fa = (int*)xcalloc((size_t)G->nf + 1, sizeof(int));
+    int* fb = (int*)xcalloc((size_t)G->nf + 1, sizeof(int));
+    double* fw = (double*)xcalloc((size_t)G->nf + 1, sizeof(double));
+    int nface = 0;
+    R->diagw = (double*)xcalloc((size_t)na + 1, sizeof(double));
+    for (int f = 0; f < G->nf; ++f) {
+        int cm = G->fcm[f], cp = G->fcp[f];
+        if (cm < 0 || cp < 0 || cm >= nc || cp >= nc) continue;
+        int am = R->g2a[cm], ap = R->g2a[cp];
+        if (am < 0 || ap < 0) continue;
+        double al = G->fnorm[f] == 0 ? alpha_x : G->fnorm[f] == 1 ? alpha_y : G->fnorm[f] == 2 ? alpha_z : 1.0;
+        double ddx = m->cx[cm] - m->cx[cp], ddy = m->cy[cm] - m->cy[cp], ddz = m->cz[cm] - m->cz[cp];
+        double dist = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+        if (dist < 1e-10) continue;
+        double vgm = pow(vol[cm] * vol[cp], 1.0 / 6.0);
+        double w = al * G->farea[f] / (dist * vgm);
+        q[nq].row = am; q[nq].col = am; q[nq].val = w; q[nq].ord = nq; nq++;
+        q[nq].row = am; q[nq].col = ap; q[nq].val = -w; q[nq].ord = nq; nq++;
+        q[nq].row = ap; q[nq].col = ap; q[nq].val = w; q[nq].ord = nq; nq++;
+        q[nq].row = ap; q[nq].col = am; q[nq].val = -w; q[nq].ord = nq; nq++;
+        fa[nface] = am; fb[nface] = ap; fw[nface] = w; nface++;
+        acount[am]++; acount[ap]++;
+        R->diagw[am] += w; R->diagw[ap] += w;
+    }
+    qsort(q, (size_t)nq, sizeof(rcoo_t), rcoo_cmp);
+    R->ptr = (int*)xcalloc((size_t)na + 1, sizeof(int));
+    R->idx = (int*)xcalloc((size_t)nq + 1, sizeof(int));
+    R->val = (double*)xcalloc((size_t)nq + 1, sizeof(double));
+    int u = 0;
+    for (int t = 0; t < nq;) {
+        int r = q[t].row, c = q[t].col;
+        double s = 0.0;
+        while (t < nq && q[t].row == r && q[t].col == c) {
+            if (q[t].val < 0) s -= -q[t].val; else s += q[t].val;
+            ++t;
+        }
+        R->idx[u] = c; R->val[u] = s; R->ptr[r + 1]++; u++;
+    }
+    for (int i = 0; i < na; ++i) R->ptr[i + 1] += R->ptr[i];
+    R->aptr = (int*)xcalloc((size_t)na + 1, sizeof(int));
+    for (int i = 0; i < na; ++i) R->aptr[i + 1] = R->aptr[i] + acount[i];
+    R->aidx = (int*)xcalloc((size_t)R->aptr[na] + 1, sizeof(int));
+    R->aw = (double*)xcalloc((size_t)R->aptr[na] + 1, sizeof(double));
+    int* fill = (int*)xcalloc((size_t)na + 1, sizeof(int));
+    for (int t = 0; t < nface; ++t) {
+        int a = fa[t], b = fb[t];
+        R->aidx[R->aptr[a] + fill[a]] = b; R->aw[R->aptr[a] + fill[a]] = fw[t]; fill[a]++;
+        R->aidx[R->aptr[b] + fill[b]] = a; R->aw[R->aptr[b] + fill[b]] = fw[t]; fill[b]++;
+    }
+    /* normalisation to a unit average diagonal (:146-160) */
+    double dsum = 0.0;
+    for (int i = 0; i < na; ++i) dsum += R->diagw[i];
+    double davg = na > 0 ? dsum / na : 1.0;
+    if (davg > 1e-30) {
+        double sc = 1.0 / davg;
+        for (int k = 0; k < u; ++k) R->val[k] *= sc;
+        for (int i = 0; i < na; ++i) R->diagw[i] *= sc;
+        for (int k = 0; k < R->aptr[na]; ++k) R->aw[k] *= sc;
+    }
+    free(vol); free(q); free(acount); free(fa); free(fb); free(fw); free(fill);
+    return R;
+}
+
+void m3d_oracle_reg_destroy(m3d_oracle_reg* R) {
+    if (!R) return;
+    free(R->a2g); free(R->g2a); free(R->ptr); free(R->idx); free(R->val);
+    free(R->aptr); free(R->aidx); free(R->aw); free(R->diagw); free(R);
+}
+
+int m3d_oracle_reg_num_active(const m3d_oracle_reg* R) { return R->na; }
+
+void m3d_oracle_reg_active_to_global(const m3d_oracle_reg* R, int* a2g) {
+    for (int j = 0; j < R->na; ++j) a2g[j] = R->a2g[j];
+}
+
+/* apply_WtW (:229-231), CSRMatrix::matvec (include/maple3dmt/common.h:52-61) */
+void m3d_oracle_reg_apply_wtw(const m3d_oracle_reg* R, const double* x, double* y) {
+    for (int i = 0; i < R->na; ++i) {
+        double s = 0.0;
+        for (int k = R->ptr[i]; k < R->ptr[i + 1]; ++k) s += R->val[k] * x[R->idx[k]];
+        y[i] = s;
+    }
+}
+
+/* diagonal_WtW (:236-246) */
+void m3d_oracle_reg_diagonal(const m3d_oracle_reg* R, double* d) {
+    for (int i = 0; i < R->na; ++i) {
+        d[i] = 0.0;
+        for (int k = R->ptr[i]; k < R->ptr[i + 1]; ++k)
+            if (R->idx[k] == i) { d[i] = R->val[k]; break; }
+    }
+}
+
+/* apply_CmCmT (:251-281): 2 n_smooth diffusion passes */
+void m3d_oracle_reg_apply_cmcmt(const m3d_oracle_reg* R, const double* x, double* y) {
+    const int na = R->na;
+    double* cur = (double*)xcalloc((size_t)na + 1, sizeof(double));
+    double* tmp = (double*)xcalloc((size_t)na + 1, sizeof(double));
+    memcpy(cur, x, sizeof(double) * (size_t)na);
+    for (int pass = 0; pass < 2 * R->n_smooth; ++pass) {
+        for (int i = 0; i < na; ++i) {
+            double sum = cur[i], wt = 1.0;
+            double dg = R->diagw[i] > 0 ? R->diagw[i] : 1.0;
+            for (int k = R->aptr[i]; k < R->aptr[i + 1]; ++k) {
+                double wn = R->aw[k] / dg;
+                sum += wn * cur[R->aidx[k]];
+                wt += wn;
+            }
+            tmp[i] = sum / wt;
+        }
+        memcpy(cur, tmp, sizeof(double) * (size_t)na);
+    }
+    memcpy(y, cur, sizeof(double) * (size_t)na);
+    free(cur); free(tmp);
+}
+
+/* evaluate (:183-201) and gradient (:206-224); params = ln(sigma) per cell,
+ * ref per active cell (NULL: zero) */
+double m3d_oracle_reg_evaluate(const m3d_oracle_reg* R, const double* params, const double* ref, double* grad) {
+    const int na = R->na;
+    double* dm = (double*)xcalloc((size_t)na + 1, sizeof(double));
+    double* wd = (double*)xcalloc((size_t)na + 1, sizeof(double));
+    for (int j = 0; j < na; ++j) dm[j] = params[R->a2g[j]] - (ref ? ref[j] : 0.0);
+    m3d_oracle_reg_apply_wtw(R, dm, wd);
+    double v = 0.0;
+    for (int j = 0; j < na; ++j) v += dm[j] * wd[j];
+    if (grad) {
+        for (int c = 0; c < R->nc; ++c) grad[c] = 0.0;
+        for (int j = 0; j < na; ++j) grad[R->a2g[j]] = 2.0 * R->alpha_s * wd[j];
+    }
+    free(dm); free(wd);
+    return R->alpha_s * v;
+}

@@ -41,6 +41,20 @@ int m3d_oracle_gradient(m3d_oracle* S, const double* freqs, int nf, const double
  * the assembled, BC-eliminated system of `freq` (setup time in *setup_s). */
 double m3d_oracle_time_iterations(m3d_oracle* S, double freq, int n_iter, double* setup_s);
 
+/* octree regularisation (src/inversion/regularization_octree.cpp) on the
+ * oracle's mesh: setup, W^T W x, diag(W^T W), CmCm^T x, objective and
+ * gradient (params = ln sigma per cell, ref per active cell or NULL). */
+typedef struct m3d_oracle_reg m3d_oracle_reg;
+m3d_oracle_reg* m3d_oracle_reg_create(const m3d_oracle* S, double alpha_s, double alpha_x, double alpha_y,
+                                      double alpha_z, int n_smooth);
+void m3d_oracle_reg_destroy(m3d_oracle_reg* R);
+int m3d_oracle_reg_num_active(const m3d_oracle_reg* R);
+void m3d_oracle_reg_active_to_global(const m3d_oracle_reg* R, int* a2g);
+void m3d_oracle_reg_apply_wtw(const m3d_oracle_reg* R, const double* x, double* y);
+void m3d_oracle_reg_diagonal(const m3d_oracle_reg* R, double* d);
+void m3d_oracle_reg_apply_cmcmt(const m3d_oracle_reg* R, const double* x, double* y);
+double m3d_oracle_reg_evaluate(const m3d_oracle_reg* R, const double* params, const double* ref, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,7 @@
 #include "maple3dmt/octree/staggered_grid.h"
 #include "maple3dmt/octree/operators.h"
 #include "maple3dmt/forward/forward_solver_fv.h"
+#include "maple3dmt/inversion/regularization_octree.h"
 #include "maple3dmt/data/mt_data.h"
 #include "maple3dmt/utils/logger.h"
 
@@ -112,6 +113,33 @@ extern "C" int ref_run(const m3d_case* cs, const char* out_path, int flags, int 
 
     Writer w(out_path);
     if (!w.f) return 1;
+
+    if (flags & 8) {
+        // RegularizationOctree (src/inversion/regularization_octree.cpp:24-286) with
+        // fixed parameters: alpha_s 1.5, alpha_x 1.0, alpha_y 0.8, alpha_z 0.5,
+        // n_smooth 2; test vector x_j = sin(0.37 j) + j / n_active; model
+        // params = ln(sigma), reference model ln(0.01) on every active cell.
+        inversion::RegParamsOctree rg;
+        rg.alpha_s = 1.5; rg.alpha_x = 1.0; rg.alpha_y = 0.8; rg.alpha_z = 0.5; rg.n_smooth = 2;
+        inversion::RegularizationOctree reg;
+        reg.setup(mesh, rg);
+        const int na = reg.n_active();
+        std::vector<int> a2g(reg.active_to_global().begin(), reg.active_to_global().end());
+        RealVec x(na), wx, cx, dg;
+        for (int j = 0; j < na; ++j) x[j] = std::sin(0.37 * j) + (double)j / na;
+        reg.apply_WtW(x, wx);
+        reg.apply_CmCmT(x, cx);
+        reg.diagonal_WtW(dg);
+        model::ConductivityModel m;
+        m.init_3d(cs->n_cells, cs->sigma_bg);
+        for (int c = 0; c < cs->n_cells; ++c) m.params()[c] = std::log(cs->sigma[c]);
+        reg.set_reference_model(RealVec(na, std::log(0.01)));
+        RealVec gr;
+        reg.gradient(m, gr);
+        w.i("reg_a2g", a2g); w.d("reg_x", x); w.d("reg_wtw_x", wx); w.d("reg_cmcm_x", cx);
+        w.d("reg_diag", dg); w.d("reg_eval", std::vector<double>{reg.evaluate(m)}); w.d("reg_grad", gr);
+        if (!(flags & 7)) return 0;
+    }
 
     forward::ForwardParamsFV fp;
     fp.bicgstab_tol = cs->bicgstab_tol;

@@ -56,6 +56,23 @@ def make(name, sv, tol, maxiter, seed, layout=True):
     print(name, os.path.getsize(path), "bytes")
 
 
+def make_regularization(name, sv):
+    """RegularizationOctree outputs of the reference (fixed parameters in
+    oracle/ref_driver.cpp): active cells, W^T W x, CmCm^T x, diag(W^T W),
+    the objective and its gradient."""
+    case = oracle.Case.from_survey(sv)
+    r = oracle.run_ref(case, layout=False, forward=False, adjoint=False, regularization=True)
+    lv = sv.leaves
+    out = dict(domain=np.array(lv.domain), min_level=lv.min_level, max_level=lv.max_level, level=lv.level,
+               cx=lv.cx, cy=lv.cy, cz=lv.cz, cell_type=lv.cell_type, sigma=sv.sigma, sigma_bg=sv.sigma_bg,
+               stations=sv.stations, freqs=sv.freqs)
+    for k in ("reg_a2g", "reg_x", "reg_wtw_x", "reg_cmcm_x", "reg_diag", "reg_eval", "reg_grad"):
+        out["ref_" + k] = r[k]
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    print(name, os.path.getsize(path), "bytes")
+
+
 def main():
     if oracle.build_ref() is None:
         raise SystemExit("reference tree not available: cannot regenerate golden fixtures")
@@ -64,6 +81,9 @@ def main():
     # the CPU-runnable halfspace configuration (5x5 stations, 1 Hz), at the
     # reference's own tolerance 1e-7
     make("halfspace_c1", mesh.halfspace_survey(), tol=1e-7, maxiter=5000, seed=2, layout=False)
+    # octree regularisation on the small mesh and on a 4/6-level layered mesh
+    make_regularization("regularization_small", mesh.small_survey(freqs=(0.5, 4.0)))
+    make_regularization("regularization_layered", mesh.layered_block_survey(min_level=4, max_level=6))
 
 
 if __name__ == "__main__":

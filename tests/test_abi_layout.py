@@ -10,12 +10,12 @@ import pytest
 
 from conftest import ROOT
 
-STRUCTS = ("m3d_params", "m3d_stats", "m3d_kernel_times")
+STRUCTS = ("m3d_params", "m3d_stats", "m3d_kernel_times", "m3d_reg_params")
 
 
 def _probe(tmp_path):
-    from maple3dmt_gb300._abi_solver import KernelTimes, Params, Stats
-    mirrors = {"m3d_params": Params, "m3d_stats": Stats, "m3d_kernel_times": KernelTimes}
+    from maple3dmt_gb300._abi_solver import KernelTimes, Params, RegParams, Stats
+    mirrors = {"m3d_params": Params, "m3d_stats": Stats, "m3d_kernel_times": KernelTimes, "m3d_reg_params": RegParams}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "m3d_gb300.h"', "int main(void) {"]
     for name in STRUCTS:
         lines.append(f'    printf("{name} sizeof %zu\\n", sizeof({name}));')
