@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""Forward + adjoint solves per second on one GB300 (BASELINE metric).
+"""Forward + adjoint solves per second on one GB300 (the headline metric).
 
 Workload (the reference's "plain FP64 forward solve on GPU" configuration,
 driven to the gradient as an inversion iteration does): a 0.5 ohm-m block in a
