@@ -259,10 +259,15 @@ void amg_build(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
 }
 
 void amg_refresh(const CsrReal& A0, const AmgOptions& opt, AmgHierarchy& H) {
+    if (H.levels.empty()) throw std::runtime_error("no hierarchy to refresh");
+    H.levels[0].A = A0;
+    amg_refresh_values(opt, H);
+}
+
+void amg_refresh_values(const AmgOptions& opt, AmgHierarchy& H) {
     if (opt.omega_p != 0.0) throw std::runtime_error("multigrid refresh needs piecewise-constant prolongation");
     const int nl = (int)H.levels.size();
     if (nl < 1 || (int)H.aggregates.size() != nl - 1) throw std::runtime_error("no hierarchy to refresh");
-    H.levels[0].A = A0;
     for (int l = 0; l < nl; ++l) {
         AmgLevel& L = H.levels[l];
         const std::vector<double> d = diagonal(L.A);

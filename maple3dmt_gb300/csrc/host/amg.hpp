@@ -50,5 +50,7 @@ void amg_build(const CsrReal& A, const AmgOptions& opt, AmgHierarchy& H);
 // `H` (the costly part of the setup).  Only for piecewise-constant
 // prolongation (omega_p = 0).
 void amg_refresh(const CsrReal& A, const AmgOptions& opt, AmgHierarchy& H);
+// The same with the new values already written into H.levels[0].A.
+void amg_refresh_values(const AmgOptions& opt, AmgHierarchy& H);
 
 }  // namespace m3d

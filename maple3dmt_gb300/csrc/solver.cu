@@ -230,6 +230,9 @@ void GpuSolver::free_all() {
     dfree(dc.lap_seg); dfree(d_lap_work); dfree(d_lap_qpos);
     free_amg();
     amg_host = AmgHierarchy{};
+    a0_pos_q.clear();
+    a0_pos_d.clear();
+    if (h_lap_pinned) { cudaFreeHost(h_lap_pinned); h_lap_pinned = nullptr; }
     reg_free();
     dc.lap_work = nullptr; dc.lap_qpos = nullptr;
     dfree(sd.cell); dfree(sd.geom); dfree(sd.e_ptr); dfree(sd.e_row); dfree(sd.e_code); dfree(sd.sigma_cell);
@@ -770,32 +773,67 @@ void GpuSolver::attach_gc(KrylovCtx<float>& c) {
 void GpuSolver::build_amg() {
     const auto t0 = std::chrono::steady_clock::now();
     const int nn = L.nn;
-    std::vector<double> diag(nn), off(h_inc_other.size());
-    cuda_ok(cudaMemcpyAsync(diag.data(), dc.lap_diag, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream), "lap");
-    cuda_ok(cudaMemcpyAsync(off.data(), dc.lap_off, sizeof(double) * off.size(), cudaMemcpyDeviceToHost, stream),
-            "lap");
+    const size_t n_inc = h_inc_other.size();
+    // the Laplacian read back through a pinned staging buffer
+    if (!h_lap_pinned) cuda_ok(cudaMallocHost(&h_lap_pinned, sizeof(double) * (nn + n_inc + 1)), "pinned");
+    double* diag = h_lap_pinned;
+    double* off = h_lap_pinned + nn;
+    cuda_ok(cudaMemcpyAsync(diag, dc.lap_diag, sizeof(double) * nn, cudaMemcpyDeviceToHost, stream), "lap");
+    cuda_ok(cudaMemcpyAsync(off, dc.lap_off, sizeof(double) * n_inc, cudaMemcpyDeviceToHost, stream), "lap");
     sync();
-    CsrReal A0;
-    A0.n_rows = A0.n_cols = nn;
-    A0.ptr.assign(nn + 1, 0);
-    for (int v = 0; v < nn; ++v) {
-        for (int q = h_inc_ptr[v]; q < h_inc_ptr[v + 1]; ++q)
-            if (off[q] != 0.0) { A0.col.push_back(h_inc_other[q]); A0.val.push_back(off[q]); }
-        A0.col.push_back(v);
-        A0.val.push_back(diag[v]);
-        A0.ptr[v + 1] = (int)A0.col.size();
-    }
     AmgOptions opt;
     opt.omega_p = 0.0;   // piecewise-constant prolongation (the kernels assume it)
     AmgHierarchy& H = amg_host;
     bool built = false;
-    if (!H.levels.empty() && H.levels[0].A.n_rows == nn) {
-        try {
-            amg_refresh(A0, opt, H);   // same mesh: keep the aggregates
-            built = true;
-        } catch (const std::exception&) {
-            built = false;
+    // same mesh and zero pattern: write level 0's values in place and refresh
+    // the coarse operators on the kept aggregates
+    if (!H.levels.empty() && H.levels[0].A.n_rows == nn && a0_pos_q.size() == n_inc && (int)a0_pos_d.size() == nn) {
+        bool same = true;
+        std::vector<double>& val = H.levels[0].A.val;
+        for (int v = 0; v < nn && same; ++v) {
+            for (int q = h_inc_ptr[v]; q < h_inc_ptr[v + 1]; ++q) {
+                const int p = a0_pos_q[q];
+                if ((off[q] != 0.0) != (p >= 0)) { same = false; break; }
+                if (p >= 0) val[p] = off[q];
+            }
+            val[a0_pos_d[v]] = diag[v];
         }
+        if (same) {
+            try {
+                amg_refresh_values(opt, H);
+                built = true;
+            } catch (const std::exception&) {
+                built = false;
+            }
+        }
+    }
+    if (!built) {
+        CsrReal A0;
+        A0.n_rows = A0.n_cols = nn;
+        A0.ptr.assign(nn + 1, 0);
+        a0_pos_q.assign(n_inc, -1);
+        a0_pos_d.assign(nn, -1);
+        for (int v = 0; v < nn; ++v) {
+            for (int q = h_inc_ptr[v]; q < h_inc_ptr[v + 1]; ++q)
+                if (off[q] != 0.0) {
+                    a0_pos_q[q] = (int)A0.col.size();
+                    A0.col.push_back(h_inc_other[q]);
+                    A0.val.push_back(off[q]);
+                }
+            a0_pos_d[v] = (int)A0.col.size();
+            A0.col.push_back(v);
+            A0.val.push_back(diag[v]);
+            A0.ptr[v + 1] = (int)A0.col.size();
+        }
+        if (!H.levels.empty() && H.levels[0].A.n_rows == nn) {
+            try {
+                amg_refresh(A0, opt, H);   // same mesh: keep the aggregates
+                built = true;
+            } catch (const std::exception&) {
+                built = false;
+            }
+        }
+        if (!built) amg_pending_A0 = std::move(A0);
     }
     const int nl_dev = amg_ok ? amg.n_levels : 0;
     if (built && nl_dev == (int)H.levels.size()) {
@@ -822,7 +860,8 @@ void GpuSolver::build_amg() {
     free_amg();
     if (!built) {
         try {
-            amg_build(A0, opt, H);
+            amg_build(amg_pending_A0, opt, H);
+            amg_pending_A0 = CsrReal{};
         } catch (const std::exception&) {
             H = AmgHierarchy{};
             return;   // Jacobi PCG

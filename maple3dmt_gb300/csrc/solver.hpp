@@ -119,6 +119,9 @@ private:
     phys::AmgDev amg{};
     bool amg_ok = false;
     AmgHierarchy amg_host;          // kept between conductivity updates: aggregates are reused
+    double* h_lap_pinned = nullptr; // pinned staging of the Laplacian read back for the host setup
+    std::vector<int> a0_pos_q, a0_pos_d;   // incidence / diagonal -> position in the level-0 operator values
+    CsrReal amg_pending_A0;         // level-0 operator waiting for a full build
     double amg_setup_ms = 0.0;      // host time of the last multigrid setup
     std::vector<void*> amg_mem;
     void build_amg();
