@@ -79,7 +79,7 @@ def build_library(force: bool = False, verbose: bool = False, extra_nvcc: list[s
                     raise RuntimeError(f"compile failed: {cmd[-3]}")
     if jobs or force or not os.path.exists(LIB):
         tmp = LIB + f".{os.getpid()}.tmp"
-        cmd = [nvcc, "-shared", *ARCH, "-o", tmp, *objs]
+        cmd = [nvcc, "-shared", *ARCH, "-o", tmp, *objs, "-lpthread"]
         _, rc, out = _compile(cmd)
         if rc != 0:
             sys.stderr.write(out)

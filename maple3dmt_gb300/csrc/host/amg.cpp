@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <stdexcept>
+#include <thread>
 
 namespace m3d {
 
@@ -280,21 +281,36 @@ void amg_refresh_values(const AmgOptions& opt, AmgHierarchy& H) {
         // A_{l+1}[I][J] = sum of a_ij over i in I, j in J (P0^T A P0), with the
         // pattern of the previous coarse operator
         AmgLevel& C = H.levels[l + 1];
-        std::vector<double> acc(C.A.n_rows, 0.0);
-        std::vector<int> pos(C.A.n_rows, -1);
         std::fill(C.A.val.begin(), C.A.val.end(), 0.0);
-        for (int I = 0; I < C.A.n_rows; ++I) {
-            for (int k = C.A.ptr[I]; k < C.A.ptr[I + 1]; ++k) pos[C.A.col[k]] = k;
-            for (int q = L.R.ptr[I]; q < L.R.ptr[I + 1]; ++q) {
-                const int i = L.R.col[q];
-                for (int k = L.A.ptr[i]; k < L.A.ptr[i + 1]; ++k) {
-                    const int J = agg[L.A.col[k]];
-                    if (J < 0) continue;
-                    if (pos[J] < C.A.ptr[I]) throw std::runtime_error("coarse pattern changed");
-                    C.A.val[pos[J]] += L.A.val[k];
+        // coarse rows are independent (each entry is summed by one thread in
+        // the same order), so they are split across host threads
+        const int nI = C.A.n_rows;
+        const int nt = std::max(1, std::min<int>(16, (int)std::thread::hardware_concurrency()));
+        std::vector<char> bad(nt, 0);
+        auto rows = [&](int t) {
+            std::vector<int> pos(nI, -1);
+            for (int I = (int)((long)nI * t / nt); I < (int)((long)nI * (t + 1) / nt); ++I) {
+                for (int k = C.A.ptr[I]; k < C.A.ptr[I + 1]; ++k) pos[C.A.col[k]] = k;
+                for (int q = L.R.ptr[I]; q < L.R.ptr[I + 1]; ++q) {
+                    const int i = L.R.col[q];
+                    for (int k = L.A.ptr[i]; k < L.A.ptr[i + 1]; ++k) {
+                        const int J = agg[L.A.col[k]];
+                        if (J < 0) continue;
+                        if (pos[J] < C.A.ptr[I]) { bad[t] = 1; return; }
+                        C.A.val[pos[J]] += L.A.val[k];
+                    }
                 }
             }
+        };
+        if (nt == 1 || nI < 4096) {
+            for (int t = 0; t < nt; ++t) rows(t);
+        } else {
+            std::vector<std::thread> th;
+            for (int t = 0; t < nt; ++t) th.emplace_back(rows, t);
+            for (auto& x : th) x.join();
         }
+        for (char b : bad)
+            if (b) throw std::runtime_error("coarse pattern changed");
     }
     const AmgLevel& Cl = H.levels.back();
     H.n_coarse = Cl.A.n_rows;
