@@ -199,6 +199,12 @@ int m3d_build_adjoint_rhs(m3d_solver* s, const double* wr, double* rhs1, double*
 int m3d_adjoint_solve(m3d_solver* s, const double* rhs, double* lambda);
 /* solve_rhs_complex (:1796-1799 -> :930-940). */
 int m3d_solve_rhs(m3d_solver* s, const double* rhs, double* x);
+/* n_rhs right-hand sides at the factorised frequency, each solved as
+ * adjoint_solve / solve_rhs does (solve_with_divcorr_, :778-888), batched 16
+ * per launch: the reference's loop over many adjoint sources (e.g. one per
+ * station and polarisation) as multi-RHS solves.  rhs, out [n_rhs][n_edges]
+ * complex; stats cover every right-hand side (first 64). */
+int m3d_solve_rhs_batch(m3d_solver* s, const double* rhs, int n_rhs, double* out);
 /* compute_sensitivity_complex (:1778-1782 -> :989-1059): g [n_cells]. */
 int m3d_compute_sensitivity(m3d_solver* s, const double* E, const double* lambda, double* g);
 /* build_perturbation_rhs_complex (:1787-1791 -> :945-984): pol 1 or 2. */

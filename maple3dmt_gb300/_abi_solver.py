@@ -88,7 +88,7 @@ SOLVER_SYMBOLS = [
     "m3d_factorize_frequency", "m3d_release_factorization", "m3d_background_E",
     "m3d_set_background_fields", "m3d_build_adjoint_rhs", "m3d_adjoint_solve", "m3d_solve_rhs",
     "m3d_compute_sensitivity", "m3d_build_perturbation_rhs", "m3d_extract_delta_impedance",
-    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
+    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_solve_rhs_batch", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
     "m3d_reg_apply_wtw", "m3d_reg_apply_cmcmt", "m3d_reg_diagonal_wtw", "m3d_reg_evaluate", "m3d_dot_batched", "m3d_dot_batched_noalloc", "m3d_get_stats",
     "m3d_timer_start", "m3d_timer_stop", "m3d_set_kernel_timing", "m3d_get_kernel_times",
 ]
@@ -114,6 +114,7 @@ def declare(lib) -> None:
     _fn(lib, "m3d_build_adjoint_rhs", C.c_int, [vp, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_adjoint_solve", C.c_int, [vp, c_double_p, c_double_p])
     _fn(lib, "m3d_solve_rhs", C.c_int, [vp, c_double_p, c_double_p])
+    _fn(lib, "m3d_solve_rhs_batch", C.c_int, [vp, c_double_p, C.c_int, c_double_p])
     _fn(lib, "m3d_compute_sensitivity", C.c_int, [vp, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_build_perturbation_rhs", C.c_int, [vp, C.c_int, c_double_p, c_double_p])
     _fn(lib, "m3d_extract_delta_impedance", C.c_int, [vp, c_double_p, C.c_int, c_double_p])

@@ -200,6 +200,12 @@ extern "C" int m3d_adjoint_solve(m3d_solver* h, const double* rhs, double* lambd
     return guarded(h, [&](m3d::GpuSolver& s) { s.adjoint_solve(rhs, lambda, false); });
 }
 
+extern "C" int m3d_solve_rhs_batch(m3d_solver* h, const double* rhs, int n_rhs, double* out) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!rhs || !out || n_rhs < 1) return fail(h, M3D_ERR_ARG, "null buffer or no right-hand side");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.solve_rhs_batch(rhs, n_rhs, out); });
+}
+
 extern "C" int m3d_solve_rhs(m3d_solver* h, const double* rhs, double* x) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!rhs || !x) return fail(h, M3D_ERR_ARG, "null buffer");

@@ -55,6 +55,7 @@ public:
     void forward_batch(const double* freqs, int nf, double* Z_out, double* E_out);
     void jtjv_batch(const double* freqs, int nf, const double* dsigma, const double* err, double inner_tol,
                     double* out);
+    void solve_rhs_batch(const double* rhs, int n_rhs, double* out);
     // octree model regularisation (RegularizationOctree) on this mesh
     RegHost reg_host;
     RegDev reg{};

@@ -144,6 +144,13 @@ class ForwardSolverFV:
         self._ck(self.lib.m3d_solve_rhs(self.h, pr, x.ctypes.data_as(c_double_p)))
         return x
 
+    def solve_rhs_batch(self, rhs):
+        """Many right-hand sides [n][n_edges] at the factorised frequency (16 per batched solve)."""
+        r, pr = _c(np.atleast_2d(rhs))
+        out = np.zeros_like(r)
+        self._ck(self.lib.m3d_solve_rhs_batch(self.h, pr, int(r.shape[0]), out.ctypes.data_as(c_double_p)))
+        return out
+
     def compute_sensitivity_complex(self, E, lam):
         e, pe = _c(E)
         l, pl = _c(lam)

@@ -285,6 +285,19 @@ def test_error_codes(g_small):
     assert e.value.code == 1
 
 
+def test_solve_rhs_batch_equals_single_solves(g_small):
+    """Twenty right-hand sides at one frequency (two launch groups of up to 16)
+    give the single solve_rhs results."""
+    g = g_small
+    s = _gpu(g)
+    s.compute_single_frequency(g["freqs"][0])
+    rng = np.random.default_rng(11)
+    B = rng.normal(size=(20, s.ne)) + 1j * rng.normal(size=(20, s.ne))
+    X = s.solve_rhs_batch(B)
+    for k in (0, 7, 15, 16, 19):
+        assert rel(X[k], s.solve_rhs_complex(B[k])) < 1e-8
+
+
 def test_solution_linear_in_rhs(g_small):
     """Size-independent property: x(b1 + 2 b2) = x(b1) + 2 x(b2) to solver tolerance."""
     g = g_small
