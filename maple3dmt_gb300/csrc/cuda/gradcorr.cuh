@@ -21,12 +21,15 @@
 // preconditions the divergence-correction PCG (host/amg.cpp).  B is a
 // different preconditioner for the same system, so the converged solution
 // and the FP64 true-residual test are unchanged; only the iteration count
-// drops (at 0.01 Hz by an order of magnitude).
+// drops (at 0.01 Hz about five-fold on the 1.7 M-edge mesh).
 //
-// The V-cycle runs in FP32 on [n][K] complex node vectors, reading the FP64
-// level operators of the device hierarchy (level 0 through the node
-// incidence of the divergence-correction Laplacian, coarser levels CSR), so
-// a conductivity update that refreshes the hierarchy refreshes it here too.
+// The V-cycle (V(0,1) by default: post-smoothing only) runs in FP32 on
+// [n][K] complex node vectors.  Level 0 is read from a packed FP32 copy of the
+// divergence-correction Laplacian's incidence lists (gc_pack_level0, redone
+// whenever the Laplacian is rebuilt); the coarser levels read the FP64 CSR
+// operators of the device hierarchy, which a conductivity update refreshes in
+// place.  The same cycle, run as V(1,1), preconditions the FP32 PCG of the
+// mixed-precision divergence correction (dc_poisson_mixed_k).
 #pragma once
 
 #include <cuda_runtime.h>
