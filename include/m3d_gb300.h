@@ -117,7 +117,9 @@ typedef struct m3d_params {
     int divcorr_precond;      /* divergence-correction PCG preconditioner: 0 Jacobi (the
                                  reference's), 1 aggregation multigrid V-cycle */
     int ssor_form;            /* mixed-precision inner solve: 0 right-preconditioned SSOR-BiCGStab
-                                 as the reference, 1 Eisenstat split form (staged rows) */
+                                 as the reference, 1 Eisenstat split form (staged rows) for batches
+                                 without a right-hand side that gets the gradient-space term (those
+                                 always run the right-preconditioned form) */
     int gradcorr;             /* 1: the mixed-precision inner solve adds a gradient-space term
                                  G (i omega L)^-1 G^T (one multigrid V-cycle on the divergence-
                                  correction Laplacian L) to the SSOR preconditioner of the
