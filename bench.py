@@ -1,23 +1,32 @@
 #!/usr/bin/env python
 """Forward + adjoint solves per second on one GB300 (the headline metric).
 
-Workload (the reference's "plain FP64 forward solve on GPU" configuration,
-driven to the gradient as an inversion iteration does): a 0.5 ohm-m block in a
-10/100/1000 ohm-m three-layer earth, octree min/max level 6/7 (1.69M edges),
-121 stations on an 11x11 grid at 1 km, 8 frequencies log-spaced 0.01-100 Hz,
-both polarisations.  One step = forward solves for all 16 (frequency,
-polarisation) right-hand sides, weighted residual, 16 adjoint solves and the
-J^T r sensitivity: 32 solves, each driven to ||b - A x|| / ||b|| <= 1e-7
-checked in FP64 (InversionFV::compute_gradient_ of the reference for every
-frequency).  Synthetic data: seeded 5 % noise on the 1-D 100 ohm-m halfspace
-impedance; random-free model.
+Workload C2 (the reference's "plain FP64 forward solve on GPU"
+configuration, driven to the gradient as an inversion iteration does): a
+0.5 ohm-m block in a 10/100/1000 ohm-m three-layer earth, octree min/max
+level 6/7 (1.69M edges), 121 stations on an 11x11 grid at 1 km, 8
+frequencies log-spaced 0.01-100 Hz, both polarisations.  One step = forward
+solves for all 16 (frequency, polarisation) right-hand sides, weighted
+residual, 16 adjoint solves and the J^T r sensitivity: 32 solves, each driven
+to ||b - A x|| / ||b|| <= 1e-7 checked in FP64 (InversionFV::compute_gradient_
+of the reference for every frequency).  Synthetic data: seeded 5 % noise on
+the 1-D 100 ohm-m halfspace impedance.
 
-  value : solves/s, device-event time of the step with sigma resident
-  e2e   : solves/s through the public C ABI with host buffers (set_sigma +
-          gradient call, host<->device copies inside the timed region)
+  value   : solves/s, device-event time of the step with sigma resident
+  e2e     : solves/s through the public C ABI with host buffers (set_sigma +
+            gradient call, host<->device copies inside the timed region)
+  plain   : the same step as the plain FP64 GPU solve (one frequency per call,
+            complex128 SSOR-BiCGStab, Jacobi divergence correction), measured
+            in the same run: the denominator of the batched-vs-plain ratio
+  cpu_baseline : the reference's CPU algorithm (the C restatement in oracle/)
+            on the host cores, converged solves of a stated sample
 
-`--impl reference` times the reference's CPU algorithm (the C restatement in
-oracle/, the only CPU path available on the GPU machine) on the same system.
+`--impl reference` times the reference's CPU algorithm alone on all host
+cores (complete adjoint solves of the two highest frequencies, one process
+per core as the reference's frequency-parallel MPI groups), with its mesh read
+from the committed leaf list (oracle/leaves/) so that the GPU library is never
+loaded.  Under torchrun (N > 1) frequencies are split round-robin over the
+ranks (freq_parallel.cpp:99-117) and the gradient is summed once.
 """
 from __future__ import annotations
 
@@ -36,6 +45,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "fwd+adjoint solves/sec per GB300, learned+batched vs plain, at 1e-7 rel residual"
 UNIT = "solves/s"
+TOL = 1e-7
 
 
 def parse():
@@ -44,19 +54,22 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c2", "c5"],
+                    help="c2: the headline workload; c5: the inversion iteration at scale (levels 6/8, "
+                         "3.1 M edges, 400 stations, 24 frequencies 0.001-1000 Hz, data from a random model)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--forward", default="reference", choices=["interleaved", "reference"])
-    ap.add_argument("--min-level", type=int, default=6)
-    ap.add_argument("--max-level", type=int, default=7)
-    ap.add_argument("--nfreq", type=int, default=8)
     # profiling runs only (a capped solve is not a bench number): Krylov
-    # iteration cap per solve, and skipping the CPU baseline
+    # iteration cap per solve
     ap.add_argument("--maxiter", type=int, default=5000)
-    ap.add_argument("--plain", action="store_true",
-                    help="the plain GPU arm the batched solve is compared with: one frequency per call, complex128 "
-                         "Krylov, CSR row kernels, Jacobi divergence correction, the reference's forward strategy")
+    ap.add_argument("--arm", default="batched", choices=["batched", "plain"],
+                    help="plain: time only the plain FP64 GPU arm as the main value (profiling)")
+    ap.add_argument("--plain-steps", type=int, default=1,
+                    help="timed steps of the plain FP64 arm measured after the batched arm (0: skip)")
+    ap.add_argument("--plain-row-kernels", type=int, default=1, choices=[0, 1])
     ap.add_argument("--ssor-form", type=int, default=1, choices=[0, 1],
-                    help="inner FP32 solve: 0 right-preconditioned SSOR-BiCGStab, 1 Eisenstat split form")
+                    help="inner FP32 solve of batches without the gradient-space term: "
+                         "0 right-preconditioned SSOR-BiCGStab, 1 Eisenstat split form")
     ap.add_argument("--divcorr-precond", type=int, default=1, choices=[0, 1],
                     help="divergence-correction PCG: 0 Jacobi (the reference's), 1 aggregation multigrid")
     ap.add_argument("--row-kernels", type=int, default=1, choices=[0, 1],
@@ -65,37 +78,49 @@ def parse():
                     help="1: gradient-space term (multigrid V-cycle on the divergence-correction Laplacian) in "
                          "the FP32 inner solve's preconditioner for frequencies <= --gradcorr-fmax")
     ap.add_argument("--gradcorr-fmax", type=float, default=1e30)
-    ap.add_argument("--gradcorr-presmooth", type=int, default=0, choices=[0, 1],
-                    help="V-cycle of the gradient-space term: 1 V(1,1), 0 V(0,1)")
-    ap.add_argument("--divcorr-mixed", type=int, default=1, choices=[0, 1],
-                    help="1: divergence-correction Poisson solve as FP32 PCG inside FP64 refinement")
-    ap.add_argument("--inner-tol-floor", type=float, default=3e-5,
-                    help="smallest relative residual asked of one complex-FP32 inner solve")
-    ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1],
-                    help="1: inner FP32 solve to the final tolerance with FP64 residual replacement")
-    ap.add_argument("--gradcorr-overlap", type=int, default=1, choices=[0, 1],
-                    help="1: V-cycles of the gradient-space term on a second stream, overlapping the SSOR sweep")
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--gradcorr-presmooth", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--divcorr-mixed", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--inner-tol-floor", type=float, default=3e-5)
+    ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--gradcorr-overlap", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--cpu-procs", type=int, default=0, help="CPU worker processes (0: all host cores)")
     return ap.parse_args()
 
 
-def workload(args):
+# ---------------------------------------------------------------------------
+# the workload (identical inputs for both arms)
+# ---------------------------------------------------------------------------
+
+CONFIG = "c2"
+
+
+def spec():
+    from maple3dmt_gb300 import workloads
+    return {"c2": workloads.C2, "c5": workloads.C5}[CONFIG]
+
+
+def survey_inputs(stations=None):
+    """Stations, frequencies, observed data and errors of the workload."""
     import numpy as np
-    from maple3dmt_gb300 import mesh
-    freqs = np.logspace(-2, 2, 8) if args.nfreq == 8 else np.logspace(-2, 2, args.nfreq)
-    sv = mesh.layered_block_survey(min_level=args.min_level, max_level=args.max_level, freqs=freqs)
-    ns, nf = len(sv.stations), len(sv.freqs)
-    rng = np.random.default_rng(42)
-    om = 2 * math.pi * sv.freqs
-    z1 = np.sqrt(1j * om * mesh.MU0 / 0.01)                        # 100 ohm-m halfspace
-    obs = np.zeros((ns, nf, 4), np.complex128)
-    obs[:, :, 1] = z1[None, :]
-    obs[:, :, 2] = -z1[None, :]
-    err = np.zeros((ns, nf, 4))
-    err[:, :, 1:3] = 0.05 * np.abs(z1)[None, :, None]
-    noise = rng.normal(size=(ns, nf, 4)) + 1j * rng.normal(size=(ns, nf, 4))
-    obs = obs + 0.05 * np.abs(obs) * noise / math.sqrt(2)
-    return sv, obs, err
+    from maple3dmt_gb300 import workloads
+    sp = spec()
+    st = workloads.station_grid(sp.n_side, sp.spacing) if stations is None else stations
+    fr = np.asarray(sp.freqs, np.float64)
+    obs, err = workloads.halfspace_data(st, fr, seed=42)
+    return st, fr, obs, err
+
+
+def bench_config(ne, nc):
+    sp = spec()
+    nf = len(sp.freqs)
+    model = ("C2: layered+block earth" if CONFIG == "c2" else
+             "C5: 100 ohm-m starting halfspace, data from a seeded random layered+blocks model with 5 % noise")
+    return {"workload": f"{model}, octree levels {sp.min_level}/{sp.max_level} ({ne} edges, "
+                        f"{nc} cells), {sp.n_side * sp.n_side} stations, {nf} freqs "
+                        f"{min(sp.freqs):g}-{max(sp.freqs):g} Hz, forward+adjoint+sensitivity gradient step "
+                        f"({4 * nf} solves)",
+            "tol": TOL, "l2": "inputs larger than L2 (matrix alone 260 MB, K=16 FP32 vector 216 MB at C2)"}
 
 
 class ClockSampler:
@@ -162,82 +187,161 @@ def ncu_traffic(kernel_class):
     return None
 
 
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
 # ---------------------------------------------------------------------------
-# CPU baseline: the reference algorithm (oracle restatement) per iteration
+# the reference's CPU algorithm (oracle/ C restatement, verbatim arithmetic
+# of the reference pinned bit for bit by tests/test_oracle.py)
 # ---------------------------------------------------------------------------
 
-def _cpu_worker(args_tuple):
-    min_level, max_level, nfreq, freq, n_iter, q = args_tuple
-    import numpy as np  # noqa: F401
-    import oracle
-    from maple3dmt_gb300 import mesh
-    fr = np.logspace(-2, 2, nfreq)
-    sv = mesh.layered_block_survey(min_level=min_level, max_level=max_level, freqs=fr)
-    o = oracle.Oracle(oracle.Case.from_survey(sv))
-    q.put(("ready", os.getpid()))
-    t_it, t_setup = o.time_iterations(freq, n_iter)
-    q.put(("done", t_it / n_iter, t_setup))
+CPU_FREQS = 2     # the sample: adjoint solves of the highest CPU_FREQS frequencies
 
 
-# Iterations per solve of the reference SSOR-BiCGStab on this workload, used
-# to turn the CPU per-iteration time into solves/s: forward (reference
-# strategy, maxiter 5000, the two 0.01 Hz solves did not converge) and
-# adjoint (interleaved divergence correction), per (frequency, polarisation),
-# from the FP64 GPU solve of the same systems.
-REF_ITERS_FWD = [5000, 5000, 3114, 4073, 1244, 1213, 458, 519, 193, 179, 72, 73, 9, 10, 3, 3]
-REF_ITERS_ADJ = [530, 524, 537, 559, 501, 534, 319, 299, 146, 142, 51, 57, 22, 21, 10, 12]
-
-
-def cpu_reference(args, n_iter=3, procs=None):
-    import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    procs = procs or max(1, min(16, os.cpu_count() or 1))
-    q = ctx.Queue()
+def _cpu_worker(conn, wid, freq_index):
+    """One host process = one frequency group of the reference's MPI mode.
+    Setup: the leaf list, the reference's forward solve of its frequency (both
+    polarisations, timed and reported), the adjoint sources of the weighted
+    residual.  Then each 'solve' command runs one complete adjoint solve
+    (solve_with_divcorr_, stopped by the reference's own tests at 1e-7)."""
     import numpy as np
-    fr = np.logspace(-2, 2, args.nfreq)
-    workers = [ctx.Process(target=_cpu_worker, args=((args.min_level, args.max_level, args.nfreq,
-                                                      float(fr[i % len(fr)]), n_iter, q),)) for i in range(procs)]
-    t0 = time.time()
-    for w in workers:
-        w.start()
-    res = []
-    while len(res) < procs:
-        m = q.get()
-        if m[0] == "done":
-            res.append(m)
-    for w in workers:
-        w.join()
-    wall = time.time() - t0
-    t_iter = statistics.mean(r[1] for r in res)
-    iters = REF_ITERS_FWD + REF_ITERS_ADJ
-    solve_s = t_iter * statistics.mean(iters)
-    value = procs / solve_s
-    return {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-            "sample": (f"{procs} concurrent processes (frequency-parallel like the reference's MPI groups), "
-                       f"each {n_iter} reference SSOR-BiCGStab iterations on the assembled C2 system; "
-                       f"{t_iter:.3f} s/iteration x mean {statistics.mean(iters):.0f} iterations/solve "
-                       f"(reference-strategy iteration counts of the same 32 solves)"),
-            "seconds_per_iteration": t_iter, "wall_s": wall}
+    import oracle
+    from oracle import leaflist
+    from maple3dmt_gb300 import workloads
+    lv = leaflist.load("c2")
+    sigma = workloads.cell_sigma(lv["cell_type"], lv["cx"], lv["cy"], lv["cz"], workloads.layered_block_sigma)
+    st, fr, obs, err = survey_inputs()
+    f = float(fr[freq_index])
+    case = oracle.Case(domain=lv["domain"], min_level=lv["min_level"], max_level=lv["max_level"],
+                       level=lv["level"], cx=lv["cx"], cy=lv["cy"], cz=lv["cz"], cell_type=lv["cell_type"],
+                       sigma=sigma, sigma_bg=workloads.SIGMA_BG, stations=st, freqs=[f], tol=TOL, maxiter=5000)
+    o = oracle.Oracle(case)
+    t0 = time.perf_counter()
+    Z = o.solve_frequency(f)
+    t_fwd = time.perf_counter() - t0
+    it_fwd = o.last_iters()
+    e = err[:, freq_index, :]
+    w2 = np.where(e > 0, 1.0 / np.where(e > 0, e, 1.0) ** 2, 0.0)
+    wr = w2 * np.conj(obs[:, freq_index, :] - Z)
+    rhs = o.adjoint_rhs(wr)
+    conn.send(("ready", o.ne, o.nc, t_fwd, it_fwd, f))
+    k = 0
+    while True:
+        cmd = conn.recv()
+        if cmd != "solve":
+            break
+        t0 = time.perf_counter()
+        o.adjoint_solve(rhs[k % 2])
+        dt = time.perf_counter() - t0
+        conn.send(("done", dt, o.last_iters()))
+        k += 1
+    conn.close()
+
+
+class CpuReference:
+    """P spawned worker processes (spawn: safe after CUDA use in the parent)."""
+
+    def __init__(self, procs):
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        self.procs = procs
+        self.pipes, self.workers = [], []
+        for w in range(procs):
+            a, b = ctx.Pipe()
+            fi = len(spec().freqs) - 1 - (w % CPU_FREQS)
+            p = ctx.Process(target=_cpu_worker, args=(b, w, fi), daemon=True)
+            p.start()
+            self.pipes.append(a)
+            self.workers.append(p)
+        t0 = time.perf_counter()
+        self.ready = [c.recv() for c in self.pipes]
+        self.setup_s = time.perf_counter() - t0
+        self.ne, self.nc = self.ready[0][1], self.ready[0][2]
+
+    def step(self, n_workers=None):
+        """All (or the first n) workers solve one adjoint RHS at once; returns
+        (wall seconds, per-solve seconds, iterations)."""
+        use = self.pipes[: n_workers or self.procs]
+        t0 = time.perf_counter()
+        for c in use:
+            c.send("solve")
+        res = [c.recv() for c in use]
+        wall = time.perf_counter() - t0
+        return wall, [r[1] for r in res], [r[2] for r in res]
+
+    def close(self):
+        for c in self.pipes:
+            try:
+                c.send("stop")
+            except (OSError, BrokenPipeError):
+                pass
+        for p in self.workers:
+            p.join(timeout=10)
+
+    def describe(self, steps, one_core=None):
+        fwd = sorted({(round(r[5], 3), r[3], tuple(r[4])) for r in self.ready})
+        d = (f"{self.procs} processes (one per host core, frequency groups as the reference's MPI mode), each "
+             f"running complete adjoint solves (solve_with_divcorr_: lexicographic SSOR-BiCGStab with "
+             f"divergence correction, the reference's own 1e-7 stopping tests) of the "
+             f"{CPU_FREQS} highest C2 frequencies on the full C2 system, {steps} step(s) of {self.procs} "
+             f"concurrent solves; setup per process (untimed): the forward solve of its frequency, "
+             + ", ".join(f"{f} Hz: {t:.1f} s, iterations {list(it)}" for f, t, it in fwd))
+        if one_core is not None:
+            d += f"; 1 core alone: {one_core:.3f} solves/s"
+        return d
+
+
+def cpu_measure(steps, warmup, procs, one_core=True):
+    procs = procs or (os.cpu_count() or 1)
+    ref = CpuReference(procs)
+    try:
+        for _ in range(warmup):
+            ref.step()
+        v1 = None
+        if one_core:
+            wall1, _, _ = ref.step(1)
+            v1 = 1.0 / wall1
+        walls, iters = [], []
+        for _ in range(steps):
+            wall, _, it = ref.step()
+            walls.append(wall)
+            iters += it
+        total = sum(walls)
+        value = procs * steps / total
+        cb = {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+              "sample": ref.describe(steps, v1), "value_1core": v1, "cpu_model": cpu_model(),
+              "nproc": os.cpu_count(), "iterations_per_solve": iters[: 2 * CPU_FREQS],
+              "setup_s": ref.setup_s}
+        return cb, total / steps, ref.ne, ref.nc
+    finally:
+        ref.close()
 
 
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
+    if CONFIG != "c2":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference sample is defined on C2 (its data "
+                          "at C5 come from a GPU forward solve of the random model)"}), flush=True)
+        return
     W, K = args.warmup, args.steps
-    cb = None
-    vals = []
-    for i in range(max(1, min(K, 1))):
-        cb = cpu_reference(args)
-        vals.append(cb["value"])
-    v = statistics.mean(vals)
-    cb["value"] = v
+    # the CPU has no caches or JIT state that warm-up would settle beyond the
+    # per-process setup; one warm-up step stands for all W
+    cb, sec_per_step, ne, nc = cpu_measure(K, min(W, 1), args.cpu_procs, one_core=True)
+    v = cb["value"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
-            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128", "data": "synthetic",
-            "config": {"workload": f"layered+block earth, octree levels {args.min_level}/{args.max_level}, "
-                                   f"121 stations, {args.nfreq} freqs 0.01-100 Hz, fwd+adjoint gradient step",
-                       "l2": "inputs larger than L2"},
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "steps": K, "warmup": W, "ms_per_step": sec_per_step * 1000.0, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": bench_config(ne, nc), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -245,87 +349,177 @@ def run_reference_arm(args, rank, world):
 # our arm
 # ---------------------------------------------------------------------------
 
-def run_ours(args, rank, world, local_rank):
+def solver_params(args, plain):
+    p = dict(bicgstab_tol=TOL, bicgstab_maxiter=args.maxiter)
+    if plain:   # the reference's algorithm on the GPU: FP64, SSOR alone, Jacobi DivCorr; forward solves run
+        # solve_with_divcorr_ like the adjoint ones (the reference's forward strategy, BiCGStab to 1e-7 then one
+        # correction, does not reach 1e-7 at 0.01 Hz on this mesh within 5000 iterations)
+        p.update(precision=0, forward_interleaved=1, row_kernels=args.plain_row_kernels, divcorr_precond=0,
+                 ssor_form=0, gradcorr=0, divcorr_mixed=0)
+    else:
+        p.update(precision=1 if args.precision == "mixed" else 0,
+                 forward_interleaved=1 if args.forward == "interleaved" else 0,
+                 row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond, ssor_form=args.ssor_form,
+                 gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
+                 gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
+                 inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
+                 gradcorr_overlap=args.gradcorr_overlap)
+    return p
+
+
+def solver_label(args, p, freqs):
+    if not p["precision"]:
+        return {"arm": "plain FP64: one frequency per call, complex128 SSOR-BiCGStab, "
+                       + ["csr", "staged"][p["row_kernels"]]
+                       + " row kernels, Jacobi-PCG divergence correction, solve_with_divcorr_ for every solve"}
+    gc_all = p["gradcorr"] and p["gradcorr_fmax"] >= max(freqs)
+    gc_none = not p["gradcorr"] or p["gradcorr_fmax"] < min(freqs)
+    eis = "Eisenstat split form" if p["ssor_form"] else "right-preconditioned"
+    form = ("right-preconditioned (every batch carries the gradient-space term)" if gc_all
+            else eis if gc_none else f"right-preconditioned with the term, {eis} above {p['gradcorr_fmax']:g} Hz")
+    return {"arm": "batched", "precision": args.precision, "inner_tol_floor": p["inner_tol_floor"],
+            "forward": args.forward, "row_kernels": ["csr", "staged"][p["row_kernels"]],
+            "divcorr_precond": ["jacobi", "multigrid"][p["divcorr_precond"]],
+            "divcorr_solve": ["fp64 pcg", "fp32 pcg in fp64 refinement"][p["divcorr_mixed"]],
+            "ssor_form_run": form,
+            "gradcorr": (f"multigrid gradient-space term, V({p['gradcorr_presmooth']},1)"
+                         + (", V-cycle on a second stream" if p["gradcorr_overlap"] else "")) if p["gradcorr"]
+            else "off",
+            "residual_replacement": bool(p["residual_replacement"])}
+
+
+def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False):
+    """Warm-up, then `steps` timed gradient steps; returns timing and stats.
+    per_freq: one gradient_batch call per frequency (the plain arm)."""
     import numpy as np
-    from maple3dmt_gb300.solver import solver_for_survey
-    sv, obs, err = workload(args)
-    if args.plain:
-        args.precision, args.forward, args.row_kernels, args.divcorr_precond = "fp64", "reference", 0, 0
-        args.ssor_form, args.gradcorr, args.divcorr_mixed = 0, 0, 0
-    s = solver_for_survey(sv, device=local_rank, bicgstab_tol=1e-7, bicgstab_maxiter=args.maxiter,
-                          precision=1 if args.precision == "mixed" else 0,
-                          forward_interleaved=1 if args.forward == "interleaved" else 0,
-                          row_kernels=args.row_kernels, divcorr_precond=args.divcorr_precond,
-                          ssor_form=args.ssor_form, gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
-                          gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
-                          inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
-                          gradcorr_overlap=args.gradcorr_overlap)
-    nf = len(sv.freqs)
-    solves_per_step = 4 * nf
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    from maple3dmt_gb300 import freq_parallel
+
+    def allreduce(v):
+        import torch
+        t = torch.from_numpy(v)
+        dist.all_reduce(t)
+        return t.numpy()
+
+    calls = []   # per-call stats of the last per-frequency step
+
+    class PerFrequency:   # gradient_batch face, one call per frequency
+        nc = s.nc
+
+        @staticmethod
+        def gradient_batch(freqs, o, e):
+            Zs, g = [], 0.0
+            calls.clear()
+            for f in range(len(freqs)):
+                Zf, gf = s.gradient_batch(freqs[f:f + 1], np.ascontiguousarray(o[:, f:f + 1]),
+                                          np.ascontiguousarray(e[:, f:f + 1]))
+                calls.append(s.stats())
+                Zs.append(Zf)
+                g = g + gf
+            return np.concatenate(Zs), g
+
+    solver = PerFrequency if per_freq else s
+
+    def step():
+        return freq_parallel.gradient_step(solver, sv.freqs, obs, err, rank, world, allreduce if dist else None)
 
     def barrier():
         if dist:
             dist.barrier()
 
-    def step():
-        if not args.plain:
-            return s.gradient_batch(sv.freqs, obs, err)
-        # one frequency per call (K = 2 forward, 2 adjoint), gradients summed
-        Zs, g = [], None
-        for fi in range(nf):
-            Zf, gf = s.gradient_batch(sv.freqs[fi:fi + 1], obs[:, fi:fi + 1], err[:, fi:fi + 1])
-            Zs.append(Zf)
-            g = gf if g is None else g + gf
-        return np.concatenate(Zs), g
-
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     barrier()
-    clocks = ClockSampler(local_rank)
-    clocks.start()
+    if clocks:
+        clocks.start()
     s.set_kernel_timing(True)
     launches0 = s.stats()["kernel_launches"]
-    dev_ms, e2e_s = 0.0, 0.0
-    iters, tres, status = [], [], []
-    grad = None
-    for _ in range(args.steps):
+    dev_ms, e2e_s, solves = 0.0, 0.0, 0
+    iters, st = [], None
+    for _ in range(steps):
         barrier()
         t0 = time.perf_counter()
         s.set_sigma(sv.sigma)                  # host -> device conductivity
         s.timer_start()
-        Z, grad = step()
+        _, _, _, n = step()
         dev_ms += s.timer_stop()
         e2e_s += time.perf_counter() - t0
+        solves += n
         st = s.stats()
         iters.append(st["total_iterations"])
-        solver_stats = {k: st[k] for k in ("forward_iterations", "adjoint_iterations", "refinements",
-                                           "divcorr_calls", "divcorr_outer", "divcorr_cg_iterations",
-                                           "divcorr_cg_sweeps", "divcorr_setup_ms", "replacements")}
-        solver_stats["iterations_per_rhs"] = st["iterations"]
-        tr = st["true_residual"][:st["n_rhs"]]
-        solver_stats["rhs_at_tol"] = sum(1 for t in tr if t <= 1e-7)
-        solver_stats["rhs_reported"] = len(tr)
-        solver_stats["true_residual_max"] = max(tr) if tr else None
     launches = s.stats()["kernel_launches"] - launches0
     kt = s.kernel_times()
     s.set_kernel_timing(False)
-    clk = clocks.stop()
-    t_dev = dev_ms / 1000.0
+    clk = clocks.stop() if clocks else None
+    if per_freq and calls:   # the step's calls together
+        st = dict(calls[-1])
+        st["true_residual"] = [t for c in calls for t in c["true_residual"][:c["n_rhs"]]]
+        st["iterations"] = [t for c in calls for t in c["iterations"][:c["n_rhs"]]]
+        st["n_rhs"] = len(st["true_residual"])
+        for key in ("forward_iterations", "adjoint_iterations", "divcorr_cg_iterations", "divcorr_cg_sweeps"):
+            st[key] = sum(c[key] for c in calls)
+        iters[-1] = sum(st["iterations"])
+    tr = st["true_residual"][:st["n_rhs"]]
+    stats = {k: st[k] for k in ("forward_iterations", "adjoint_iterations", "refinements", "divcorr_calls",
+                                "divcorr_outer", "divcorr_cg_iterations", "divcorr_cg_sweeps", "replacements")}
+    stats.update(iterations_per_rhs=st["iterations"], rhs_at_tol=sum(1 for t in tr if t <= TOL),
+                 rhs_reported=len(tr), true_residual_max=max(tr) if tr else None)
+    return dict(t_dev=dev_ms / 1000.0, e2e_s=e2e_s, solves=solves, launches=launches, kt=kt, clocks=clk,
+                iters=iters, stats=stats)
+
+
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    from maple3dmt_gb300 import mesh
+    from maple3dmt_gb300.solver import solver_for_survey
+    from maple3dmt_gb300 import workloads
+    sp = spec()
+    plain_main = args.arm == "plain"
+    p = solver_params(args, plain_main)
+    if CONFIG == "c2":
+        sv = mesh.layered_block_survey(min_level=sp.min_level, max_level=sp.max_level, n_side=sp.n_side,
+                                       spacing=sp.spacing, freqs=np.asarray(sp.freqs))
+        _, _, obs, err = survey_inputs(sv.stations)
+        s = solver_for_survey(sv, device=local_rank, **p)
+    else:
+        # synthetic data: the forward response of the random model, 5 % noise
+        sv = mesh.c5_survey()
+        s = solver_for_survey(sv, device=local_rank, **p)
+        s.set_sigma(sv.meta["sigma_true"])
+        Z_true = s.forward_batch(sv.freqs)                          # [nf, ns, 4]
+        obs, err = workloads.noisy_data(Z_true.transpose(1, 0, 2), seed=42)
+        s.set_sigma(sv.sigma)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+    r = run_steps(s, sv, obs, err, args.steps, args.warmup, rank, world, dist, ClockSampler(local_rank),
+                  per_freq=plain_main)
+    t_dev, e2e_s = r["t_dev"], r["e2e_s"]
+    solves = r["solves"]
     if dist:
         import torch
-        tt = torch.tensor([t_dev, e2e_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, e2e_s = float(tt[0]), float(tt[1])
-        g = torch.from_numpy(grad)
-        dist.all_reduce(g)                     # frequency-group gradient sum (freq_parallel.cpp:129)
+        tt = torch.tensor([t_dev, e2e_s, float(solves)], dtype=torch.float64)
+        mx = tt[:2].clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        tot = tt[2:].clone()
+        dist.all_reduce(tot)
+        t_dev, e2e_s, solves = float(mx[0]), float(mx[1]), int(tot[0])
+    # the plain FP64 arm on the same system, measured in the same run
+    plain = None
+    if not plain_main and args.plain_steps > 0 and world == 1 and CONFIG == "c2":
+        pp = solver_params(args, True)
+        sp_ = solver_for_survey(sv, device=local_rank, **pp)
+        rp = run_steps(sp_, sv, obs, err, args.plain_steps, 1, rank, world, None, per_freq=True)
+        plain = {"value": rp["solves"] / rp["t_dev"], "unit": UNIT, "steps": args.plain_steps, "warmup": 1,
+                 "ms_per_step": rp["t_dev"] * 1000.0 / args.plain_steps,
+                 "rhs_at_tol": rp["stats"]["rhs_at_tol"], "rhs_reported": rp["stats"]["rhs_reported"],
+                 "true_residual_max": rp["stats"]["true_residual_max"],
+                 "krylov_iterations_per_step": statistics.mean(rp["iters"]), **solver_label(args, pp, sv.freqs)}
+        sp_.close()
     if rank != 0:
         return
-    total_solves = solves_per_step * args.steps * world
-    value = total_solves / t_dev
-    e2e = total_solves / e2e_s
+    value = solves / t_dev
+    e2e = solves / e2e_s
+    kt = r["kt"]
     # roofline of the dominant kernel class, on its full-width (K = 16)
     # launches: the ones whose DRAM traffic the committed ncu capture measured
     dom = max(("spmv", "ssor", "vector"), key=lambda k: kt[k]["ms"])
@@ -336,56 +530,51 @@ def run_ours(args, rank, world, local_rank):
     achieved_all = d["bytes"] / (d["ms"] * 1e-3) / 1e9 if d["ms"] else 0.0
     peak, peak_kind = measured_peak_hbm()
     traffic = ncu_traffic(dom)
+    nf = len(sv.freqs)
     h2d = s.nc * 8 + obs.size * 16 + err.size * 8
     d2h = s.nc * 8 + nf * len(sv.stations) * 4 * 16
     try:
-        cb = None if args.no_cpu else cpu_reference(args)
+        cb = None
+        if not args.no_cpu and world == 1 and CONFIG == "c2":
+            cb = cpu_measure(1, 0, args.cpu_procs, one_core=False)[0]
     except Exception as exc:  # the baseline must not hide the GPU number
         cb = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev * 1000.0 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.precision == "fp64" else "c64+c128",
+        "scaling": "strong", "vs_baseline": None, "dtype": "c128" if not p["precision"] else "c64+c128",
         "data": "synthetic",
-        "config": {"workload": f"layered+block earth, octree levels {args.min_level}/{args.max_level} "
-                               f"({s.ne} edges, {s.nc} cells), 121 stations, {nf} freqs 0.01-100 Hz, "
-                               f"forward+adjoint+sensitivity gradient step ({solves_per_step} solves)",
-                   "tol": 1e-7, "precision": args.precision, "inner_tol_floor": args.inner_tol_floor,
-                   "residual_replacement": bool(args.residual_replacement),
-                   "forward": args.forward,
-                   "colours": s.n_colours, "row_kernels": ["csr", "staged"][args.row_kernels],
-                   "divcorr_precond": ["jacobi", "multigrid"][args.divcorr_precond],
-                   "divcorr_solve": ["fp64 pcg", "fp32 pcg in fp64 refinement"][args.divcorr_mixed],
-                   "ssor_form": ["right-preconditioned", "eisenstat"][args.ssor_form],
-                   "gradcorr": (f"multigrid gradient-space term, V({args.gradcorr_presmooth},1), "
-                                f"f <= {args.gradcorr_fmax:g} Hz"
-                                + (", V-cycle on a second stream" if args.gradcorr_overlap else "")
-                                if args.gradcorr else "off"),
-                   "arm": "plain (per frequency, complex128)" if args.plain else "batched",
-                   "l2": "inputs larger than L2 (matrix alone 260 MB)",
-                   "parallelism": f"replica x{world}"},
+        "config": bench_config(s.ne, s.nc),
+        "solver": {**solver_label(args, p, sv.freqs), "colours": s.n_colours,
+                   "parallelism": f"frequency groups x{world} (round-robin, one gradient SUM)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain": plain,
+        "batched_over_plain": value / plain["value"] if plain else None,
         "roofline": {"bound": "hbm", "kernel": dom, "launches": "K=16" if src is b16 else "all",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "achieved_all_widths": achieved_all},
         "kernel_classes": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                "GB/s": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9, 1) if v["ms"] else None,
+                               "frac_of_peak": round(v["bytes"] / (v["ms"] * 1e-3) / 1e9 / peak, 3)
+                               if v["ms"] else None,
                                "by_batch_width": {kk: {"ms": round(b["ms"], 1),
                                                        "GB/s": round(b["bytes"] / (b["ms"] * 1e-3) / 1e9, 1)
                                                        if b["ms"] and b["bytes"] else None}
                                                   for kk, b in v["by_k"].items()}}
                            for k, v in kt.items()},
-        "krylov_iterations_per_step": statistics.mean(iters),
-        "solver_stats_last_step": solver_stats,
-        "gpu_launches": launches,
-        "clocks": clk,
+        "krylov_iterations_per_step": statistics.mean(r["iters"]),
+        "solver_stats_last_step": r["stats"],
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
         "cpu_baseline": cb,
     }
     print(json.dumps(line), flush=True)
 
 
 def main():
+    global CONFIG
     args = parse()
+    CONFIG = args.config
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -140,6 +140,11 @@ typedef struct m3d_params {
                                  0 (default): restart per FP64 refinement, measured faster on C2 */
     int gradcorr_overlap;     /* 1: the V-cycles of the gradient-space term run on a second CUDA stream,
                                  overlapping the forward SSOR sweep (same arithmetic); 0: one stream */
+    int krylov;               /* inner solve of the mixed-precision path: 0 BiCGStab (default), 1 flexible
+                                 GMRES (restart fgmres_m) with the SSOR / gradient-space preconditioner */
+    int fgmres_m;             /* FGMRES restart length (20) */
+    int learned_period;       /* with krylov = 1 and a trained network (m3d_learn_*): every learned_period-th
+                                 FGMRES direction comes from the network instead of SSOR (0: never; 2) */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -315,20 +320,113 @@ int m3d_timer_start(m3d_solver* s);
 int m3d_timer_stop(m3d_solver* s, double* ms);
 
 /* Kernel classes: 0 SpMV, 1 SSOR apply (all colour sweeps), 2 Krylov vector
- * updates, 3 divergence correction, 4 gradient-space term of the preconditioner.  bytes = algorithmic bytes
- * (matrix entries, diagonals and vector streams each counted once). */
+ * updates, 3 divergence correction (one interval per call, its bytes counted
+ * from the call's PCG sweeps), 4 gradient-space term of the preconditioner,
+ * 5 J^T r sensitivity.  bytes = algorithmic bytes (matrix entries, diagonals
+ * and vector streams each counted once). */
 typedef struct m3d_kernel_times {
-    long long launches[5];
-    double ms[5];
-    double bytes[5];
+    long long launches[6];
+    double ms[6];
+    double bytes[6];
     /* the same split by batch width: [class][K = 2, 4, 8, 16, other] */
-    long long launches_k[5][5];
-    double ms_k[5][5];
-    double bytes_k[5][5];
+    long long launches_k[6][5];
+    double ms_k[6][5];
+    double bytes_k[6][5];
 } m3d_kernel_times;
 
 int m3d_set_kernel_timing(m3d_solver* s, int on);   /* also resets the totals */
 int m3d_get_kernel_times(m3d_solver* s, m3d_kernel_times* out);
+
+/* ---------------------------------------------------------------------- */
+/* Autotuner (no counterpart in the reference, which runs one serial      */
+/* solve): row-kernel layout and right-hand-side block size of the        */
+/* batched FP32 inner solve, measured on this mesh and GPU.               */
+/* ---------------------------------------------------------------------- */
+
+typedef struct m3d_tune_entry {
+    int row_kernels;          /* 0 CSR rows read by the lanes, 1 slice-staged rows */
+    int K;                    /* right-hand sides per batch (2, 4, 8, 16) */
+    double ms_per_iter;       /* one FP32 BiCGStab iteration of the batch */
+    double ms_per_rhs_iter;   /* the same per right-hand side */
+} m3d_tune_entry;
+
+/* Times `reps` FP32 inner-solve iterations at frequency freq for both
+ * layouts and K = 2 .. max_K (at most 8 entries into table, *n_entries set),
+ * then applies the layout fastest at max_K (m3d_params.row_kernels) and the
+ * K with the least time per right-hand side as the batch of
+ * m3d_solve_rhs_batch (*row_kernels, *rhs_block report them).  Results are
+ * cached per (edges, stiffness entries, max_K, gradient-space term) for the
+ * process: a repeated call applies the cached choice without timing
+ * (*cached = 1) unless force != 0.  Drops the factorisation and the resident
+ * fields; call after m3d_set_sigma, before the solves. */
+int m3d_autotune(m3d_solver* s, double freq, int max_K, int reps, int force, m3d_tune_entry* table,
+                 int* n_entries, int* row_kernels, int* rhs_block, int* cached);
+
+/* ---------------------------------------------------------------------- */
+/* Learned preconditioner network (no counterpart in the reference, whose */
+/* solve has no learned part): a 3-D convolutional network, 3x3x3 kernels, */
+/* ReLU between layers, BF16 weights and activations with FP32            */
+/* accumulation on the tcgen05 tensor cores.  These entry points take     */
+/* host arrays, for checking the kernels; the solver drives the same      */
+/* network on device data (m3d_learn_*).                                  */
+/* ---------------------------------------------------------------------- */
+
+typedef struct m3d_cnn m3d_cnn;
+
+/* layers >= 2; c_in, hidden, c_out in 1..32; He-initialised from seed. */
+int m3d_cnn_create(int device, int layers, int c_in, int hidden, int c_out, unsigned seed, m3d_cnn** out);
+void m3d_cnn_destroy(m3d_cnn* c);
+const char* m3d_cnn_last_error(const m3d_cnn* c);
+/* w [layers][27][32 c_out][32 c_in] (zero-padded), b [layers][32], FP32;
+ * tap t = (dz + 1) 9 + (dy + 1) 3 + (dx + 1) */
+int m3d_cnn_get_weights(m3d_cnn* c, float* w, float* b);
+int m3d_cnn_set_weights(m3d_cnn* c, const float* w, const float* b);
+/* x [n][D][H][W][c_in] -> y [n][D][H][W][c_out]; W in {32, 64, 128}, H a
+ * multiple of 128 / W; zero padding at the grid boundary */
+int m3d_cnn_forward(m3d_cnn* c, const float* x, int n, int D, int H, int W, float* y);
+/* gradients of sum(dy * network(x)): dw, db as in get_weights, dx like x
+ * (may be null) */
+int m3d_cnn_backward(m3d_cnn* c, const float* x, const float* dy, int n, int D, int H, int W, float* dw, float* db,
+                     float* dx);
+/* one Adam step on 0.5 mean |network(x) - target|^2 (mean over voxels and
+ * samples, summed over channels); the loss before the step into *loss */
+int m3d_cnn_train_step(m3d_cnn* c, const float* x, const float* target, int n, int D, int H, int W, float lr,
+                       double* loss);
+
+/* The network as the solver's learned preconditioner.  A dense grid of
+ * (2^grid_level)^3 cells over the mesh's unit cube carries each right-hand
+ * side's field to the network (per cell and direction means, unit RMS, plus
+ * conductivity and frequency channels) and the network's output back to the
+ * edges.  Training pairs are recorded from the plain FP64 SSOR-BiCGStab
+ * forward solves of m3d_learn_collect (residual r_k -> error x* - x_k, at
+ * every poll of the solve).  With m3d_params.krylov = 1 the mixed-precision
+ * solve runs flexible GMRES and, once m3d_learn_train has run, takes every
+ * learned_period-th direction from the network: the network's coarse
+ * correction c (scaled per right-hand side by least squares) followed by one
+ * SSOR / gradient-space application to the rest, z = a c + B (v - a A c).
+ * The FP64 true residual remains the stopping test. */
+int m3d_learn_setup(m3d_solver* s, int grid_level, int layers, int hidden, unsigned seed, long long max_samples);
+/* the inner solve between calls: m3d_params.krylov, fgmres_m, learned_period */
+int m3d_set_krylov(m3d_solver* s, int krylov, int fgmres_m, int learned_period);
+/* plain FP64 forward solves of freqs at the current conductivity, recording
+ * pairs until max_samples are held; *n_samples = pairs held */
+int m3d_learn_collect(m3d_solver* s, const double* freqs, int nf, long long* n_samples);
+/* Adam (learning rate lr, minibatch <= 16) over the first (1 - val_frac) of
+ * the pairs; mean loss per epoch into epoch_loss[epochs] (may be null), the
+ * held-out pairs' loss into *val_loss (may be null) */
+int m3d_learn_train(m3d_solver* s, int epochs, float lr, int batch, unsigned seed, double val_frac,
+                    double* epoch_loss, double* val_loss);
+
+/* ---------------------------------------------------------------------- */
+/* Test hook (no counterpart in the reference).                           */
+/* ---------------------------------------------------------------------- */
+
+/* on != 0: every slice-staged kernel of this solver polls its copy barrier
+ * once without blocking and takes its timeout path when the copy has not
+ * landed (the block skips its slices and waits, bounded, for the copy in
+ * flight); the next solve then fails with M3D_ERR_CUDA.  on = 0 restores
+ * the bounded waits.  For testing the error path only. */
+int m3d_test_set_consume_no_wait(m3d_solver* s, int on);
 
 #ifdef __cplusplus
 }

@@ -34,6 +34,9 @@ class Params(C.Structure):
         ("inner_tol_floor", C.c_double),
         ("residual_replacement", C.c_int),
         ("gradcorr_overlap", C.c_int),
+        ("krylov", C.c_int),
+        ("fgmres_m", C.c_int),
+        ("learned_period", C.c_int),
     ]
 
 
@@ -62,13 +65,19 @@ class Stats(C.Structure):
 class KernelTimes(C.Structure):
     """struct m3d_kernel_times."""
     _fields_ = [
-        ("launches", C.c_longlong * 5),
-        ("ms", C.c_double * 5),
-        ("bytes", C.c_double * 5),
-        ("launches_k", (C.c_longlong * 5) * 5),
-        ("ms_k", (C.c_double * 5) * 5),
-        ("bytes_k", (C.c_double * 5) * 5),
+        ("launches", C.c_longlong * 6),
+        ("ms", C.c_double * 6),
+        ("bytes", C.c_double * 6),
+        ("launches_k", (C.c_longlong * 5) * 6),
+        ("ms_k", (C.c_double * 5) * 6),
+        ("bytes_k", (C.c_double * 5) * 6),
     ]
+
+
+class TuneEntry(C.Structure):
+    """struct m3d_tune_entry."""
+    _fields_ = [("row_kernels", C.c_int), ("K", C.c_int), ("ms_per_iter", C.c_double),
+                ("ms_per_rhs_iter", C.c_double)]
 
 
 class RegParams(C.Structure):
@@ -79,7 +88,7 @@ class RegParams(C.Structure):
     ]
 
 
-KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "gradcorr")
+KERNEL_CLASSES = ("spmv", "ssor", "vector", "divcorr", "gradcorr", "sensitivity")
 
 SOLVER_SYMBOLS = [
     "m3d_params_default", "m3d_solver_create", "m3d_solver_destroy", "m3d_last_error",
@@ -91,6 +100,10 @@ SOLVER_SYMBOLS = [
     "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_solve_rhs_batch", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
     "m3d_reg_apply_wtw", "m3d_reg_apply_cmcmt", "m3d_reg_diagonal_wtw", "m3d_reg_evaluate", "m3d_dot_batched", "m3d_dot_batched_noalloc", "m3d_get_stats",
     "m3d_timer_start", "m3d_timer_stop", "m3d_set_kernel_timing", "m3d_get_kernel_times",
+    "m3d_test_set_consume_no_wait", "m3d_autotune",
+    "m3d_cnn_create", "m3d_cnn_destroy", "m3d_cnn_last_error", "m3d_cnn_get_weights", "m3d_cnn_set_weights",
+    "m3d_cnn_forward", "m3d_cnn_backward", "m3d_cnn_train_step",
+    "m3d_learn_setup", "m3d_learn_collect", "m3d_learn_train", "m3d_set_krylov",
 ]
 
 
@@ -136,3 +149,21 @@ def declare(lib) -> None:
     _fn(lib, "m3d_timer_stop", C.c_int, [vp, c_double_p])
     _fn(lib, "m3d_set_kernel_timing", C.c_int, [vp, C.c_int])
     _fn(lib, "m3d_get_kernel_times", C.c_int, [vp, C.POINTER(KernelTimes)])
+    _fn(lib, "m3d_test_set_consume_no_wait", C.c_int, [vp, C.c_int])
+    fp = C.POINTER(C.c_float)
+    _fn(lib, "m3d_cnn_create", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint, C.POINTER(vp)])
+    _fn(lib, "m3d_cnn_destroy", None, [vp])
+    _fn(lib, "m3d_cnn_last_error", C.c_char_p, [vp])
+    _fn(lib, "m3d_cnn_get_weights", C.c_int, [vp, fp, fp])
+    _fn(lib, "m3d_cnn_set_weights", C.c_int, [vp, fp, fp])
+    _fn(lib, "m3d_cnn_forward", C.c_int, [vp, fp, C.c_int, C.c_int, C.c_int, C.c_int, fp])
+    _fn(lib, "m3d_cnn_backward", C.c_int, [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_int, fp, fp, fp])
+    _fn(lib, "m3d_cnn_train_step", C.c_int, [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float,
+                                             C.POINTER(C.c_double)])
+    _fn(lib, "m3d_set_krylov", C.c_int, [vp, C.c_int, C.c_int, C.c_int])
+    _fn(lib, "m3d_learn_setup", C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_uint, C.c_longlong])
+    _fn(lib, "m3d_learn_collect", C.c_int, [vp, c_double_p, C.c_int, C.POINTER(C.c_longlong)])
+    _fn(lib, "m3d_learn_train", C.c_int, [vp, C.c_int, C.c_float, C.c_int, C.c_uint, C.c_double, c_double_p,
+                                          c_double_p])
+    _fn(lib, "m3d_autotune", C.c_int, [vp, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(TuneEntry), c_int_p,
+                                       c_int_p, c_int_p, c_int_p])

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SRCS = ["host/octree_build.cpp", "host/mesh_capi.cpp", "host/layout.cpp", "host/layout_capi.cpp", "host/amg.cpp",
              "host/regularization.cpp"]
 CUDA_SRCS = ["cuda/krylov.cu", "cuda/physics.cu", "cuda/gradcorr.cu", "cuda/regularization.cu", "cuda/dot.cu",
-             "solver.cu", "capi.cu", "noalloc.cu"]
+             "cuda/learned.cu", "solver.cu", "learned_solver.cu", "capi.cu", "noalloc.cu", "learned_capi.cu"]
 
 
 def _nvcc() -> str:

@@ -7,7 +7,11 @@
 #include <algorithm>
 #include <new>
 #include <stdexcept>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "m3d_gb300.h"
 #include "solver.hpp"
@@ -47,6 +51,17 @@ int guarded(m3d_solver* h, F&& f) {
 
 bool ready(const m3d_solver* h) { return h && h->s && h->s->ready; }
 
+// Inputs that enter a solve are checked on the host: a NaN or Inf in a
+// right-hand side, field or data vector fails the call with M3D_ERR_NUMERIC
+// before anything is launched (the reference would iterate on it to maxiter).
+bool all_finite(const double* v, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+size_t edge_doubles(const m3d_solver* h) { return 2 * (size_t)h->s->n_edges(); }
+
 }  // namespace
 
 namespace m3d {
@@ -82,6 +97,9 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->inner_tol_floor = 3e-5;
     p->residual_replacement = 0;
     p->gradcorr_overlap = 1;
+    p->krylov = 0;
+    p->fgmres_m = 20;
+    p->learned_period = 2;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -118,9 +136,20 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
         !(params->gradcorr_fmax >= 0.0) || params->gradcorr_presmooth < 0 || params->gradcorr_presmooth > 1 ||
         params->divcorr_mixed < 0 || params->divcorr_mixed > 1 || !(params->inner_tol_floor > 0.0) ||
         params->inner_tol_floor >= 1.0 || params->residual_replacement < 0 || params->residual_replacement > 1 ||
-        params->gradcorr_overlap < 0 || params->gradcorr_overlap > 1)
+        params->gradcorr_overlap < 0 || params->gradcorr_overlap > 1 || params->krylov < 0 ||
+        params->krylov > 1 || params->fgmres_m < 2 || params->fgmres_m > 47 || params->learned_period < 0)
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
+}
+
+extern "C" int m3d_set_krylov(m3d_solver* h, int krylov, int fgmres_m, int learned_period) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (krylov < 0 || krylov > 1 || fgmres_m < 2 || fgmres_m > 47 || learned_period < 0)
+        return fail(h, M3D_ERR_ARG, "invalid Krylov settings");
+    h->s->P.krylov = krylov;
+    h->s->P.fgmres_m = fgmres_m;
+    h->s->P.learned_period = learned_period;
+    return M3D_OK;
 }
 
 extern "C" int m3d_solver_sizes(const m3d_solver* h, int* ne, int* nc, int* nn, int* ncol) {
@@ -185,48 +214,60 @@ extern "C" int m3d_background_E(m3d_solver* h, int pol, double* E_out) {
 extern "C" int m3d_set_background_fields(m3d_solver* h, const double* E1, const double* E2) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!E1 || !E2) return fail(h, M3D_ERR_ARG, "null field");
+    if (!all_finite(E1, edge_doubles(h)) || !all_finite(E2, edge_doubles(h)))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in a background field");
     return guarded(h, [&](m3d::GpuSolver& s) { s.set_background(E1, E2); });
 }
 
 extern "C" int m3d_build_adjoint_rhs(m3d_solver* h, const double* wr, double* rhs1, double* rhs2) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!wr || !rhs1 || !rhs2) return fail(h, M3D_ERR_ARG, "null buffer");
+    if (!all_finite(wr, 8 * (size_t)h->s->n_stations()))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in the weighted residual");
     return guarded(h, [&](m3d::GpuSolver& s) { s.build_adjoint_rhs(wr, rhs1, rhs2); });
 }
 
 extern "C" int m3d_adjoint_solve(m3d_solver* h, const double* rhs, double* lambda) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!rhs || !lambda) return fail(h, M3D_ERR_ARG, "null buffer");
+    if (!all_finite(rhs, edge_doubles(h))) return fail(h, M3D_ERR_NUMERIC, "non-finite value in the right-hand side");
     return guarded(h, [&](m3d::GpuSolver& s) { s.adjoint_solve(rhs, lambda, false); });
 }
 
 extern "C" int m3d_solve_rhs_batch(m3d_solver* h, const double* rhs, int n_rhs, double* out) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!rhs || !out || n_rhs < 1) return fail(h, M3D_ERR_ARG, "null buffer or no right-hand side");
+    if (!all_finite(rhs, edge_doubles(h) * (size_t)n_rhs))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in a right-hand side");
     return guarded(h, [&](m3d::GpuSolver& s) { s.solve_rhs_batch(rhs, n_rhs, out); });
 }
 
 extern "C" int m3d_solve_rhs(m3d_solver* h, const double* rhs, double* x) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!rhs || !x) return fail(h, M3D_ERR_ARG, "null buffer");
+    if (!all_finite(rhs, edge_doubles(h))) return fail(h, M3D_ERR_NUMERIC, "non-finite value in the right-hand side");
     return guarded(h, [&](m3d::GpuSolver& s) { s.adjoint_solve(rhs, x, true); });
 }
 
 extern "C" int m3d_compute_sensitivity(m3d_solver* h, const double* E, const double* lambda, double* g) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!E || !lambda || !g) return fail(h, M3D_ERR_ARG, "null buffer");
+    if (!all_finite(E, edge_doubles(h)) || !all_finite(lambda, edge_doubles(h)))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in a field");
     return guarded(h, [&](m3d::GpuSolver& s) { s.sensitivity(E, lambda, g); });
 }
 
 extern "C" int m3d_build_perturbation_rhs(m3d_solver* h, int pol, const double* dsig, double* rhs) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if ((pol != 1 && pol != 2) || !dsig || !rhs) return fail(h, M3D_ERR_ARG, "pol must be 1 or 2");
+    if (!all_finite(dsig, (size_t)h->s->n_cells())) return fail(h, M3D_ERR_NUMERIC, "non-finite value in dsigma");
     return guarded(h, [&](m3d::GpuSolver& s) { s.perturbation_rhs(pol, dsig, rhs); });
 }
 
 extern "C" int m3d_extract_delta_impedance(m3d_solver* h, const double* dE, int pol, double* dZ) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if ((pol != 1 && pol != 2) || !dE || !dZ) return fail(h, M3D_ERR_ARG, "pol must be 1 or 2");
+    if (!all_finite(dE, edge_doubles(h))) return fail(h, M3D_ERR_NUMERIC, "non-finite value in dE");
     return guarded(h, [&](m3d::GpuSolver& s) { s.delta_impedance(dE, pol, dZ); });
 }
 
@@ -293,6 +334,8 @@ extern "C" int m3d_jtjv_batch(m3d_solver* h, const double* freqs, int nf, const 
     if (nf > 8) return fail(h, M3D_ERR_ARG, "at most 8 frequencies per call");
     if (!(inner_tol > 0.0) || inner_tol >= 1.0) return fail(h, M3D_ERR_ARG, "inner_tol must be in (0, 1)");
     for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    if (!all_finite(dsigma, (size_t)h->s->n_cells()) || !all_finite(obs_err, 4 * (size_t)h->s->n_stations() * nf))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in dsigma or the data errors");
     return guarded(h, [&](m3d::GpuSolver& s) { s.jtjv_batch(freqs, nf, dsigma, obs_err, inner_tol, out); });
 }
 
@@ -301,6 +344,9 @@ extern "C" int m3d_gradient_batch(m3d_solver* h, const double* freqs, int nf, co
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!freqs || nf < 1 || !obs_Z || !obs_err || !grad) return fail(h, M3D_ERR_ARG, "null buffer");
     for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    const size_t nd = 4 * (size_t)h->s->n_stations() * nf;
+    if (!all_finite(obs_Z, 2 * nd) || !all_finite(obs_err, nd))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in the observed data or errors");
     return guarded(h, [&](m3d::GpuSolver& s) { s.gradient_batch(freqs, nf, obs_Z, obs_err, Z_out, grad); });
 }
 
@@ -338,12 +384,96 @@ extern "C" int m3d_set_kernel_timing(m3d_solver* h, int on) {
     return guarded(h, [&](m3d::GpuSolver& s) { s.timer.reset(); s.timer.on = on != 0; });
 }
 
+namespace {
+struct TuneKey {
+    int ne;
+    long long nnz;
+    int max_K, gradcorr, device;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(ne, nnz, max_K, gradcorr, device) < std::tie(o.ne, o.nnz, o.max_K, o.gradcorr, o.device);
+    }
+};
+struct TuneChoice {
+    std::vector<m3d::TuneEntry> table;
+    int row_kernels, rhs_block;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+}  // namespace
+
+extern "C" int m3d_autotune(m3d_solver* h, double freq, int max_K, int reps, int force, m3d_tune_entry* table,
+                            int* n_entries, int* row_kernels, int* rhs_block, int* cached) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!(freq > 0) || max_K < 2 || max_K > 16 || reps < 1) return fail(h, M3D_ERR_ARG, "invalid tuning arguments");
+    return guarded(h, [&](m3d::GpuSolver& s) {
+        const TuneKey key{s.n_edges(), s.nnz_off, max_K, s.P.gradcorr, s.device};
+        TuneChoice ch;
+        bool hit = false;
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            if (it != g_tune_cache.end() && !force) { ch = it->second; hit = true; }
+        }
+        if (hit) {
+            s.P.row_kernels = ch.row_kernels;
+            s.rhs_block = ch.rhs_block;
+        } else {
+            ch.table = s.autotune(freq, max_K, reps);
+            ch.row_kernels = s.P.row_kernels;
+            ch.rhs_block = s.rhs_block;
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            g_tune_cache[key] = ch;
+        }
+        const int n = std::min<int>((int)ch.table.size(), 8);
+        for (int i = 0; i < n && table; ++i)
+            table[i] = m3d_tune_entry{ch.table[i].row_kernels, ch.table[i].K, ch.table[i].ms_per_iter,
+                                      ch.table[i].ms_per_rhs_iter};
+        if (n_entries) *n_entries = n;
+        if (row_kernels) *row_kernels = ch.row_kernels;
+        if (rhs_block) *rhs_block = ch.rhs_block;
+        if (cached) *cached = hit ? 1 : 0;
+    });
+}
+
+extern "C" int m3d_learn_setup(m3d_solver* h, int grid_level, int layers, int hidden, unsigned seed,
+                               long long max_samples) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (layers < 2 || hidden < 1 || hidden > 32 || max_samples < 1) return fail(h, M3D_ERR_ARG, "invalid network");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.learn_setup(grid_level, layers, hidden, seed, (long)max_samples); });
+}
+
+extern "C" int m3d_learn_collect(m3d_solver* h, const double* freqs, int nf, long long* n_samples) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (!freqs || nf < 1) return fail(h, M3D_ERR_ARG, "need frequencies");
+    for (int f = 0; f < nf; ++f) if (!(freqs[f] > 0)) return fail(h, M3D_ERR_ARG, "frequencies must be > 0");
+    return guarded(h, [&](m3d::GpuSolver& s) {
+        const long n = s.learn_collect(freqs, nf);
+        if (n_samples) *n_samples = n;
+    });
+}
+
+extern "C" int m3d_learn_train(m3d_solver* h, int epochs, float lr, int batch, unsigned seed, double val_frac,
+                               double* epoch_loss, double* val_loss) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (epochs < 1 || !(lr > 0.0f) || batch < 1 || val_frac < 0.0 || val_frac >= 1.0)
+        return fail(h, M3D_ERR_ARG, "invalid training arguments");
+    return guarded(h, [&](m3d::GpuSolver& s) {
+        const std::vector<double> hist = s.learn_train(epochs, lr, batch, seed, val_frac, val_loss);
+        if (epoch_loss) std::copy(hist.begin(), hist.end(), epoch_loss);
+    });
+}
+
+extern "C" int m3d_test_set_consume_no_wait(m3d_solver* h, int on) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.set_test_consume_no_wait(on != 0); });
+}
+
 extern "C" int m3d_get_kernel_times(m3d_solver* h, m3d_kernel_times* out) {
     if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
     if (!out) return fail(h, M3D_ERR_ARG, "null output");
     return guarded(h, [&](m3d::GpuSolver& s) {
         s.timer.collect();
-        for (int i = 0; i < 5; ++i) {
+        for (int i = 0; i < m3d::kNumCls; ++i) {
             out->launches[i] = s.timer.launches[i];
             out->ms[i] = s.timer.ms[i];
             out->bytes[i] = s.timer.bytes[i];

@@ -61,6 +61,11 @@ void KernelTimer::end(int h, cudaStream_t s) {
     cudaEventRecord(open[h].b, s ? s : stream);
 }
 
+void KernelTimer::set_bytes(int h, double algorithmic_bytes) {
+    if (h < 0) return;
+    open[h].bytes = algorithmic_bytes;
+}
+
 void KernelTimer::collect() {
     if (open.empty()) return;
     cudaStreamSynchronize(stream);
@@ -1204,6 +1209,22 @@ void ssor_apply(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* o
 #undef CALL
 }
 
+// out = B in: the SSOR apply plus, when the context carries it, the
+// gradient-space term (V-cycle on the side stream, added by the backward
+// sweep) -- the right preconditioner of one half iteration of iteration_k.
+template <class R>
+void precond_apply(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out) {
+#define CALL(K)                                  \
+    {                                            \
+        GcRowTerm gt;                            \
+        if (c.gc) gt = gc_row_term(*c.gc, c.B);  \
+        gc_term<R, K>(c, in);                    \
+        ssor_k<R, K>(c, in, y, out, gt);         \
+    }
+    M3D_DISPATCH_K(c.B.K, CALL)
+#undef CALL
+}
+
 template <class R>
 void bicg_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st) {
     spmv(c, kSpmvInit, v.x, v.r, v.b, v.r0, st);
@@ -1242,6 +1263,7 @@ template void spmv<double>(const KrylovCtx<double>&, int, const double2*, double
 template void spmv<float>(const KrylovCtx<float>&, int, const float2*, float2*, const float2*, float2*, BicgState*);
 template void ssor_apply<double>(const KrylovCtx<double>&, const double2*, double2*, double2*);
 template void ssor_apply<float>(const KrylovCtx<float>&, const float2*, float2*, float2*);
+template void precond_apply<float>(const KrylovCtx<float>&, const float2*, float2*, float2*);
 template void bicg_init<double>(const KrylovCtx<double>&, const KrylovVecs<double>&, BicgState*);
 template void bicg_init<float>(const KrylovCtx<float>&, const KrylovVecs<float>&, BicgState*);
 template void bicg_iteration<double>(const KrylovCtx<double>&, const KrylovVecs<double>&, BicgState*);

@@ -92,16 +92,18 @@ __device__ __forceinline__ float2 gc_grad_row(const GcRowTerm& t, const float2* 
 }
 
 // Optional CUDA-event timing of kernel classes on the solver's stream.
-enum KernelClass : int { kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsGradcorr = 4, kNumCls = 5 };
+enum KernelClass : int {
+    kClsSpmv = 0, kClsSsor = 1, kClsVec = 2, kClsDivcorr = 3, kClsGradcorr = 4, kClsSens = 5, kNumCls = 6
+};
 struct KernelTimer {
     bool on = false;
     cudaStream_t stream = nullptr;
     std::vector<cudaEvent_t> pool;
     struct Pair { int cls; int kb; cudaEvent_t a, b; double bytes; };
     std::vector<Pair> open;
-    long long launches[kNumCls] = {0, 0, 0, 0, 0};
-    double ms[kNumCls] = {0, 0, 0, 0, 0};
-    double bytes[kNumCls] = {0, 0, 0, 0, 0};
+    long long launches[kNumCls] = {};
+    double ms[kNumCls] = {};
+    double bytes[kNumCls] = {};
     static constexpr int kNumKBins = 5;   // K = 2, 4, 8, 16, other
     long long launches_k[kNumCls][kNumKBins] = {};
     double ms_k[kNumCls][kNumKBins] = {};
@@ -111,6 +113,9 @@ struct KernelTimer {
     // stream that the timer's stream joins before collect()
     int begin(int cls, double algorithmic_bytes, int K = 0, cudaStream_t s = nullptr);   // handle or -1
     void end(int handle, cudaStream_t s = nullptr);
+    // algorithmic bytes of an interval whose work is only known after its
+    // launches were issued (the PCG sweeps of a divergence correction)
+    void set_bytes(int handle, double algorithmic_bytes);
     void collect();   // synchronises and folds finished pairs into the totals
     void reset();
     ~KernelTimer();
@@ -176,6 +181,9 @@ void spmv(const KrylovCtx<R>& c, int mode, const dev::cplx<R>* x, dev::cplx<R>* 
           const dev::cplx<R>* aux, dev::cplx<R>* aux_out, BicgState* st);
 template <class R>
 void ssor_apply(const KrylovCtx<R>& c, const dev::cplx<R>* in, dev::cplx<R>* y, dev::cplx<R>* out);
+// SSOR apply plus the gradient-space term of c (if attached): out = B in
+template <class R>
+void precond_apply(const KrylovCtx<R>& c, const dev::cplx<R>* in, dev::cplx<R>* y, dev::cplx<R>* out);
 template <class R>
 void bicg_init(const KrylovCtx<R>& c, const KrylovVecs<R>& v, BicgState* st);
 template <class R>

@@ -30,6 +30,11 @@ namespace dev {
 constexpr int kSegHeader = 64;                  // bytes of the row-end table
 constexpr long long kWaitCycles = 4000000000LL;  // bound of every barrier wait (~2 s)
 constexpr unsigned kErrCopyTimeout = 1u;
+// Test hook, set by the host in the same flag word: with this bit set, the
+// consume wait of every staged kernel polls its barrier once without
+// blocking and takes the timeout path if the copy has not landed; the drain
+// wait for a copy in flight keeps its full bound.
+constexpr unsigned kTestConsumeNoWait = 1u << 31;
 
 template <class R>
 struct SegView {
@@ -79,6 +84,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Non-blocking test of phase `parity` of `bar`.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(smem_addr(bar)), "r"(parity)
@@ -140,20 +158,23 @@ template <int K> struct StagedShape {
 // blockIdx.x + gridDim.x, ... < n_items; item i's lower (PARTS & 1) and upper
 // (PARTS & 2) segments are bulk-copied into stage k & 1 one item ahead of
 // use, so the next slice's matrix stream is in flight while body() runs.
-// Every wait is bounded: on a timeout the block sets kErrCopyTimeout in *err,
-// skips the stage, waits (bounded) for its copy in flight and stops.
+// Every thread waits (bounded) on the stage's barrier itself; the one block
+// barrier per item also ORs the threads' outcomes, so the whole block takes
+// the same branch: on a timeout it sets kErrCopyTimeout in *err, skips the
+// stage, waits (bounded) for the late copy and stops.  The call's results
+// are then invalid and the host reports the error.
 template <int PARTS, class Body>
 __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__ seg, const int4* __restrict__ work,
                                                long n_items, int stage_bytes, unsigned* err, Body body) {
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int4 wk[2];
-    __shared__ int abort_flag;
+    __shared__ int no_wait;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_mbar_init();
-        abort_flag = 0;
+        no_wait = (*reinterpret_cast<volatile unsigned*>(err) & kTestConsumeNoWait) != 0;
     }
     __syncthreads();
     auto issue = [&](long i, int stg) {   // thread 0 only
@@ -171,30 +192,38 @@ __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__
         }
         if (PARTS & 2) bulk_g2s(dst, seg + (size_t)it.up_off * 16, (unsigned)it.up_len * 16u, &bar[stg]);
     };
+    auto wait_stage = [&](int stg, unsigned parity) {
+        return no_wait ? mbar_test_wait(&bar[stg], parity) : mbar_wait_bounded(&bar[stg], parity);
+    };
     long i = blockIdx.x;
-    if (threadIdx.x == 0 && i < n_items) issue(i, 0);
-    for (int k = 0; i < n_items; i += gridDim.x, ++k) {
+    if (i >= n_items) return;   // uniform: the whole block has no item
+    if (threadIdx.x == 0) issue(i, 0);
+    // outcome of the wait for the item about to be consumed, block-uniform
+    bool fail = __syncthreads_or(!wait_stage(0, 0u)) != 0;
+    int k = 0;
+    for (;;) {
         const int stg = k & 1;
-        if (threadIdx.x == 0 && i + gridDim.x < n_items) {
-            fence_proxy_async_smem();
-            issue(i + gridDim.x, stg ^ 1);
-        }
-        const bool ok = mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
-        if (ok) {
-            body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
-        } else {
-            atomicOr(err, kErrCopyTimeout);
-            abort_flag = 1;
-        }
-        __syncthreads();
-        if (abort_flag) {
-            // never consume a stage that did not arrive; let the copy already
-            // issued for the next item land (bounded) before the block leaves
-            if (threadIdx.x == 0 && i + gridDim.x < n_items)
-                mbar_wait_bounded(&bar[stg ^ 1], (unsigned)((k + 1) >> 1) & 1u);
+        if (fail) {
+            // never consume a stage that did not arrive; let the late copy
+            // land (bounded) before the block leaves
+            if (threadIdx.x == 0) {
+                atomicOr(err, kErrCopyTimeout);
+                mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
+            }
             __syncthreads();
-            break;
+            return;
         }
+        const long next = i + gridDim.x;
+        if (threadIdx.x == 0 && next < n_items) {
+            fence_proxy_async_smem();
+            issue(next, stg ^ 1);
+        }
+        body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
+        if (next >= n_items) break;
+        // wait for the next item's stage; the same barrier ends this item
+        fail = __syncthreads_or(!wait_stage(stg ^ 1, (unsigned)((k + 1) >> 1) & 1u)) != 0;
+        i = next;
+        ++k;
     }
 }
 

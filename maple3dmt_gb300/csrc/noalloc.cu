@@ -12,11 +12,14 @@
 //
 // How: the reduction scratch is a file-scope device array of fixed size,
 // K <= 16 right-hand sides x 1024 blocks of partial sums (256 KiB per
-// device).  Its address is looked up once per device with
-// cudaGetSymbolAddress while that device is current.  That first call per
-// device does the set-up (the runtime may load the module there), so make it
-// before any latency-critical region.  Larger K is rejected with
-// M3D_ERR_TOO_LARGE; n is unlimited (the kernel strides over the grid).
+// device).  Its address is looked up once per device context with
+// cudaGetSymbolAddress while that device is current, and cached together with
+// the context's id (cuCtxGetId).  The first call on a device, and the first
+// call after that device's context was replaced (cudaDeviceReset, or a new
+// primary context), does this set-up (the runtime may load the module there),
+// so make it before any latency-critical region and before any stream
+// capture.  Larger K is rejected with M3D_ERR_TOO_LARGE; n is unlimited (the
+// kernel strides over the grid).
 //
 // The only scratch state that must start at zero is the arrival counter of
 // the grid reduction; each call clears it on the caller's stream before the
@@ -27,6 +30,7 @@
 // overlap: two calls in flight at once (different streams, or host threads
 // without a lock) race on the partial sums and the counter and give wrong
 // results.  Issue them on one stream, or serialise them.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -50,9 +54,41 @@ static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 constexpr int kMaxDevices = 64;
 std::mutex g_addr_mu;
 NoAllocScratch* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 
-// Device address of this device's scratch; looked up on the first call per
-// device with that device current.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Id of the calling thread's current context (unique for the life of the
+// process), or 0 when it cannot be read.  The driver functions are reached
+// through the runtime's entry-point query, so the library needs no -lcuda.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1{}, q2{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+        cudaGetLastError();
+        looked_up = true;
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of this device's scratch; looked up with that device
+// current on the first call, and again whenever the device's context differs
+// from the one the cached address belongs to.
 int scratch_of_current_device(NoAllocScratch** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) {
@@ -61,13 +97,16 @@ int scratch_of_current_device(NoAllocScratch** out) {
     }
     if (dev < 0 || dev >= kMaxDevices) return M3D_ERR_TOO_LARGE;
     std::lock_guard<std::mutex> lock(g_addr_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_addr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
             cudaGetLastError();
             return M3D_ERR_CUDA;
         }
         g_addr[dev] = static_cast<NoAllocScratch*>(p);
+        // the lookup made the context current if it was not yet
+        g_ctx_id[dev] = current_context_id();
     }
     *out = g_addr[dev];
     return M3D_OK;

@@ -202,6 +202,7 @@ GpuSolver::~GpuSolver() {
 
 void GpuSolver::free_all() {
     if (stream) cudaStreamSynchronize(stream);
+    learn_free();
     dfree(md.perm); dfree(md.iperm); dfree(md.flags); dfree(md.dir); dfree(md.ez); dfree(md.s_diag);
     dfree(md.me_geom); dfree(md.adual); dfree(md.elen); dfree(md.nadj); dfree(md.adj_ptr); dfree(md.adj_cell);
     dfree(md.lift_ptr); dfree(md.lift_col); dfree(md.lift_val); dfree(md.hp);
@@ -244,7 +245,8 @@ void GpuSolver::free_all() {
     if (gc_fork) { cudaEventDestroy(gc_fork); gc_fork = nullptr; }
     if (gc_join) { cudaEventDestroy(gc_join); gc_join = nullptr; }
     if (stream) { cudaStreamDestroy(stream); stream = nullptr; }
-    kv_K = 0; fwd_cap = 0; dc_K = 0; hc_cap = 0; obs_cap = 0; diag_cap = 0;
+    kv_K = 0; fwd_cap = 0; E_cap = 0; E_nf = 0; E_K = 0; dc_K = 0; hc_cap = 0; obs_cap = 0; diag_cap = 0;
+    jtj_ns = -1;
     ready = false; have_sigma = false; lap_built = false; stations_set = false;
 }
 
@@ -312,6 +314,40 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     }
     // later neighbours are coloured afterwards; greedy above only looked at
     // j < i, which is exactly the constraint set of sequential greedy.
+    //
+    // Small colours (under 1 % of the free rows; greedy leaves a few, each a
+    // launch per sweep and mostly padding slices): each of their rows moves
+    // to the lowest large colour that none of its neighbours has; colours
+    // left empty disappear and the rest are renumbered in order.
+    {
+        int nc0 = *std::max_element(colour.begin(), colour.end()) + 1;
+        std::vector<long> cnt(nc0, 0);
+        long nfree = 0;
+        for (int i = 0; i < ne; ++i)
+            if (free_row(i)) { ++cnt[colour[i]]; ++nfree; }
+        std::vector<char> small(nc0, 0);
+        for (int c = 0; c < nc0; ++c) small[c] = cnt[c] > 0 && cnt[c] < nfree / 100;
+        std::vector<int> mark(nc0, -1);
+        for (int i = 0; i < ne; ++i) {
+            if (!free_row(i) || !small[colour[i]]) continue;
+            for (int k = L.s_ptr[i]; k < L.s_ptr[i + 1]; ++k) {
+                const int j = L.s_idx[k];
+                if (j != i && free_row(j)) mark[colour[j]] = i;
+            }
+            for (int c = 0; c < nc0; ++c)
+                if (!small[c] && mark[c] != i) {
+                    --cnt[colour[i]];
+                    ++cnt[c];
+                    colour[i] = c;
+                    break;
+                }
+        }
+        std::vector<int> remap(nc0, -1);
+        int next = 0;
+        for (int c = 0; c < nc0; ++c)
+            if (cnt[c] > 0 || c == 0) remap[c] = next++;
+        for (int i = 0; i < ne; ++i) colour[i] = remap[colour[i]];
+    }
     const int n_col = *std::max_element(colour.begin(), colour.end()) + 1;
 
     // Permutation: the reference order (cell by cell along the Morton curve)
@@ -538,6 +574,7 @@ void GpuSolver::set_sigma(const double* sigma, int n) {
     cuda_ok(cudaMemcpyAsync(d_sigma, sigma, sizeof(double) * n, cudaMemcpyHostToDevice, stream), "sigma");
     phys::edge_mass(md, d_sigma, d_Me, d_me_dc, stream);
     phys::diag_coeffs(md, d_Me, d_diag, d_diag32, stream);
+    learn_sigma_changed();
     launches += 2;
     have_sigma = true;
     lap_built = false;
@@ -606,6 +643,13 @@ void GpuSolver::set_stations(const double* xyz, int n) {
     stations_set = true;
     hc_cap = 0;
     dfree(d_hc); dfree(d_Z); dfree(d_wr);
+    // every buffer sized by the station count goes with the old stations:
+    // observed data and errors of gradient_batch, the weighted dZ and
+    // residual buffers of jtjv_batch
+    dfree(d_obs); dfree(d_err);
+    obs_cap = 0;
+    dfree(d_jtj_dz); dfree(d_jtj_wr0); dfree(d_jtj_wr1); dfree(d_jtj_err);
+    jtj_ns = -1;
     sync();
 }
 
@@ -623,13 +667,29 @@ void GpuSolver::ensure_vecs(int K) {
     kv_K = K;
 }
 
+// Work vectors of the forward / adjoint calls.  The resident background
+// field d_E is not among them: a call that only needs wider scratch (e.g.
+// solve_rhs_batch with 16 right-hand sides after a 2-frequency forward) must
+// not drop the field that jtjv_batch, perturbation_rhs and background_E read.
 void GpuSolver::ensure_fields(int K) {
     if (fwd_cap >= K) return;
-    dfree(d_E); dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
+    dfree(d_Epri); dfree(d_Ebc); dfree(d_rhs); dfree(d_tmp); dfree(d_lam); dfree(d_adj);
     const size_t n = (size_t)n_pad * K;
-    d_E = dalloc<double2>(n); d_Epri = dalloc<double2>(n); d_Ebc = dalloc<double2>(n);
+    d_Epri = dalloc<double2>(n); d_Ebc = dalloc<double2>(n);
     d_rhs = dalloc<double2>(n); d_tmp = dalloc<double2>(n); d_lam = dalloc<double2>(n); d_adj = dalloc<double2>(n);
     fwd_cap = K;
+}
+
+// The resident background field, [n_pad][K] with the writer's K as stride.
+// Only its writers (run_forward, set_background) grow it; a regrow discards
+// the old field, so the resident-field state is reset with it.
+void GpuSolver::ensure_E(int K) {
+    if (E_cap >= K) return;
+    dfree(d_E);
+    d_E = dalloc<double2>((size_t)n_pad * K);
+    E_cap = K;
+    E_nf = 0;
+    E_K = 0;
 }
 
 void GpuSolver::ensure_dc(int K) {
@@ -1015,13 +1075,14 @@ BatchResult GpuSolver::solve_batch(int K, const int* fmap, double2* b, double2* 
             sync();
             bool run = false;
             for (int k = 0; k < K; ++k) run |= hs[k].status == kRunning;
+            if (collecting && net && run) collect_snapshot(v.x, v.r, K, hs, fmap);   // training pairs
             if (!run || it >= maxiter) break;
             for (int i = 0; i < chunk && it < maxiter; ++i, ++it) bicg_iteration(c, v, d_states);
         }
         for (int k = 0; k < K; ++k) {
             if (!run_set[k]) continue;
             R.iters[k] += hs[k].iter;
-            R.status[k] = hs[k].status;
+            R.status[k] = hs[k].status == kRunning ? kMaxIter : hs[k].status;   // stopped by the host's cap
             R.res[k] = hs[k].res;
         }
         // FP64 true residual || b - A x || / || b || of every active rhs
@@ -1035,12 +1096,15 @@ BatchResult GpuSolver::solve_batch(int K, const int* fmap, double2* b, double2* 
         sync();
         for (int k = 0; k < K; ++k) {
             if (active[k]) R.true_res[k] = hs[k].true_res;
+            // non-finite values reached the iterate: report a breakdown
+            if (active[k] && !std::isfinite(R.true_res[k])) R.status[k] = kBreakdown;
             const bool again = run_set[k] && R.status[k] == kConverged && R.true_res[k] > tol &&
                                R.iters[k] < maxiter;
             run_set[k] = again ? 1 : 0;
             if (again && pass + 1 < passes) ++stats.refinements;
         }
     }
+    if (collecting && net) collect_finish(x, K);
     timer.collect();
     return R;
 }
@@ -1108,18 +1172,34 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
 
 BatchResult GpuSolver::solve_any(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
                                  double tol, int maxiter) {
-    BatchResult R = (P.precision == 1) ? solve_batch_mixed(K, fmap, b, x, active, tol, maxiter)
-                                       : solve_batch(K, fmap, b, x, active, tol, maxiter);
+    BatchResult R = (P.precision == 1 && P.krylov == 1) ? solve_batch_fgmres(K, fmap, b, x, active, tol, maxiter)
+                    : (P.precision == 1)                 ? solve_batch_mixed(K, fmap, b, x, active, tol, maxiter)
+                                                         : solve_batch(K, fmap, b, x, active, tol, maxiter);
     check_seg_err();
     return R;
 }
 
+// A staged kernel whose barrier wait timed out skipped its slices: the
+// call's results are invalid and the call fails with M3D_ERR_CUDA.  The error
+// bit is cleared (a test-hook bit is kept) so that the next call starts clean.
 void GpuSolver::check_seg_err() {
     if (!d_seg_err) return;
     unsigned e = 0;
     cuda_ok(cudaMemcpyAsync(&e, d_seg_err, sizeof(unsigned), cudaMemcpyDeviceToHost, stream), "seg err");
     sync();
-    if (e) throw std::runtime_error("slice-staged copy did not complete (barrier wait timed out)");
+    if (e & dev::kErrCopyTimeout) {
+        const unsigned keep = e & dev::kTestConsumeNoWait;
+        cuda_ok(cudaMemcpyAsync(d_seg_err, &keep, sizeof(unsigned), cudaMemcpyHostToDevice, stream), "seg err");
+        sync();
+        throw std::runtime_error("slice-staged copy did not complete (barrier wait timed out)");
+    }
+}
+
+void GpuSolver::set_test_consume_no_wait(bool on) {
+    if (!d_seg_err) throw std::logic_error("solver not set up");
+    const unsigned v = on ? dev::kTestConsumeNoWait : 0u;
+    cuda_ok(cudaMemcpyAsync(d_seg_err, &v, sizeof(unsigned), cudaMemcpyHostToDevice, stream), "seg err");
+    sync();
 }
 
 // Slice segments (staged.cuh) of the split operator for both precisions:
@@ -1240,7 +1320,12 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             R.res[k] = rel;
             if (!run[k]) continue;
             if (rel <= tol) { run[k] = 0; R.status[k] = kConverged; continue; }
-            if (!std::isfinite(rel) || rel > 0.9 * prev[k] || R.iters[k] >= maxiter || step == max_steps) {
+            if (!std::isfinite(rel)) {   // non-finite values reached the iterate: report, stop this lane
+                run[k] = 0;
+                R.status[k] = kBreakdown;
+                continue;
+            }
+            if (rel > 0.9 * prev[k] || R.iters[k] >= maxiter || step == max_steps) {
                 run[k] = 0;
                 if (R.status[k] == kInactive || R.status[k] == kConverged) R.status[k] = kMaxIter;
                 continue;
@@ -1452,6 +1537,31 @@ double GpuSolver::timer_stop() {
     return ms;
 }
 
+// Algorithmic bytes of one divergence-correction call, from its counters:
+// per outer round the divergence div(sigma E) (E read, edge mass, two
+// incidence entries per edge, divJ written) and the update E -= G phi (E read
+// and written, phi gathered); per PCG sweep of the Poisson solve the
+// Laplacian product and the vector streams -- FP32 vectors and the packed
+// 8-byte Laplacian entries (read by the product and twice by the level-0
+// smoothing) in the mixed-precision solve, FP64 vectors with 12-byte CSR
+// entries in the FP64 PCG.  Coarse multigrid levels are not counted.
+double GpuSolver::divcorr_bytes(const phys::DcCounters& before, const phys::DcCounters& after, int K) const {
+    const double n = L.ne, nn = L.nn, q = 2.0 * L.ne;
+    const double outer = (double)(after.outer - before.outer);
+    const double sweeps = (double)(after.cg_sweeps - before.cg_sweeps);
+    const double round = (n * K * 16 + n * 8 + q * 12 + nn * K * 16) + (2 * n * K * 16 + q * 12 + nn * K * 16);
+    const double sweep = P.divcorr_mixed && P.divcorr_precond ? 10.0 * nn * K * 8 + 3.0 * 8 * q
+                                                              : 8.0 * nn * K * 16 + q * 12 + nn * 8;
+    return outer * round + sweeps * sweep;
+}
+
+// Algorithmic bytes of one sensitivity launch over `lanes` (E, lambda) pairs:
+// both fields once, the cell->edge map (about 12 index + weight entries per
+// cell), sigma read and the gradient read and written.
+double GpuSolver::sens_bytes(int lanes) const {
+    return 2.0 * L.ne * 16.0 * lanes + (double)L.nc * (12.0 * 12.0) + 24.0 * L.nc;
+}
+
 // ---------------------------------------------------------------------------
 // forward: solve_frequency (forward_solver_fv.cpp:84-531) for nf frequencies
 // ---------------------------------------------------------------------------
@@ -1466,6 +1576,7 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
     factorize(freqs);
     ensure_vecs(K);
     ensure_fields(K);
+    ensure_E(K);
     ensure_hc(nf);
     std::vector<int> fmap(K, 0), pol(K, -1), active(K, 0);
     for (int k = 0; k < Kreal; ++k) { fmap[k] = k / 2; pol[k] = k % 2; active[k] = 1; }
@@ -1496,9 +1607,11 @@ void GpuSolver::run_forward(const std::vector<double>& freqs, double* Z_out) {
     if (P.div_correction) {
         ensure_dc(K);
         const int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
+        const phys::DcCounters dc0 = dcc;
         launches += phys::divcorr(md, d_me_dc, E, false, dc, P.div_corr_iters, P.div_corr_tol, active.data(),
                                   red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
         timer.end(th);
+        timer.set_bytes(th, divcorr_bytes(dc0, dcc, K));
     }
     phys::station_impedance(sd, E, d_omegas, nf, d_hc, d_Z, stream);
     ++launches;
@@ -1536,6 +1649,7 @@ void GpuSolver::background_E(int pol, double* out) {
 
 void GpuSolver::set_background(const double* E1, const double* E2) {
     ensure_fields(2);
+    ensure_E(2);
     cuda_ok(cudaMemsetAsync(d_E, 0, sizeof(double2) * (size_t)n_pad * 2, stream), "memset");
     for (int p = 0; p < 2; ++p) {
         cuda_ok(cudaMemcpyAsync(d_host_stage, p == 0 ? E1 : E2, sizeof(double2) * L.ne, cudaMemcpyHostToDevice, stream), "E");
@@ -1573,9 +1687,13 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
     phys::dc_phi0(md, VecK{rhs, K}, info, dc, stream);
     ++launches;
     int th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
-    launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
-                              active.data(), red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
-    timer.end(th);
+    {
+        const phys::DcCounters dc0 = dcc;
+        launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
+                                  active.data(), red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
+        timer.end(th);
+        timer.set_bytes(th, divcorr_bytes(dc0, dcc, K));
+    }
     std::vector<int> done(K, 0);
     std::vector<double> prev(K, 1e30);
     for (int k = 0; k < K; ++k) done[k] = !active[k];
@@ -1606,9 +1724,11 @@ void GpuSolver::solve_divcorr(int K, const int* fmap, const RhsInfo& info, doubl
         for (int k = 0; k < K; ++k) anyd |= dca[k] != 0;
         if (!anyd) break;
         th = timer.on ? timer.begin(kClsDivcorr, 0.0, K) : -1;
+        const phys::DcCounters dc0 = dcc;
         launches += phys::divcorr(md, d_me_dc, VecK{x, K}, true, dc, P.div_corr_iters, P.div_corr_tol,
                                   dca.data(), red, stream, 25, &dcc, amg_or_null(), mixed_or_null());
         timer.end(th);
+        timer.set_bytes(th, divcorr_bytes(dc0, dcc, K));
         std::vector<BicgState> hs(K);
         for (int k = 0; k < K; ++k) {
             std::memset(&hs[k], 0, sizeof(BicgState));
@@ -1700,8 +1820,9 @@ void GpuSolver::solve_rhs_batch(const double* rhs_h, int n_rhs, double* out) {
     std::vector<int> all_it, all_st;
     std::vector<double> all_tr;
     long long it_total = 0;
-    for (int r0 = 0; r0 < n_rhs; r0 += dev::kMaxRhs) {
-        const int g = std::min(dev::kMaxRhs, n_rhs - r0);
+    const int blk = std::max(2, std::min(dev::kMaxRhs, rhs_block));
+    for (int r0 = 0; r0 < n_rhs; r0 += blk) {
+        const int g = std::min(blk, n_rhs - r0);
         const int K = pow2_at_least(std::max(2, g));
         ensure_fields(K);
         ensure_vecs(K);
@@ -1837,11 +1958,15 @@ void GpuSolver::jtjv_batch(const double* freqs, int nf, const double* dsigma, co
     if (!d_jtj_rhs) {
         d_jtj_rhs = dalloc<double2>(nv); d_jtj_dE = dalloc<double2>(nv);
         d_jtj_a = dalloc<double2>(nv); d_jtj_b = dalloc<double2>(nv);
+        d_jtj_ds = dalloc<double>((size_t)L.nc);
+    }
+    if (jtj_ns != ns) {   // station-sized buffers follow the current station set
+        dfree(d_jtj_dz); dfree(d_jtj_wr0); dfree(d_jtj_wr1); dfree(d_jtj_err);
         d_jtj_dz = dalloc<double2>((size_t)dev::kMaxRhs * std::max(1, ns) * 4);
         d_jtj_wr0 = dalloc<double2>((size_t)8 * std::max(1, ns) * 4);
         d_jtj_wr1 = dalloc<double2>((size_t)8 * std::max(1, ns) * 4);
-        d_jtj_ds = dalloc<double>((size_t)L.nc);
         d_jtj_err = dalloc<double>((size_t)8 * std::max(1, ns) * 4);
+        jtj_ns = ns;
     }
     ensure_fields(K);
     cuda_ok(cudaMemcpyAsync(d_jtj_ds, dsigma, sizeof(double) * L.nc, cudaMemcpyHostToDevice, stream), "dsigma");
@@ -1896,7 +2021,11 @@ void GpuSolver::jtjv_batch(const double* freqs, int nf, const double* dsigma, co
     run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
     it_total += stats.total_iterations;
     keep();
-    phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, nf, 2, d_grad, stream);
+    {
+        const int ts = timer.on ? timer.begin(kClsSens, sens_bytes(2 * nf), K) : -1;
+        phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, nf, 2, d_grad, stream);
+        timer.end(ts);
+    }
     ++launches;
     cuda_ok(cudaMemcpyAsync(out, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "out");
     sync();
@@ -2036,7 +2165,9 @@ void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, c
         run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
         it_total += stats.total_iterations;
         keep();
+        const int ts = timer.on ? timer.begin(kClsSens, sens_bytes(2 * g), K) : -1;
         phys::sensitivity(md, d_sigma, VecK{d_E, K}, VecK{d_lam, K}, d_omegas, g, 2, d_grad, stream);
+        timer.end(ts);
         ++launches;
     }
     cuda_ok(cudaMemcpyAsync(grad, d_grad, sizeof(double) * L.nc, cudaMemcpyDeviceToHost, stream), "grad");
@@ -2050,6 +2181,96 @@ void GpuSolver::gradient_batch(const double* freqs, int nf, const double* obs, c
     }
     stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     end_call();
+}
+
+// ---------------------------------------------------------------------------
+// autotuner of the batched FP32 inner solve (no counterpart in the reference,
+// which has one serial solve)
+// ---------------------------------------------------------------------------
+
+// For each row-kernel layout (CSR rows read by the lanes, slice-staged rows)
+// and each batch width K <= max_K (right-hand sides sharing one matrix
+// stream), runs `reps` iterations of the FP32 BiCGStab inner solve -- with
+// the gradient-space term when the solver would use it at this frequency --
+// on a constant right-hand side with tolerance 0, timed with CUDA events on
+// the solver's stream.  The layout that is fastest at the widest batch and
+// the batch width with the least time per right-hand side are applied
+// (row_kernels, rhs_block).  The factorisation and the resident fields are
+// dropped: call after set_sigma, before the solves.
+std::vector<TuneEntry> GpuSolver::autotune(double freq, int max_K, int reps) {
+    if (!(freq > 0.0)) throw std::invalid_argument("frequency must be > 0");
+    if (reps < 1) throw std::invalid_argument("reps must be >= 1");
+    max_K = std::max(2, std::min(dev::kMaxRhs, max_K));
+    factorize(std::vector<double>{freq});
+    ensure_vecs32(max_K);
+    const double om = 2.0 * kPi * freq;
+    const bool use_gc = gc_ok && P.gradcorr == 1 && gc.omega_max > 0.0 && om <= gc.omega_max;
+    const int rk_saved = P.row_kernels;
+    std::vector<TuneEntry> out;
+    cudaEvent_t e0, e1;
+    cuda_ok(cudaEventCreate(&e0), "event");
+    cuda_ok(cudaEventCreate(&e1), "event");
+    const bool timer_on = timer.on;
+    timer.on = false;
+    try {
+        for (int rk : {kRowsDirect, kRowsStaged}) {
+            P.row_kernels = rk;
+            for (int K = 2; K <= max_K; K *= 2) {
+                std::vector<int> fmap(K, 0);
+                const size_t n = (size_t)n_pad * K;
+                // b = 1 + 1i on every row (bit pattern of 1.0f), x = 0
+                const std::vector<float2> ones(n, make_float2(1.0f, 1.0f));
+                cuda_ok(cudaMemcpyAsync(kv32.b, ones.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, stream),
+                        "b");
+                cuda_ok(cudaMemsetAsync(kv32.x, 0, sizeof(float2) * n, stream), "memset");
+                std::vector<BicgState> st(K);
+                for (int k = 0; k < K; ++k) {
+                    std::memset(&st[k], 0, sizeof(BicgState));
+                    st[k].tol = 0.0;
+                    st[k].maxiter = 1 << 30;
+                    st[k].status = kRunning;
+                }
+                cuda_ok(cudaMemcpyAsync(d_states, st.data(), sizeof(BicgState) * K, cudaMemcpyHostToDevice, stream),
+                        "states");
+                KrylovCtx<float> c32 = kctx32(K, fmap.data());
+                if (use_gc) attach_gc(c32);
+                bicg_init(c32, kv32, d_states);
+                for (int i = 0; i < 2; ++i) bicg_iteration(c32, kv32, d_states);   // warm-up
+                cuda_ok(cudaEventRecord(e0, stream), "event");
+                for (int i = 0; i < reps; ++i) bicg_iteration(c32, kv32, d_states);
+                cuda_ok(cudaEventRecord(e1, stream), "event");
+                cuda_ok(cudaEventSynchronize(e1), "event");
+                float ms = 0.f;
+                cuda_ok(cudaEventElapsedTime(&ms, e0, e1), "event");
+                check_seg_err();
+                out.push_back(TuneEntry{rk, K, ms / reps, ms / reps / K});
+            }
+        }
+    } catch (...) {
+        P.row_kernels = rk_saved;
+        timer.on = timer_on;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    timer.on = timer_on;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // layout: fastest at the widest batch; batch width: least time per rhs
+    int best_rk = rk_saved;
+    double best_t = 1e300;
+    for (const TuneEntry& t : out)
+        if (t.K == max_K && t.ms_per_iter < best_t) { best_t = t.ms_per_iter; best_rk = t.row_kernels; }
+    int best_K = max_K;
+    double best_r = 1e300;
+    for (const TuneEntry& t : out)
+        if (t.row_kernels == best_rk && t.ms_per_rhs_iter < best_r) { best_r = t.ms_per_rhs_iter; best_K = t.K; }
+    P.row_kernels = best_rk;
+    rhs_block = best_K;
+    release();
+    E_nf = 0;
+    E_K = 0;
+    return out;
 }
 
 }  // namespace m3d

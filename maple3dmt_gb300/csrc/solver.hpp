@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <complex>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -15,8 +17,19 @@
 #include "cuda/physics.cuh"
 #include "cuda/gradcorr.cuh"
 #include "cuda/regularization.cuh"
+#include "cuda/learned.cuh"
 
 namespace m3d {
+
+// One measured configuration of the autotuner: row-kernel layout, batch
+// width K, milliseconds per FP32 BiCGStab iteration of the batch and per
+// right-hand side.
+struct TuneEntry {
+    int row_kernels;
+    int K;
+    double ms_per_iter;
+    double ms_per_rhs_iter;
+};
 
 struct BatchResult {
     int K = 0;
@@ -43,6 +56,27 @@ public:
     void factorize(const std::vector<double>& freqs);
     void compute_single_frequency(double freq, double* Z_out);
     void background_E(int pol, double* out);
+    void set_test_consume_no_wait(bool on);   // test hook of the staged kernels' error path
+    // times the FP32 inner solve for each row-kernel layout and batch width
+    // (<= max_K) at frequency freq and applies the fastest; drops the
+    // factorisation and the resident fields
+    std::vector<TuneEntry> autotune(double freq, int max_K, int reps);
+    int rhs_block = 16;   // right-hand sides per batched solve of solve_rhs_batch
+
+    // ---- learned preconditioner (no counterpart in the reference) ----
+    // dense grid of 2^grid_level cells per axis, a `layers`-deep network of
+    // `hidden` channels, room for max_samples training pairs
+    void learn_setup(int grid_level, int layers, int hidden, unsigned seed, long max_samples);
+    // plain FP64 SSOR-BiCGStab forward solves of freqs (current sigma),
+    // recording training pairs; returns the pairs held
+    long learn_collect(const double* freqs, int nf);
+    // Adam epochs over the first (1 - val_frac) of the pairs; mean loss per
+    // epoch, the held-out pairs' loss to *val_loss
+    std::vector<double> learn_train(int epochs, float lr, int batch, unsigned seed, double val_frac,
+                                    double* val_loss);
+    long learn_samples() const { return ds_n; }
+    bool learn_trained() const { return net_trained; }
+    learn::Cnn* learn_net() { return net.get(); }
     void set_background(const double* E1, const double* E2);
     void build_adjoint_rhs(const double* wr, double* rhs1, double* rhs2);
     void adjoint_solve(const double* rhs, double* lam, bool perturbation);
@@ -88,6 +122,8 @@ public:
 
     int n_edges() const { return L.ne; }
     int n_cells() const { return L.nc; }
+    int n_stations() const { return sd.ns; }
+    long nnz_off = 0;       // off-diagonal stiffness entries
     int n_nodes() const { return L.nn; }
     int n_colours() const { return (int)colour_ptr.size() - 1; }
 
@@ -183,6 +219,8 @@ private:
     double2* d_lam = nullptr;     // adjoint solutions
     double2* d_adj = nullptr;     // adjoint sources
     int fwd_cap = 0;
+    int E_cap = 0;       // capacity (lanes) of d_E, grown only by its writers
+    int jtj_ns = -1;     // station count the jtjv_batch station buffers were sized for
 
     // divergence correction
     phys::DcWork dc{};
@@ -208,6 +246,9 @@ private:
     void ensure_sigma_device();
     void ensure_vecs(int K);
     void ensure_fields(int K);
+    void ensure_E(int K);
+    double divcorr_bytes(const phys::DcCounters& before, const phys::DcCounters& after, int K) const;
+    double sens_bytes(int lanes) const;
     void ensure_dc(int K);
     void ensure_hc(int nf);
     KrylovCtx<double> kctx(int K, const int* fmap) const;
@@ -231,8 +272,37 @@ private:
     void solve_divcorr(int K, const int* fmap, const RhsInfo& info, double2* rhs, double2* x,
                        const std::vector<int>& active, double tol, std::vector<int>& iters,
                        std::vector<int>& status, std::vector<double>& tres);
-    long nnz_off = 0;
     phys::DcCounters dcc;   // divergence-correction counters of the current call
+    // learned preconditioner state (learned_solver.cu)
+    std::unique_ptr<learn::Cnn> net;
+    learn::GridMap gm{};
+    int learn_level = 0;
+    __nv_bfloat16* ds_feat = nullptr;   // [ds_cap][G^3][8] network inputs
+    float* ds_tgt = nullptr;            // [ds_cap][G^3][6] targets
+    long ds_n = 0, ds_cap = 0;
+    float* lw_work = nullptr;           // grid means scratch [16][G^3][6] + 16
+    double* d_lane_freq = nullptr;
+    int* d_snap_lane = nullptr;
+    long* d_snap_slot = nullptr;
+    float* tr_target = nullptr;
+    bool net_trained = false;
+    bool collecting = false;
+    struct Snap { int lane; long slot; };
+    std::vector<Snap> pending;
+    float2 *fg_V = nullptr, *fg_Z = nullptr, *fg_w = nullptr;
+    double2 *fg_part = nullptr, *fg_h = nullptr;
+    double *fg_inv = nullptr, *fg_scale = nullptr;
+    int fg_cap_K = 0, fg_cap_m = 0;
+    void learn_free();
+    void learn_sigma_changed();
+    void collect_snapshot(const double2* x, const double2* r, int K, const std::vector<BicgState>& hs,
+                          const int* fmap);
+    void collect_finish(const double2* x, int K);
+    void net_apply(const KrylovCtx<float>& c32, const float2* v, float2* z, int K, const int* fmap);
+    void ensure_fgmres(int K, int m);
+    void fg_mdot(const float2* V, int nv, const float2* w, int K, std::vector<std::complex<double>>& h);
+    BatchResult solve_batch_fgmres(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
+                                   double tol, int maxiter);
     void sync();
 };
 

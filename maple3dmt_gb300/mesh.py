@@ -17,8 +17,8 @@ import numpy as np
 
 from . import _abi, _loader
 
-MU0 = 4.0e-7 * math.pi
-SIGMA_AIR = 1e-8
+from .workloads import (MU0, SIGMA_AIR, driver_domain, layered_block_sigma, skin_depth,  # noqa: F401
+                        station_grid)
 
 
 @dataclass
@@ -91,10 +91,6 @@ def build_octree(domain, min_level, max_level, stations, freqs, *, station_refin
                   level, q, cx, cy, cz, ty)
 
 
-def skin_depth(freq, sigma):
-    return math.sqrt(2.0 / (2.0 * math.pi * freq * MU0 * sigma))
-
-
 @dataclass
 class Survey:
     """A synthetic MT survey: mesh, conductivity, stations and frequencies."""
@@ -105,28 +101,6 @@ class Survey:
     stations: np.ndarray       # [ns, 3]
     freqs: np.ndarray          # [nf] Hz
     meta: dict = field(default_factory=dict)
-
-
-def station_grid(n, spacing):
-    c = (np.arange(n) - (n - 1) / 2.0) * spacing
-    xx, yy = np.meshgrid(c, c, indexing="xy")
-    return np.stack([xx.ravel(), yy.ravel(), np.zeros(n * n)], axis=1)
-
-
-def _driver_mesh(stations, freqs, half_width, sigma0, min_level, max_level, radius=None):
-    """Domain and station radius rules of examples/real_inversion_octree.cpp:298-379."""
-    fmin = float(np.min(freqs))
-    dmax = skin_depth(fmin, sigma0)
-    domain = (-half_width, half_width, -half_width, half_width, -3.0 * dmax, dmax)
-    if radius is None:
-        st = np.asarray(stations)
-        d = np.sqrt(((st[:, None, :2] - st[None, :, :2]) ** 2).sum(-1))
-        d = d[d > 100]
-        min_sp = float(d.min()) if d.size else 1000.0
-        finest = 2.0 * half_width / 2.0 ** max_level
-        radius = max(3.0 * finest, min_sp, 2000.0)
-        radius = min(radius, dmax * 0.1)
-    return domain, radius
 
 
 def assign_sigma(leaves: Leaves, earth_fn) -> np.ndarray:
@@ -141,20 +115,12 @@ def halfspace_survey(*, half_width=50000.0, min_level=3, max_level=5, n_side=5, 
     st = station_grid(n_side, spacing)
     fr = np.asarray(freqs, dtype=np.float64)
     sigma0 = 0.01
-    domain, radius = _driver_mesh(st, fr, half_width, sigma0, min_level, max_level)
+    domain, radius = driver_domain(st, fr, half_width, sigma0, max_level)
     lv = build_octree(domain, min_level, max_level, st, fr, station_refine_radius=radius,
                       sigma_bg=sigma0, lib=lib)
     sig = assign_sigma(lv, lambda x, y, z: np.full_like(z, 1.0 / rho))
     return Survey("halfspace", lv, sig, sigma0, st, fr,
                   {"station_refine_radius": radius, "rho": rho})
-
-
-def layered_block_sigma(x, y, z):
-    """10/100/1000 ohm-m layers (interfaces -1 km, -10 km) with a 0.5 ohm-m block
-    x in [-0.5, 0.5] km, y in [-1, 1] km, z in [-2.25, -0.25] km."""
-    s = np.where(z > -1000.0, 0.1, np.where(z > -10000.0, 0.01, 0.001))
-    blk = (np.abs(x) <= 500.0) & (np.abs(y) <= 1000.0) & (z <= -250.0) & (z >= -2250.0)
-    return np.where(blk, 2.0, s)
 
 
 def layered_block_survey(*, half_width=50000.0, min_level=5, max_level=7, n_side=11,
@@ -165,7 +131,7 @@ def layered_block_survey(*, half_width=50000.0, min_level=5, max_level=7, n_side
     st = station_grid(n_side, spacing)
     fr = np.logspace(-2, 2, 8) if freqs is None else np.asarray(freqs, dtype=np.float64)
     sigma0 = 0.01
-    domain, radius = _driver_mesh(st, fr, half_width, sigma0, min_level, max_level, radius)
+    domain, radius = driver_domain(st, fr, half_width, sigma0, max_level, radius)
     lv = build_octree(domain, min_level, max_level, st, fr, station_refine_radius=radius,
                       sigma_bg=sigma0, lib=lib)
     sig = assign_sigma(lv, layered_block_sigma)
@@ -175,6 +141,23 @@ def layered_block_survey(*, half_width=50000.0, min_level=5, max_level=7, n_side
         sig[earth] = sig[earth] * 10.0 ** rng.normal(0.0, noise_std, int(earth.sum()))
     return Survey("layered_block", lv, sig, sigma0, st, fr,
                   {"station_refine_radius": radius})
+
+
+def c5_survey(*, seed=7, rho_start=100.0, lib=None) -> Survey:
+    """C5, the inversion iteration at scale: octree levels 6/8 (about 3.1 M
+    edges), 400 stations on a 20x20 grid at 1 km, 24 frequencies log-spaced
+    0.001-1000 Hz.  `sigma` is the starting model (a 100 ohm-m halfspace under
+    air); meta["sigma_true"] is the seeded random layered-plus-blocks model
+    the synthetic data come from."""
+    from . import workloads
+    sp = workloads.C5
+    sv = layered_block_survey(min_level=sp.min_level, max_level=sp.max_level, n_side=sp.n_side,
+                              spacing=sp.spacing, freqs=np.asarray(sp.freqs), lib=lib)
+    lv = sv.leaves
+    true = workloads.cell_sigma(lv.cell_type, lv.cx, lv.cy, lv.cz, workloads.random_layered_blocks(seed))
+    start = workloads.cell_sigma(lv.cell_type, lv.cx, lv.cy, lv.cz, workloads.halfspace_sigma(rho_start))
+    return Survey("c5", lv, start, sv.sigma_bg, sv.stations, sv.freqs,
+                  {**sv.meta, "sigma_true": true, "seed": seed, "rho_start": rho_start})
 
 
 def small_survey(*, min_level=2, max_level=4, n_side=2, spacing=4000.0, freqs=(0.5,),

@@ -14,7 +14,7 @@ import numpy as np
 
 from . import _loader, mesh
 from ._abi import c_double_p, c_int_p
-from ._abi_solver import KERNEL_CLASSES, KernelTimes, Params, RegParams, Stats
+from ._abi_solver import KERNEL_CLASSES, KernelTimes, Params, RegParams, Stats, TuneEntry
 
 ERRORS = {1: "ARG", 2: "STATE", 3: "CUDA", 4: "OOM", 5: "NO_DEVICE", 6: "TOO_LARGE", 7: "NUMERIC"}
 
@@ -78,6 +78,7 @@ class ForwardSolverFV:
     def setup(self, leaves: mesh.Leaves, params: Params | None = None, **kw):
         p = params or default_params(**kw)
         self._leaves = leaves
+        self._krylov = [p.krylov, p.fgmres_m, p.learned_period]
         st = mesh.leaves_struct(leaves)
         self._ck(self.lib.m3d_solver_setup(self.h, C.byref(st), C.byref(p)))
         ne, nc, nn, ncol = C.c_int(), C.c_int(), C.c_int(), C.c_int()
@@ -252,6 +253,47 @@ class ForwardSolverFV:
         ms = C.c_double()
         self._ck(self.lib.m3d_timer_stop(self.h, C.byref(ms)))
         return ms.value
+
+    def autotune(self, freq, max_K=16, reps=10, force=False) -> dict:
+        """Measure and apply the row-kernel layout and the right-hand-side
+        block of the batched FP32 inner solve (include/m3d_gb300.h)."""
+        table = (TuneEntry * 8)()
+        n, rk, blk, cached = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._ck(self.lib.m3d_autotune(self.h, float(freq), int(max_K), int(reps), 1 if force else 0, table,
+                                       C.byref(n), C.byref(rk), C.byref(blk), C.byref(cached)))
+        return dict(row_kernels=rk.value, rhs_block=blk.value, cached=bool(cached.value),
+                    table=[dict(row_kernels=t.row_kernels, K=t.K, ms_per_iter=t.ms_per_iter,
+                                ms_per_rhs_iter=t.ms_per_rhs_iter) for t in table[:n.value]])
+
+    def set_params(self, krylov=None, fgmres_m=None, learned_period=None):
+        """Change the inner solve between calls (m3d_set_krylov)."""
+        k = self._krylov
+        for i, v in enumerate((krylov, fgmres_m, learned_period)):
+            if v is not None:
+                k[i] = int(v)
+        self._ck(self.lib.m3d_set_krylov(self.h, *k))
+
+    # ---- learned preconditioner (include/m3d_gb300.h, m3d_learn_*) ----
+    def learn_setup(self, grid_level=5, layers=6, hidden=32, seed=0, max_samples=5000):
+        self._ck(self.lib.m3d_learn_setup(self.h, int(grid_level), int(layers), int(hidden), int(seed),
+                                          int(max_samples)))
+
+    def learn_collect(self, freqs) -> int:
+        f, pf = _d(np.asarray(freqs, np.float64).reshape(-1))
+        n = C.c_longlong()
+        self._ck(self.lib.m3d_learn_collect(self.h, pf, int(f.shape[0]), C.byref(n)))
+        return n.value
+
+    def learn_train(self, epochs=20, lr=1e-3, batch=16, seed=0, val_frac=0.1):
+        hist = np.zeros(int(epochs))
+        val = C.c_double()
+        self._ck(self.lib.m3d_learn_train(self.h, int(epochs), float(lr), int(batch), int(seed), float(val_frac),
+                                          hist.ctypes.data_as(c_double_p), C.byref(val)))
+        return hist, val.value
+
+    def test_set_consume_no_wait(self, on: bool):
+        """Test hook: staged kernels take their copy-wait timeout path."""
+        self._ck(self.lib.m3d_test_set_consume_no_wait(self.h, 1 if on else 0))
 
     def set_kernel_timing(self, on: bool):
         self._ck(self.lib.m3d_set_kernel_timing(self.h, 1 if on else 0))

@@ -81,6 +81,8 @@ def main():
     # the CPU-runnable halfspace configuration (5x5 stations, 1 Hz), at the
     # reference's own tolerance 1e-7
     make("halfspace_c1", mesh.halfspace_survey(), tol=1e-7, maxiter=5000, seed=2, layout=False)
+    # the same at 1e-10, below the solver-noise floor of the 1e-7 solve
+    make("halfspace_c1_t10", mesh.halfspace_survey(), tol=1e-10, maxiter=5000, seed=2, layout=False)
     # octree regularisation on the small mesh and on a 4/6-level layered mesh
     make_regularization("regularization_small", mesh.small_survey(freqs=(0.5, 4.0)))
     make_regularization("regularization_layered", mesh.layered_block_survey(min_level=4, max_level=6))

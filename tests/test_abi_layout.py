@@ -10,12 +10,13 @@ import pytest
 
 from conftest import ROOT
 
-STRUCTS = ("m3d_params", "m3d_stats", "m3d_kernel_times", "m3d_reg_params")
+STRUCTS = ("m3d_params", "m3d_stats", "m3d_kernel_times", "m3d_reg_params", "m3d_tune_entry")
 
 
 def _probe(tmp_path):
-    from maple3dmt_gb300._abi_solver import KernelTimes, Params, RegParams, Stats
-    mirrors = {"m3d_params": Params, "m3d_stats": Stats, "m3d_kernel_times": KernelTimes, "m3d_reg_params": RegParams}
+    from maple3dmt_gb300._abi_solver import KernelTimes, Params, RegParams, Stats, TuneEntry
+    mirrors = {"m3d_params": Params, "m3d_stats": Stats, "m3d_kernel_times": KernelTimes, "m3d_reg_params": RegParams,
+               "m3d_tune_entry": TuneEntry}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "m3d_gb300.h"', "int main(void) {"]
     for name in STRUCTS:
         lines.append(f'    printf("{name} sizeof %zu\\n", sizeof({name}));')

@@ -133,6 +133,22 @@ def test_halfspace_c1_against_reference(lib):
     assert rel(Zg[:, 1:3], Zref[:, 1:3]) < 1e-5
 
 
+def test_halfspace_c1_tight_against_reference(lib):
+    """C1 with both solves at 1e-10: all four impedance components of the GPU
+    solve agree with the reference's to 1e-6 relative (max |dZ| / max |Z|),
+    in FP64 and in mixed precision."""
+    g = load_golden("halfspace_c1_t10")
+    Zref = g["ref_Z"].reshape(-1, 4)
+    for precision in (0, 1):
+        s = _gpu(g, bicgstab_tol=1e-10, precision=precision)
+        Zg = s.compute_single_frequency(float(g["freqs"][0]))
+        st = s.stats()
+        assert all(t <= 1e-10 for t in st["true_residual"][:2]), st
+        e = rel(Zg, Zref)
+        print(f"C1 at 1e-10, precision {precision}: Z relative error {e:.2e}")
+        assert e < 1e-6
+
+
 def test_adjoint_pieces_match_oracle(g_small):
     g = g_small
     s = _gpu(g)
