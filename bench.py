@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--config", default="c2", choices=["c2", "c5"],
                     help="c2: the headline workload; c5: the inversion iteration at scale (levels 6/8, "
                          "3.1 M edges, 400 stations, 24 frequencies 0.001-1000 Hz, data from a random model)")
+    # profiling runs only: a smaller mesh of the same survey (octree levels)
+    ap.add_argument("--min-level", type=int, default=0, help="override the configuration's min octree level")
+    ap.add_argument("--max-level", type=int, default=0, help="override the configuration's max octree level")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--forward", default="reference", choices=["interleaved", "reference"])
     # profiling runs only (a capped solve is not a bench number): Krylov
@@ -93,11 +96,18 @@ def parse():
 # ---------------------------------------------------------------------------
 
 CONFIG = "c2"
+LEVELS = (0, 0)   # profiling overrides of (min, max) octree level
 
 
 def spec():
+    import dataclasses
     from maple3dmt_gb300 import workloads
-    return {"c2": workloads.C2, "c5": workloads.C5}[CONFIG]
+    sp = {"c2": workloads.C2, "c5": workloads.C5}[CONFIG]
+    if LEVELS[0]:
+        sp = dataclasses.replace(sp, min_level=LEVELS[0])
+    if LEVELS[1]:
+        sp = dataclasses.replace(sp, max_level=LEVELS[1])
+    return sp
 
 
 def survey_inputs(stations=None):
@@ -328,9 +338,9 @@ def cpu_measure(steps, warmup, procs, one_core=True):
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
-    if CONFIG != "c2":
-        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference sample is defined on C2 (its data "
-                          "at C5 come from a GPU forward solve of the random model)"}), flush=True)
+    if CONFIG != "c2" or LEVELS != (0, 0):
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference sample is defined on the C2 mesh "
+                          "(its leaf list is committed; C5 data come from a GPU forward solve)"}), flush=True)
         return
     W, K = args.warmup, args.steps
     # the CPU has no caches or JIT state that warm-up would settle beyond the
@@ -535,7 +545,7 @@ def run_ours(args, rank, world, local_rank):
     d2h = s.nc * 8 + nf * len(sv.stations) * 4 * 16
     try:
         cb = None
-        if not args.no_cpu and world == 1 and CONFIG == "c2":
+        if not args.no_cpu and world == 1 and CONFIG == "c2" and LEVELS == (0, 0):
             cb = cpu_measure(1, 0, args.cpu_procs, one_core=False)[0]
     except Exception as exc:  # the baseline must not hide the GPU number
         cb = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {exc}"}
@@ -572,9 +582,10 @@ def run_ours(args, rank, world, local_rank):
 
 
 def main():
-    global CONFIG
+    global CONFIG, LEVELS
     args = parse()
     CONFIG = args.config
+    LEVELS = (args.min_level, args.max_level)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -381,7 +381,7 @@ const char* m3d_cnn_last_error(const m3d_cnn* c);
  * tap t = (dz + 1) 9 + (dy + 1) 3 + (dx + 1) */
 int m3d_cnn_get_weights(m3d_cnn* c, float* w, float* b);
 int m3d_cnn_set_weights(m3d_cnn* c, const float* w, const float* b);
-/* x [n][D][H][W][c_in] -> y [n][D][H][W][c_out]; W in {32, 64, 128}, H a
+/* x [n][D][H][W][c_in] -> y [n][D][H][W][c_out]; W in {16, 32, 64, 128}, H a
  * multiple of 128 / W; zero padding at the grid boundary */
 int m3d_cnn_forward(m3d_cnn* c, const float* x, int n, int D, int H, int W, float* y);
 /* gradients of sum(dy * network(x)): dw, db as in get_weights, dx like x

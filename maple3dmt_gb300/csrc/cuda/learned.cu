@@ -607,7 +607,8 @@ unsigned Cnn::error_flag() {
 }
 
 void Cnn::ensure(int n, int D_, int H_, int W_) {
-    if (W_ != 32 && W_ != 64 && W_ != 128) throw std::invalid_argument("cnn: grid W must be 32, 64 or 128");
+    if (W_ != 16 && W_ != 32 && W_ != 64 && W_ != 128)
+        throw std::invalid_argument("cnn: grid W must be 16, 32, 64 or 128");
     const int bw_ = W_, bh_ = 128 / W_;
     if (H_ % bh_ != 0 || D_ < 1 || n < 1) throw std::invalid_argument("cnn: grid H must be a multiple of 128 / W");
     if (n <= n_cap && D_ == D && H_ == H && W_ == W) return;

@@ -40,7 +40,7 @@ public:
     void get_weights(float* w, float* b) const;
     void set_weights(const float* w, const float* b);
 
-    // Buffers for n samples of a D x H x W grid (W in {32, 64, 128}, H a
+    // Buffers for n samples of a D x H x W grid (W in {16, 32, 64, 128}, H a
     // multiple of 128 / W).
     void ensure(int n, int D, int H, int W);
     // input activations: [n][D][H][W][32] BF16, channels >= c_in zero

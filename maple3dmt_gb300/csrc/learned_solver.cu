@@ -267,7 +267,7 @@ void GpuSolver::learn_free() {
 
 void GpuSolver::learn_setup(int grid_level, int layers, int hidden, unsigned seed, long max_samples) {
     if (!ready) throw std::logic_error("solver not set up");
-    if (grid_level < 5 || grid_level > 7) throw std::invalid_argument("grid level must be 5, 6 or 7");
+    if (grid_level < 4 || grid_level > 7) throw std::invalid_argument("grid level must be 4 .. 7");
     if (max_samples < 1) throw std::invalid_argument("max_samples must be >= 1");
     learn_free();
     const int G = 1 << grid_level;
