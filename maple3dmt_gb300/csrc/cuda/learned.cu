@@ -497,7 +497,8 @@ Cnn::Cnn(int device, int layers, int c_in, int hidden, int c_out, unsigned seed)
     if (L < 2 || cin < 1 || cin > kCh || cout < 1 || cout > kCh || hid < 1 || hid > kCh)
         throw std::invalid_argument("cnn: layers >= 2, channels 1..32");
     ck(cudaSetDevice(dev), "cudaSetDevice");
-    ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+    ck(cudaStreamCreateWithFlags(&own_st, cudaStreamNonBlocking), "stream");
+    st = own_st;
     ci.assign(L, hid);
     co.assign(L, hid);
     ci[0] = cin;
@@ -543,7 +544,7 @@ Cnn::~Cnn() {
     dfree(wtbf);
     dfree(err);
     dfree(dch);
-    if (st) cudaStreamDestroy(st);
+    if (own_st) cudaStreamDestroy(own_st);   // never a caller's stream (set_stream)
 }
 
 void Cnn::free_grid() {

@@ -57,13 +57,16 @@ public:
     void get_grads(float* dw, float* db) const;
     unsigned error_flag();
     cudaStream_t stream() const { return st; }
-    void set_stream(cudaStream_t s) { st = s; }
+    // run on the caller's stream (the caller keeps ownership; null: the
+    // network's own stream again)
+    void set_stream(cudaStream_t s) { st = s ? s : own_st; }
 
 private:
     int dev, L, cin, hid, cout;
     int n_cap = 0, D = 0, H = 0, W = 0, V = 0;
     int bw = 0, bh = 0;
-    cudaStream_t st = nullptr;
+    cudaStream_t st = nullptr;       // the stream launches go to
+    cudaStream_t own_st = nullptr;   // created and destroyed by this object
     std::vector<int> ci, co;                 // channels in / out of each layer
     float *w32 = nullptr, *b32 = nullptr;    // FP32 masters
     float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;

@@ -101,16 +101,17 @@ __global__ void k_fg_add64(double2* __restrict__ x, const float2* __restrict__ d
 }
 
 // part[q][block][k] = sum over this block's elements of conj(V_q) w, q < nv
-// (V_q at V + q * ld); FP64 sums, lanes reduced in a fixed tree.
+// (V_q at V + q * ld), and for q = nv (with_self) of conj(w) w; FP64 sums,
+// lanes reduced in a fixed tree.
 constexpr int kFgMaxV = 48;
-__global__ void __launch_bounds__(256) k_fg_mdot(const float2* __restrict__ V, long ld, int nv,
+__global__ void __launch_bounds__(256) k_fg_mdot(const float2* __restrict__ V, long ld, int nv, int with_self,
                                                  const float2* __restrict__ w, int K, long n,
                                                  double2* __restrict__ part) {
     __shared__ double2 sh[256];
     const int nb = gridDim.x;
-    for (int q = 0; q < nv; ++q) {
+    for (int q = 0; q < nv + with_self; ++q) {
         double2 acc = make_double2(0.0, 0.0);
-        const float2* vq = V + (size_t)q * ld;
+        const float2* vq = q < nv ? V + (size_t)q * ld : w;
         for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)nb * blockDim.x) {
             const float2 a = vq[i], b = w[i];
             acc.x += (double)a.x * b.x + (double)a.y * b.y;
@@ -550,15 +551,18 @@ void GpuSolver::ensure_fgmres(int K, int m) {
     fg_cap_m = m;
 }
 
-// h[q][k] = (V_q, w)_k for q < nv into host h (also left in fg_h)
-void GpuSolver::fg_mdot(const float2* V, int nv, const float2* w, int K, std::vector<std::complex<double>>& h) {
+// h[q][k] = (V_q, w)_k for q < nv, and (w, w)_k as q = nv when with_self,
+// into host h (the first nv also left in fg_h)
+void GpuSolver::fg_mdot(const float2* V, int nv, const float2* w, int K, std::vector<std::complex<double>>& h,
+                        bool with_self) {
     const long n = (long)n_pad * K;
     const int nb = (int)std::min<long>(1024, (n + 255) / 256);
-    k_fg_mdot<<<nb, 256, 0, stream>>>(V, n, nv, w, K, n, fg_part);
-    k_fg_mdot_final<<<(nv * K + 255) / 256, 256, 0, stream>>>(fg_part, nv, nb, K, fg_h);
+    const int nq = nv + (with_self ? 1 : 0);
+    k_fg_mdot<<<nb, 256, 0, stream>>>(V, n, nv, with_self ? 1 : 0, w, K, n, fg_part);
+    k_fg_mdot_final<<<(nq * K + 255) / 256, 256, 0, stream>>>(fg_part, nq, nb, K, fg_h);
     lck(cudaGetLastError(), "mdot");
     launches += 2;
-    std::vector<double2> t((size_t)nv * K);
+    std::vector<double2> t((size_t)nq * K);
     lck(cudaMemcpyAsync(t.data(), fg_h, sizeof(double2) * t.size(), cudaMemcpyDeviceToHost, stream), "h");
     sync();
     h.resize(t.size());
@@ -654,21 +658,41 @@ BatchResult GpuSolver::solve_batch_fgmres(int K, const int* fmap, double2* b, do
             if (learned && (j % P.learned_period) == P.learned_period - 1) net_apply(c32, vj, zj, K, fmap);
             else precond_apply(c32, vj, kv32.y, zj);
             spmv(c32, kSpmvPlain, zj, fg_w, nullptr, nullptr, nullptr);
-            // classical Gram-Schmidt, twice
+            // classical Gram-Schmidt with the norm of w in the same reduction:
+            // |w - V h|^2 = |w|^2 - |h|^2 (V orthonormal); a second pass only
+            // where that cancels below half of |w|^2 (DGKS criterion)
             std::vector<cd> h1, h2;
-            fg_mdot(fg_V, j + 1, fg_w, K, h1);
+            fg_mdot(fg_V, j + 1, fg_w, K, h1, true);
             k_fg_maxpy<<<blocks(n), 256, 0, stream>>>(fg_V, ld, j + 1, fg_h, K, n, fg_w, -1.0f);
-            fg_mdot(fg_V, j + 1, fg_w, K, h2);
-            k_fg_maxpy<<<blocks(n), 256, 0, stream>>>(fg_V, ld, j + 1, fg_h, K, n, fg_w, -1.0f);
-            std::vector<cd> nw;
-            fg_mdot(fg_w, 1, fg_w, K, nw);
-            launches += 4;
+            launches += 3;
+            std::vector<double> nrm2(K, 0.0);
+            bool again = false;
+            for (int k = 0; k < K; ++k) {
+                if (!live[k]) continue;
+                double hh = 0.0;
+                for (int q = 0; q <= j; ++q) hh += std::norm(h1[(size_t)q * K + k]);
+                const double ww = h1[(size_t)(j + 1) * K + k].real();
+                nrm2[k] = ww - hh;
+                again |= nrm2[k] < 0.5 * ww;
+            }
+            if (again) {
+                fg_mdot(fg_V, j + 1, fg_w, K, h2, true);
+                k_fg_maxpy<<<blocks(n), 256, 0, stream>>>(fg_V, ld, j + 1, fg_h, K, n, fg_w, -1.0f);
+                launches += 3;
+                for (int k = 0; k < K; ++k) {
+                    if (!live[k]) continue;
+                    double hh = 0.0;
+                    for (int q = 0; q <= j; ++q) hh += std::norm(h2[(size_t)q * K + k]);
+                    nrm2[k] = h2[(size_t)(j + 1) * K + k].real() - hh;
+                }
+            }
             for (int k = 0; k < K; ++k) {
                 inv[k] = 0.0;
                 if (!live[k]) continue;
                 std::vector<cd>& Hk = H[k];
-                for (int q = 0; q <= j; ++q) Hk[(size_t)q * m + j] = h1[(size_t)q * K + k] + h2[(size_t)q * K + k];
-                const double hn = std::sqrt(std::max(0.0, nw[k].real()));
+                for (int q = 0; q <= j; ++q)
+                    Hk[(size_t)q * m + j] = h1[(size_t)q * K + k] + (again ? h2[(size_t)q * K + k] : cd(0.0));
+                const double hn = std::sqrt(std::max(0.0, nrm2[k]));
                 Hk[(size_t)(j + 1) * m + j] = hn;
                 inv[k] = hn > 1e-30 * beta[k] ? 1.0 / hn : 0.0;
                 // previous rotations on column j

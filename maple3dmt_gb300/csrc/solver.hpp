@@ -300,7 +300,8 @@ private:
     void collect_finish(const double2* x, int K);
     void net_apply(const KrylovCtx<float>& c32, const float2* v, float2* z, int K, const int* fmap);
     void ensure_fgmres(int K, int m);
-    void fg_mdot(const float2* V, int nv, const float2* w, int K, std::vector<std::complex<double>>& h);
+    void fg_mdot(const float2* V, int nv, const float2* w, int K, std::vector<std::complex<double>>& h,
+                 bool with_self = false);
     BatchResult solve_batch_fgmres(int K, const int* fmap, double2* b, double2* x, const std::vector<int>& active,
                                    double tol, int maxiter);
     void sync();

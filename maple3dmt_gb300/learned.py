@@ -79,3 +79,39 @@ class Cnn:
         loss = C.c_double()
         self._ck(self.lib.m3d_cnn_train_step(self.h, px, pt, n, D, H, W, float(lr), C.byref(loss)))
         return loss.value
+
+
+def _main(argv=None):
+    """Runs the default network (6 layers, 32 channels, 8 -> 6 channels) on a
+    batch of 16 grids of 32^3 cells: forward passes and Adam steps through the
+    C ABI, wall-clock per call (host copies included).  The tensor-core
+    kernels' own times come from the profiler."""
+    import argparse
+    import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=16)
+    ap.add_argument("--grid", type=int, default=32)
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args(argv)
+    net = Cnn(layers=6, c_in=8, hidden=32, c_out=6, seed=1)
+    rng = np.random.default_rng(0)
+    g = a.grid
+    x = rng.normal(size=(a.n, g, g, g, 8)).astype(np.float32)
+    t = rng.normal(size=(a.n, g, g, g, 6)).astype(np.float32)
+    net.forward(x)
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        net.forward(x)
+    tf = (time.perf_counter() - t0) / a.reps
+    net.train_step(x, t)
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        loss = net.train_step(x, t)
+    tt = (time.perf_counter() - t0) / a.reps
+    flop = 2.0 * a.n * g ** 3 * 32 * 27 * 32 * 6
+    print(f"forward {tf * 1e3:.2f} ms, train step {tt * 1e3:.2f} ms per call (host copies included); "
+          f"{flop / 1e9:.1f} GFLOP per forward; loss {loss:.3f}")
+
+
+if __name__ == "__main__":
+    _main()
