@@ -54,9 +54,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c2", "c5"],
-                    help="c2: the headline workload; c5: the inversion iteration at scale (levels 6/8, "
+    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
+                    help="c2: the headline workload; c3: one mesh per frequency (16 meshes of 0.9-3.0 M "
+                         "edges, 0.001-1000 Hz), forward + per-station adjoint gradients, meshes run "
+                         "concurrently; c5: the inversion iteration at scale (levels 6/8, "
                          "3.1 M edges, 400 stations, 24 frequencies 0.001-1000 Hz, data from a random model)")
+    ap.add_argument("--c3-freqs", type=int, default=16, help="c3: frequencies (meshes) of the 16, evenly spread")
+    ap.add_argument("--c3-sources", type=int, default=8,
+                    help="c3: station sources per mesh (2 adjoint solves each; the full workload has 121)")
+    ap.add_argument("--c3-concurrent", type=int, default=4, help="c3: meshes run at once (0: all)")
     # profiling runs only: a smaller mesh of the same survey (octree levels)
     ap.add_argument("--min-level", type=int, default=0, help="override the configuration's min octree level")
     ap.add_argument("--max-level", type=int, default=0, help="override the configuration's max octree level")
@@ -86,6 +92,14 @@ def parse():
     ap.add_argument("--inner-tol-floor", type=float, default=3e-5)
     ap.add_argument("--residual-replacement", type=int, default=0, choices=[0, 1])
     ap.add_argument("--gradcorr-overlap", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--sweep-rows", type=int, default=0,
+                    help="SSOR ordering by (super-block, colour), super-blocks of about this many edges (0: off)")
+    ap.add_argument("--coop-sweep", type=int, default=0, choices=[0, 1],
+                    help="1: each staged SSOR sweep as one cooperative launch over its groups")
+    ap.add_argument("--learned-steps", type=int, default=1,
+                    help="timed steps of the learned arm (FGMRES with the trained network; 0: skip)")
+    ap.add_argument("--learned-pairs", type=int, default=1024, help="training pairs the learned arm collects")
+    ap.add_argument("--fgmres-m", type=int, default=40, help="FGMRES restart length of the learned arm")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-procs", type=int, default=0, help="CPU worker processes (0: all host cores)")
     return ap.parse_args()
@@ -373,7 +387,8 @@ def solver_params(args, plain):
                  gradcorr=args.gradcorr, gradcorr_fmax=args.gradcorr_fmax,
                  gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
                  inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
-                 gradcorr_overlap=args.gradcorr_overlap)
+                 gradcorr_overlap=args.gradcorr_overlap, sweep_rows=args.sweep_rows,
+                 coop_sweep=args.coop_sweep)
     return p
 
 
@@ -395,7 +410,8 @@ def solver_label(args, p, freqs):
             "gradcorr": (f"multigrid gradient-space term, V({p['gradcorr_presmooth']},1)"
                          + (", V-cycle on a second stream" if p["gradcorr_overlap"] else "")) if p["gradcorr"]
             else "off",
-            "residual_replacement": bool(p["residual_replacement"])}
+            "residual_replacement": bool(p["residual_replacement"]),
+            "sweep_rows": p["sweep_rows"], "coop_sweep": bool(p["coop_sweep"])}
 
 
 def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False):
@@ -477,6 +493,40 @@ def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, pe
                 iters=iters, stats=stats)
 
 
+def run_learned(args, sv, obs, err, local_rank):
+    """The learned arm on the same step: a 6-layer 32-channel network on a
+    32^3 grid, trained on the GPU from (residual -> error) pairs that the
+    plain FP64 SSOR-BiCGStab records while solving the step's frequencies
+    from 0.5 Hz up (untimed, reported), then the step with flexible GMRES
+    whose every second direction is the two-level step with the network as
+    coarse solve, and the same FGMRES without the network (the gain)."""
+    from maple3dmt_gb300.solver import solver_for_survey
+    p = solver_params(args, False)
+    p.update(krylov=1, fgmres_m=args.fgmres_m, learned_period=2)
+    s = solver_for_survey(sv, device=local_rank, **p)
+    try:
+        t0 = time.perf_counter()
+        s.learn_setup(grid_level=5, layers=6, hidden=32, seed=1, max_samples=args.learned_pairs)
+        n = s.learn_collect(sv.freqs[sv.freqs >= 0.5])
+        t1 = time.perf_counter()
+        hist, val = s.learn_train(epochs=4, lr=1e-3, batch=16, seed=3, val_frac=0.1)
+        t2 = time.perf_counter()
+        out = {"unit": UNIT, "steps": args.learned_steps, "warmup": 1, "network": "6 x conv3x3x3, 32 channels, "
+               "BF16 tcgen05 kernels, 32^3 grid", "krylov": f"FGMRES({args.fgmres_m}), network every 2nd direction",
+               "pairs": n, "collect_s": t1 - t0, "train_s": t2 - t1, "train_loss": [hist[0], hist[-1]],
+               "held_out_loss": val}
+        for period, key in ((2, "with_network"), (0, "without_network")):
+            s.set_params(learned_period=period)
+            r = run_steps(s, sv, obs, err, args.learned_steps if period else 1, 1 if period else 0, 0, 1, None)
+            out[key] = {"value": r["solves"] / r["t_dev"], "ms_per_step": r["t_dev"] * 1000.0 / max(1, len(r["iters"])),
+                        "krylov_iterations_per_step": statistics.mean(r["iters"]),
+                        "rhs_at_tol": r["stats"]["rhs_at_tol"], "rhs_reported": r["stats"]["rhs_reported"]}
+        out["value"] = out["with_network"]["value"]
+        return out
+    finally:
+        s.close()
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     from maple3dmt_gb300 import mesh
@@ -525,6 +575,12 @@ def run_ours(args, rank, world, local_rank):
                  "true_residual_max": rp["stats"]["true_residual_max"],
                  "krylov_iterations_per_step": statistics.mean(rp["iters"]), **solver_label(args, pp, sv.freqs)}
         sp_.close()
+    learned = None
+    if not plain_main and args.learned_steps > 0 and world == 1 and CONFIG == "c2":
+        try:
+            learned = run_learned(args, sv, obs, err, local_rank)
+        except Exception as exc:  # the learned arm must not hide the headline number
+            learned = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:
         return
     value = solves / t_dev
@@ -560,6 +616,7 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "plain": plain,
         "batched_over_plain": value / plain["value"] if plain else None,
+        "learned": learned,
         "roofline": {"bound": "hbm", "kernel": dom, "launches": "K=16" if src is b16 else "all",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind, "traffic": traffic, "achieved_all_widths": achieved_all},
@@ -581,6 +638,85 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+def run_c3(args, rank, world, local_rank):
+    """C3: one mesh per frequency (skin-depth refinement per frequency, so the
+    meshes differ in size), the C2 earth with seeded log-normal noise, 121
+    stations.  A step is, for every mesh, the forward solve of both
+    polarisations and the per-station adjoint gradients of --c3-sources
+    station sources (two adjoint solves each), all meshes through one
+    m3d_group_station_gradients call that runs them concurrently on the
+    device.  The work spans one CUDA stream per mesh, so the step is timed by
+    the host clock between device synchronisations (the call returns after
+    every mesh's results are on the host); host copies are inside."""
+    import numpy as np
+    from maple3dmt_gb300 import mesh, workloads
+    from maple3dmt_gb300.solver import group_station_gradients, solver_for_survey
+    if world > 1:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "unavailable": "c3 runs on one GPU"}), flush=True)
+        return
+    allf = np.asarray(workloads.C3.freqs)
+    idx = np.unique(np.round(np.linspace(0, len(allf) - 1, max(1, min(args.c3_freqs, len(allf))))).astype(int))
+    freqs = allf[idx]
+    t0 = time.perf_counter()
+    svs = mesh.c3_surveys(freqs)
+    p = solver_params(args, False)
+    solvers = [solver_for_survey(sv, device=local_rank, **p) for sv in svs]
+    setup_s = time.perf_counter() - t0
+    rng = np.random.default_rng(42)
+    wr = [workloads.station_sources(s.ns, rng)[:args.c3_sources] for s in solvers]
+    n_solves = sum(2 + 2 * w.shape[0] for w in wr)
+    clocks = ClockSampler(local_rank)
+
+    def step():
+        return group_station_gradients(solvers, freqs, wr, max_concurrent=args.c3_concurrent)
+
+    for _ in range(args.warmup):
+        step()
+    clocks.start()
+    launches0 = sum(s.stats()["kernel_launches"] for s in solvers)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    sts = [s.stats() for s in solvers]
+    launches = sum(st["kernel_launches"] for st in sts) - launches0
+    tr = [t for st in sts for t in st["true_residual"][:st["n_rhs"]]]
+    total = sum(times)
+    # the sequential schedule of the same handles (one mesh at a time) for comparison
+    t = time.perf_counter()
+    group_station_gradients(solvers, freqs, wr, max_concurrent=1)
+    one_at_a_time = n_solves / (time.perf_counter() - t)
+    ne = [s.ne for s in solvers]
+    h2d = sum(w.size * 16 for w in wr)
+    d2h = sum(s.ns * 4 * 16 + w.shape[0] * s.nc * 8 for w, s in zip(wr, solvers))
+    line = {
+        "metric": METRIC, "value": n_solves * args.steps / total, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total * 1000.0 / args.steps, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "c64+c128", "data": "synthetic",
+        "config": {"workload": f"C3: one mesh per frequency ({len(freqs)} of 16 frequencies "
+                               f"{freqs.min():g}-{freqs.max():g} Hz, {min(ne)}-{max(ne)} edges), C2 earth with "
+                               f"log10 sigma + N(0, 0.3^2), 121 stations; per mesh 2 forward + "
+                               f"{2 * args.c3_sources} station adjoint solves ({args.c3_sources} station sources) "
+                               f"and their per-station gradients ({n_solves} solves per step)",
+                   "tol": TOL, "edges_per_mesh": ne, "meshes_at_once": args.c3_concurrent,
+                   "timing": "host clock between device synchronisations (one stream per mesh)",
+                   "l2": "inputs larger than L2"},
+        "solver": {**solver_label(args, p, freqs), "parallelism": "meshes run concurrently, one host thread and "
+                                                                   "CUDA stream per mesh"},
+        "e2e": {"value": n_solves * args.steps / total, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "one_mesh_at_a_time": {"value": one_at_a_time, "unit": UNIT},
+        "rhs_at_tol": sum(1 for t in tr if t <= TOL), "rhs_reported": len(tr),
+        "setup_s": setup_s, "gpu_launches": launches, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    for s in solvers:
+        s.close()
+
+
 def main():
     global CONFIG, LEVELS
     args = parse()
@@ -595,6 +731,8 @@ def main():
         dist.init_process_group("gloo", rank=rank, world_size=world)
     if args.impl == "reference":
         run_reference_arm(args, rank, world)
+    elif CONFIG == "c3":
+        run_c3(args, rank, world, local_rank)
     else:
         run_ours(args, rank, world, local_rank)
     if world > 1:

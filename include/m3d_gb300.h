@@ -145,6 +145,10 @@ typedef struct m3d_params {
     int fgmres_m;             /* FGMRES restart length (20) */
     int learned_period;       /* with krylov = 1 and a trained network (m3d_learn_*): every learned_period-th
                                  FGMRES direction comes from the network instead of SSOR (0: never; 2) */
+    int sweep_rows;           /* SSOR ordering (super-block, colour) with super-blocks of about sweep_rows
+                                 edges, so a sweep's gathers stay in L2; 0: colour order over the mesh */
+    int coop_sweep;           /* 1: each staged SSOR sweep is one cooperative launch over all its groups
+                                 (bounded grid barriers between groups); 0: one launch per group */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -212,6 +216,35 @@ int m3d_solve_rhs(m3d_solver* s, const double* rhs, double* x);
  * station and polarisation) as multi-RHS solves.  rhs, out [n_rhs][n_edges]
  * complex; stats cover every right-hand side (first 64). */
 int m3d_solve_rhs_batch(m3d_solver* s, const double* rhs, int n_rhs, double* out);
+/* Gradients of n_src residual sources at the solved single frequency
+ * (m3d_compute_single_frequency first), one per source: for source j,
+ * build_adjoint_rhs_from_residual (:1804-2013) of wr[j], both adjoint solves
+ * (adjoint_solve_complex, :914-924) and compute_sensitivity_complex
+ * (:989-1059) of each polarisation, summed over the two polarisations as
+ * InversionFV::compute_gradient_ sums them (src/inversion/inversion_fv.cpp:
+ * 280-290).  With wr[j] non-zero at one station, g[j] is that station's row
+ * of J^T W^2 r.  Built, solved (eight sources, sixteen right-hand sides per
+ * batched solve) and reduced on the device.  wr [n_src][n_stations][4]
+ * complex, g [n_src][n_cells]; stats cover every right-hand side (first 64). */
+int m3d_station_gradients(m3d_solver* s, const double* wr, int n_src, double* g);
+/* Per-frequency meshes of uneven size (one handle per frequency mesh, each
+ * set up, with conductivity and stations, all on one device), run
+ * concurrently: one host thread per handle, each on its handle's own CUDA
+ * stream, started in decreasing order of stiffness entries, at most
+ * max_concurrent at once
+ * (0: all).  For mesh m: m3d_compute_single_frequency(freqs[m]) -> Z_out[m]
+ * [n_stations][4] (Z_out or Z_out[m] nullable), then
+ * m3d_station_gradients(wr[m], n_src[m]) -> g_out[m] [n_src[m]][n_cells(m)].
+ * The GPU counterpart of the reference's per-frequency loop
+ * (src/inversion/inversion_fv.cpp:250-291) and of its frequency-parallel
+ * manager (src/utils/freq_parallel.cpp:99-195) on one device.  status[m]
+ * gets mesh m's return code (m3d_last_error(handles[m]) its message); the
+ * call returns the first non-zero status in mesh order, M3D_OK if none.
+ * The handles must be distinct and must not be used by other threads
+ * during the call. */
+int m3d_group_station_gradients(m3d_solver* const* handles, int n_meshes, const double* freqs,
+                                const double* const* wr, const int* n_src, double* const* Z_out,
+                                double* const* g_out, int max_concurrent, int* status);
 /* compute_sensitivity_complex (:1778-1782 -> :989-1059): g [n_cells]. */
 int m3d_compute_sensitivity(m3d_solver* s, const double* E, const double* lambda, double* g);
 /* build_perturbation_rhs_complex (:1787-1791 -> :945-984): pol 1 or 2. */

@@ -128,6 +128,24 @@ public:
         return g;
     }
 
+    // ---- per-source gradients at the solved frequency (one row of J^T W^2 r per station source) ----
+    // wr: [source][station] residual weights; returns [source][cell]
+    std::vector<RealVec> station_gradients(const std::vector<std::vector<std::array<Complex, 4>>>& wr) {
+        const int n = (int)wr.size();
+        std::vector<std::array<Complex, 4>> flat;
+        flat.reserve((size_t)n * ns_);
+        for (const auto& w : wr) {
+            if ((int)w.size() != ns_) throw SolverError(M3D_ERR_ARG, "station_gradients: one entry per station");
+            flat.insert(flat.end(), w.begin(), w.end());
+        }
+        RealVec g((size_t)n * nc_, 0.0);
+        check(m3d_station_gradients(h_, reinterpret_cast<const double*>(flat.data()), n, g.data()),
+              "station_gradients");
+        std::vector<RealVec> out(n);
+        for (int j = 0; j < n; ++j) out[j].assign(g.begin() + (size_t)j * nc_, g.begin() + (size_t)(j + 1) * nc_);
+        return out;
+    }
+
     // ---- GN-CG J^T W^2 J v (ImplicitJtJOperatorFV::Mult, data term) ----
     // after forward_batch(freqs) (the cached background fields); err: [station][freq][4]
     RealVec jtjv(const RealVec& freqs, const RealVec& dsigma, const RealVec& err, double inner_tol = 1e-4) {

@@ -37,6 +37,8 @@ class Params(C.Structure):
         ("krylov", C.c_int),
         ("fgmres_m", C.c_int),
         ("learned_period", C.c_int),
+        ("sweep_rows", C.c_int),
+        ("coop_sweep", C.c_int),
     ]
 
 
@@ -97,7 +99,8 @@ SOLVER_SYMBOLS = [
     "m3d_factorize_frequency", "m3d_release_factorization", "m3d_background_E",
     "m3d_set_background_fields", "m3d_build_adjoint_rhs", "m3d_adjoint_solve", "m3d_solve_rhs",
     "m3d_compute_sensitivity", "m3d_build_perturbation_rhs", "m3d_extract_delta_impedance",
-    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_solve_rhs_batch", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
+    "m3d_forward_batch", "m3d_gradient_batch", "m3d_jtjv_batch", "m3d_solve_rhs_batch", "m3d_station_gradients",
+    "m3d_group_station_gradients", "m3d_reg_setup", "m3d_reg_num_active", "m3d_reg_active_to_global",
     "m3d_reg_apply_wtw", "m3d_reg_apply_cmcmt", "m3d_reg_diagonal_wtw", "m3d_reg_evaluate", "m3d_dot_batched", "m3d_dot_batched_noalloc", "m3d_get_stats",
     "m3d_timer_start", "m3d_timer_stop", "m3d_set_kernel_timing", "m3d_get_kernel_times",
     "m3d_test_set_consume_no_wait", "m3d_autotune",
@@ -128,6 +131,10 @@ def declare(lib) -> None:
     _fn(lib, "m3d_adjoint_solve", C.c_int, [vp, c_double_p, c_double_p])
     _fn(lib, "m3d_solve_rhs", C.c_int, [vp, c_double_p, c_double_p])
     _fn(lib, "m3d_solve_rhs_batch", C.c_int, [vp, c_double_p, C.c_int, c_double_p])
+    _fn(lib, "m3d_station_gradients", C.c_int, [vp, c_double_p, C.c_int, c_double_p])
+    _fn(lib, "m3d_group_station_gradients", C.c_int,
+        [C.POINTER(vp), C.c_int, c_double_p, C.POINTER(c_double_p), C.POINTER(C.c_int),
+         C.POINTER(c_double_p), C.POINTER(c_double_p), C.c_int, C.POINTER(C.c_int)])
     _fn(lib, "m3d_compute_sensitivity", C.c_int, [vp, c_double_p, c_double_p, c_double_p])
     _fn(lib, "m3d_build_perturbation_rhs", C.c_int, [vp, C.c_int, c_double_p, c_double_p])
     _fn(lib, "m3d_extract_delta_impedance", C.c_int, [vp, c_double_p, C.c_int, c_double_p])

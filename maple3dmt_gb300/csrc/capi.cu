@@ -5,11 +5,13 @@
 
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <stdexcept>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -100,6 +102,8 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->krylov = 0;
     p->fgmres_m = 20;
     p->learned_period = 2;
+    p->sweep_rows = 0;
+    p->coop_sweep = 0;
 }
 
 extern "C" int m3d_solver_create(int device, m3d_solver** out) {
@@ -137,7 +141,8 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
         params->divcorr_mixed < 0 || params->divcorr_mixed > 1 || !(params->inner_tol_floor > 0.0) ||
         params->inner_tol_floor >= 1.0 || params->residual_replacement < 0 || params->residual_replacement > 1 ||
         params->gradcorr_overlap < 0 || params->gradcorr_overlap > 1 || params->krylov < 0 ||
-        params->krylov > 1 || params->fgmres_m < 2 || params->fgmres_m > 47 || params->learned_period < 0)
+        params->krylov > 1 || params->fgmres_m < 2 || params->fgmres_m > 47 || params->learned_period < 0 || params->sweep_rows < 0 ||
+        params->coop_sweep < 0 || params->coop_sweep > 1)
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
 }
@@ -240,6 +245,70 @@ extern "C" int m3d_solve_rhs_batch(m3d_solver* h, const double* rhs, int n_rhs, 
     if (!all_finite(rhs, edge_doubles(h) * (size_t)n_rhs))
         return fail(h, M3D_ERR_NUMERIC, "non-finite value in a right-hand side");
     return guarded(h, [&](m3d::GpuSolver& s) { s.solve_rhs_batch(rhs, n_rhs, out); });
+}
+
+extern "C" int m3d_station_gradients(m3d_solver* h, const double* wr, int n_src, double* g) {
+    if (!ready(h)) return fail(h, M3D_ERR_STATE, "solver not set up");
+    if (n_src < 0 || (n_src > 0 && (!wr || !g))) return fail(h, M3D_ERR_ARG, "null buffer or n_src < 0");
+    if (n_src > 0 && !all_finite(wr, (size_t)n_src * h->s->n_stations() * 8))
+        return fail(h, M3D_ERR_NUMERIC, "non-finite value in a residual source");
+    return guarded(h, [&](m3d::GpuSolver& s) { s.station_gradients(wr, n_src, g); });
+}
+
+extern "C" int m3d_group_station_gradients(m3d_solver* const* handles, int n_meshes, const double* freqs,
+                                           const double* const* wr, const int* n_src, double* const* Z_out,
+                                           double* const* g_out, int max_concurrent, int* status) {
+    if (!handles || n_meshes < 1 || !freqs || !wr || !n_src || !g_out || !status) return M3D_ERR_ARG;
+    for (int m = 0; m < n_meshes; ++m) status[m] = M3D_OK;
+    for (int m = 0; m < n_meshes; ++m) {
+        if (!ready(handles[m])) status[m] = fail(handles[m], M3D_ERR_STATE, "solver not set up");
+        for (int q = 0; q < m; ++q)
+            if (handles[q] == handles[m]) status[m] = fail(handles[m], M3D_ERR_ARG, "handle repeated in the group");
+    }
+    for (int m = 0; m < n_meshes; ++m)
+        if (status[m] != M3D_OK) return status[m];
+    // most stiffness entries first, so the long solves start early and the
+    // small ones fill in behind them
+    std::vector<int> order(n_meshes);
+    for (int m = 0; m < n_meshes; ++m) order[m] = m;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return handles[a]->s->nnz_off > handles[b]->s->nnz_off;
+    });
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n_meshes) return;
+            const int m = order[i];
+            m3d_solver* h = handles[m];
+            if (cudaSetDevice(h->s->device) != cudaSuccess) {
+                cudaGetLastError();
+                status[m] = fail(h, M3D_ERR_CUDA, "cudaSetDevice failed");
+                continue;
+            }
+            std::vector<double> z;
+            double* zp = Z_out ? Z_out[m] : nullptr;
+            if (!zp) {
+                z.resize((size_t)std::max(1, h->s->n_stations()) * 8);
+                zp = z.data();
+            }
+            int rc = m3d_compute_single_frequency(h, freqs[m], zp);
+            if (rc == M3D_OK) rc = m3d_station_gradients(h, wr[m], n_src[m], g_out[m]);
+            status[m] = rc;
+        }
+    };
+    const int nw = max_concurrent > 0 ? std::min(max_concurrent, n_meshes) : n_meshes;
+    std::vector<std::thread> pool;
+    try {
+        for (int w = 1; w < nw; ++w) pool.emplace_back(worker);
+    } catch (...) {
+        // fewer threads than asked: the ones started and this one share the work
+    }
+    worker();
+    for (auto& t : pool) t.join();
+    for (int m = 0; m < n_meshes; ++m)
+        if (status[m] != M3D_OK) return status[m];
+    return M3D_OK;
 }
 
 extern "C" int m3d_solve_rhs(m3d_solver* h, const double* rhs, double* x) {

@@ -7,6 +7,7 @@
 #include <map>
 #include <mutex>
 #include <stdexcept>
+#include <string>
 #include <tuple>
 #include <type_traits>
 #include <utility>
@@ -433,81 +434,173 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
 // SSOR forward sweep of one colour over slice-staged lower parts
 // (ssor.h:58-66); items work_col[0..count) of the colour.
 template <class R, int K>
+__device__ __forceinline__ void ssor_fwd_rows(const SegItem& it, const unsigned char* base, const DiagView<R>& D,
+                                              R om, int rhs, int lr0, const cplx<R>* __restrict__ in, cplx<R>* y) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    SegRows<R> lo;
+    lo.bind(base);
+    // every pass's gathers are issued before the first row is written
+    RowHead<R, K> h[Sh::PASSES];
+    C iv[Sh::PASSES], dv[Sh::PASSES];
+#pragma unroll
+    for (int ps = 0; ps < Sh::PASSES; ++ps) {
+        const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+        const int row = it.slice * kSlice + lr;
+        iv[ps] = in[(size_t)row * K + rhs];
+        dv[ps] = diag_of(D, row, om);
+        h[ps].load(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs);
+    }
+#pragma unroll
+    for (int ps = 0; ps < Sh::PASSES; ++ps) {
+        const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+        const int row = it.slice * kSlice + lr;
+        C s = h[ps].sum(cm<R>(0, 0));
+        const int b = lo.begin_of(lr) + 8, e = lo.end[lr];
+        if (b < e) s = seg_row_dot<R, K>(lo.col, lo.val, b, e, y, rhs, s);
+        y[(size_t)row * K + rhs] = cmul(csub(iv[ps], s), inv_c(dv[ps]));
+    }
+}
+
+// SSOR forward sweep of one colour over slice-staged lower parts (ssor.h:58-66).
+template <class R, int K>
 __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_fwd_st(SegView<R> S, const int4* __restrict__ work,
                                                                     int count, DiagView<R> D, BatchView B,
                                                                     const cplx<R>* __restrict__ in, cplx<R>* y) {
-    using C = cplx<R>;
-    using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int rhs = lane % K;
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
     slice_pipeline<1>(S.seg, work, count, S.stage_lo, S.err, [&](const SegItem& it, const unsigned char* base) {
-        SegRows<R> lo;
-        lo.bind(base);
-#pragma unroll
-        for (int ps = 0; ps < Sh::PASSES; ++ps) {
-            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
-            const int row = it.slice * kSlice + lr;
-            const size_t i = (size_t)row * K + rhs;
-            const C iv = in[i];
-            const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs, cm<R>(0, 0));
-            y[i] = cmul(csub(iv, s), inv_c(d));
-        }
+        ssor_fwd_rows<R, K>(it, base, D, om, rhs, lr0, in, y);
     });
 }
 
-// SSOR backward sweep of one colour over slice-staged upper parts (ssor.h:69-78).
-// GC: the preconditioner's gradient-space term c = G~ y0 / (i omega) is added
-// to the written row, out_i = w_i + c_i; the sweep then keeps w in y (in
-// place of the forward result, read once per row before it is replaced) and
-// gathers the later colours' w from there.
+// The backward rows of one staged slice (ssor.h:69-78).  GC: the
+// preconditioner's gradient-space term c = G~ y0 / (i omega) is added to the
+// written row, out_i = w_i + c_i; the sweep then keeps w in y (in place of the
+// forward result, read once per row before it is replaced) and gathers the
+// later colours' w from there.
+template <class R, int K, bool GC>
+__device__ __forceinline__ void ssor_bwd_rows(const SegItem& it, const unsigned char* base, const DiagView<R>& D,
+                                              R om, int rhs, int lr0, cplx<R>* y, cplx<R>* out,
+                                              const GcRowTerm& gt) {
+    using C = cplx<R>;
+    using Sh = StagedShape<K>;
+    constexpr int NP = Sh::PASSES;
+    SegRows<R> up;
+    up.bind(base);
+    // every pass's loads (the term's node indices first, the row gathers, then
+    // the node values) are issued before the first row is written
+    int n0[NP], n1[NP];
+    if (GC) {
+#pragma unroll
+        for (int ps = 0; ps < NP; ++ps) {
+            const int row = it.slice * kSlice + ps * Sh::ROWS_PER_PASS + lr0;
+            n0[ps] = __ldg(&gt.e_node[2 * row]);
+            n1[ps] = __ldg(&gt.e_node[2 * row + 1]);
+        }
+    }
+    RowHead<R, K> h[NP];
+    C yv[NP], dv[NP];
+#pragma unroll
+    for (int ps = 0; ps < NP; ++ps) {
+        const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+        const int row = it.slice * kSlice + lr;
+        yv[ps] = y[(size_t)row * K + rhs];
+        dv[ps] = diag_of(D, row, om);
+        h[ps].load(up.col, up.val, up.begin_of(lr), up.end[lr], GC ? y : out, rhs);
+    }
+    float g0[NP], g1[NP];
+    float2 ya[NP], yb[NP];
+#pragma unroll
+    for (int ps = 0; ps < NP; ++ps) {
+        g0[ps] = g1[ps] = 0.0f;
+        ya[ps] = yb[ps] = make_float2(0.0f, 0.0f);
+        if (GC) {
+            const int row = it.slice * kSlice + ps * Sh::ROWS_PER_PASS + lr0;
+            g0[ps] = __ldg(&gt.e_g[2 * row]);
+            g1[ps] = __ldg(&gt.e_g[2 * row + 1]);
+            ya[ps] = gt.ya[(size_t)n0[ps] * K + rhs];
+            yb[ps] = gt.ya[(size_t)n1[ps] * K + rhs];
+        }
+    }
+#pragma unroll
+    for (int ps = 0; ps < NP; ++ps) {
+        const int lr = ps * Sh::ROWS_PER_PASS + lr0;
+        const int row = it.slice * kSlice + lr;
+        const size_t i = (size_t)row * K + rhs;
+        C s = h[ps].sum(cm<R>(0, 0));
+        const int b = up.begin_of(lr) + 8, e = up.end[lr];
+        if (b < e) s = seg_row_dot<R, K>(up.col, up.val, b, e, GC ? y : out, rhs, s);
+        const C w = csub(yv[ps], cmul(s, inv_c(dv[ps])));
+        if (GC) {
+            y[i] = w;
+            const float sc = gt.s[rhs];
+            const float gx = g0[ps] * ya[ps].x + g1[ps] * yb[ps].x, gy = g0[ps] * ya[ps].y + g1[ps] * yb[ps].y;
+            out[i] = cm<R>(w.x + (R)(sc * gy), w.y - (R)(sc * gx));
+        } else {
+            out[i] = w;
+        }
+    }
+}
+
+// SSOR backward sweep of one colour over slice-staged upper parts.
 template <class R, int K, bool GC>
 __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_bwd_st(SegView<R> S, const int4* __restrict__ work,
                                                                     int count, DiagView<R> D, BatchView B,
                                                                     cplx<R>* y, cplx<R>* out, GcRowTerm gt) {
-    using C = cplx<R>;
-    using Sh = StagedShape<K>;
     constexpr int RPW = Rpw<K>::v;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int rhs = lane % K;
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
     slice_pipeline<2>(S.seg, work, count, S.stage_up, S.err, [&](const SegItem& it, const unsigned char* base) {
-        SegRows<R> up;
-        up.bind(base);
-#pragma unroll
-        for (int ps = 0; ps < Sh::PASSES; ++ps) {
-            const int lr = ps * Sh::ROWS_PER_PASS + lr0;
-            const int row = it.slice * kSlice + lr;
-            const size_t i = (size_t)row * K + rhs;
-            // the term's node values are loaded ahead of the row's gathers
-            float g0 = 0.0f, g1 = 0.0f;
-            float2 ya = make_float2(0.0f, 0.0f), yb = ya;
-            if (GC) {
-                g0 = __ldg(&gt.e_g[2 * row]);
-                g1 = __ldg(&gt.e_g[2 * row + 1]);
-                const int n0 = __ldg(&gt.e_node[2 * row]), n1 = __ldg(&gt.e_node[2 * row + 1]);
-                ya = gt.ya[(size_t)n0 * K + rhs];
-                yb = gt.ya[(size_t)n1 * K + rhs];
-            }
-            const C yv = y[i];
-            const C d = diag_of(D, row, om);
-            const C s = seg_row_dot<R, K>(up.col, up.val, up.begin_of(lr), up.end[lr], GC ? y : out, rhs,
-                                          cm<R>(0, 0));
-            const C w = csub(yv, cmul(s, inv_c(d)));
-            if (GC) {
-                y[i] = w;
-                const float sc = gt.s[rhs];
-                const float gx = g0 * ya.x + g1 * yb.x, gy = g0 * ya.y + g1 * yb.y;
-                out[i] = cm<R>(w.x + (R)(sc * gy), w.y - (R)(sc * gx));
-            } else {
-                out[i] = w;
-            }
-        }
+        ssor_bwd_rows<R, K, GC>(it, base, D, om, rhs, lr0, y, out, gt);
     });
+}
+
+// Whole sweeps in one cooperative launch: the sweep groups (colours, or
+// (super-block, colour) pairs) one after another, a grid barrier between
+// groups in place of a kernel boundary.  gptr: device copy of the groups'
+// slice ranges; bar: the barrier's counter and generation.
+template <class R, int K>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_fwd_coop(
+    SegView<R> S, const int4* __restrict__ work, const int* __restrict__ gptr, int n_groups, DiagView<R> D,
+    BatchView B, const cplx<R>* __restrict__ in, cplx<R>* y, unsigned* bar) {
+    constexpr int RPW = Rpw<K>::v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    for (int g = 0; g < n_groups; ++g) {
+        if (g > 0) grid_barrier(bar, bar + 1, S.err);
+        const int s0 = gptr[g], s1 = gptr[g + 1];
+        slice_pipeline<1>(S.seg, work + s0, s1 - s0, S.stage_lo, S.err,
+                          [&](const SegItem& it, const unsigned char* base) {
+                              ssor_fwd_rows<R, K>(it, base, D, om, rhs, lr0, in, y);
+                          });
+    }
+}
+
+template <class R, int K, bool GC>
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_ssor_bwd_coop(
+    SegView<R> S, const int4* __restrict__ work, const int* __restrict__ gptr, int n_groups, DiagView<R> D,
+    BatchView B, cplx<R>* y, cplx<R>* out, GcRowTerm gt, unsigned* bar) {
+    constexpr int RPW = Rpw<K>::v;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rhs = lane % K;
+    const int lr0 = warp * RPW + lane / K;
+    const R om = (R)B.omega[rhs];
+    for (int g = n_groups - 1; g >= 0; --g) {
+        if (g < n_groups - 1) grid_barrier(bar, bar + 1, S.err);
+        const int s0 = gptr[g], s1 = gptr[g + 1];
+        slice_pipeline<2>(S.seg, work + s0, s1 - s0, S.stage_up, S.err,
+                          [&](const SegItem& it, const unsigned char* base) {
+                              ssor_bwd_rows<R, K, GC>(it, base, D, om, rhs, lr0, y, out, gt);
+                          });
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -727,6 +820,27 @@ __global__ void __launch_bounds__(kBlock) k_add_gc_term(long n, cplx<R>* __restr
     out[i] = o;
 }
 
+// Blocks of a cooperative launch: every block resident at once (the
+// occupancy of the kernel at this shared memory on every SM), less a quarter
+// when another stream's kernels should run beside it.
+inline int coop_grid(const void* kernel, int nt, int smem, bool share) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, nt, smem);
+    const int full = std::max(1, per_sm) * std::max(1, sms);
+    return share ? std::max(sms, full - full / 4) : full;
+}
+
+inline void cuda_check_launch(cudaError_t e, long long* launches) {
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error(std::string("cooperative sweep launch failed: ") + cudaGetErrorString(e));
+    }
+    if (launches) ++*launches;
+}
+
 template <class R, int K>
 void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, const GcRowTerm& gt = GcRowTerm{}) {
     constexpr int G = kSlice / Rpw<K>::v;   // row-group tasks per slice
@@ -747,6 +861,44 @@ void ssor_k(const KrylovCtx<R>& c, const cplx<R>* in, cplx<R>* y, cplx<R>* out, 
         cudaStreamWaitEvent(c.stream, c.gc_join, 0);
         th = c.timer ? c.timer->begin(kClsSsor, 0.0, K) : -1;
     };
+    if (c.row_kernels == kRowsStaged && c.coop && c.colour_ptr_d && c.gridbar && nc > 1) {
+        constexpr int NT = StagedShape<K>::NT;
+        // with the gradient-space V-cycle running beside the forward sweep,
+        // a quarter of the resident blocks is left to it
+        const bool share = gt.ya && c.gc_stream;
+        {
+            auto kf = k_ssor_fwd_coop<R, K>;
+            const int smem = 2 * c.seg.stage_lo;
+            const int grid = coop_grid(reinterpret_cast<const void*>(kf), NT, smem, share);
+            cudaMemsetAsync(c.gridbar, 0, sizeof(unsigned), c.stream);
+            void* args[] = {(void*)&c.seg, (void*)&c.seg.work_col, (void*)&c.colour_ptr_d, (void*)&nc,
+                            (void*)&c.D, (void*)&c.B, (void*)&in, (void*)&y, (void*)&c.gridbar};
+            cuda_check_launch(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kf), grid, NT, args, smem,
+                                                          c.stream), c.launches);
+        }
+        wait_join();
+        {
+            const int smem = 2 * c.seg.stage_up;
+            cudaMemsetAsync(c.gridbar, 0, sizeof(unsigned), c.stream);
+            if (gt.ya) {
+                auto kf = k_ssor_bwd_coop<R, K, true>;
+                const int grid = coop_grid(reinterpret_cast<const void*>(kf), NT, smem, false);
+                void* args[] = {(void*)&c.seg, (void*)&c.seg.work_col, (void*)&c.colour_ptr_d, (void*)&nc,
+                                (void*)&c.D, (void*)&c.B, (void*)&y, (void*)&out, (void*)&gt, (void*)&c.gridbar};
+                cuda_check_launch(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kf), grid, NT, args,
+                                                              smem, c.stream), c.launches);
+            } else {
+                auto kf = k_ssor_bwd_coop<R, K, false>;
+                const int grid = coop_grid(reinterpret_cast<const void*>(kf), NT, smem, false);
+                void* args[] = {(void*)&c.seg, (void*)&c.seg.work_col, (void*)&c.colour_ptr_d, (void*)&nc,
+                                (void*)&c.D, (void*)&c.B, (void*)&y, (void*)&out, (void*)&gt, (void*)&c.gridbar};
+                cuda_check_launch(cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kf), grid, NT, args,
+                                                              smem, c.stream), c.launches);
+            }
+        }
+        if (c.timer) c.timer->end(th);
+        return;
+    }
     if (c.row_kernels == kRowsStaged) {
         constexpr int NT = StagedShape<K>::NT;
         for (int col = 0; col < nc; ++col) {

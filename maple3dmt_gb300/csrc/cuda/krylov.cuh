@@ -157,6 +157,11 @@ struct KrylovCtx {
     // and joined before the backward sweep, overlapping the forward sweep
     cudaStream_t gc_stream = nullptr;
     cudaEvent_t gc_fork = nullptr, gc_join = nullptr;
+    // staged rows: each SSOR sweep as one cooperative launch over all sweep
+    // groups (grid barriers between groups) instead of one launch per group
+    int coop = 0;
+    const int* colour_ptr_d = nullptr;   // device copy of colour_ptr
+    unsigned* gridbar = nullptr;         // [2] barrier counter and generation
 };
 
 enum RowKernels : int { kRowsDirect = 0, kRowsStaged = 1 };

@@ -873,16 +873,19 @@ __global__ void k_wr(int ns, int nf, int nf_total, int f0, const double2* __rest
 }
 
 // forward_solver_fv.cpp:1837-2010, one thread per frequency (stations may share edges)
+// Thread f builds source f: wr[f] [ns][4], the station cache hcs[f * hc_stride]
+// and omegas[f * om_stride] (strides ns and 1 over frequencies, 0 and 0 for
+// many sources at one frequency), into lanes 2f and 2f + 1.
 __global__ void k_adjoint_rhs(StationDev st, const double2* __restrict__ wr, const HCache* __restrict__ hcs,
-                              const double* __restrict__ omegas, int nf, VecK out) {
+                              const double* __restrict__ omegas, int nf, int hc_stride, int om_stride, VecK out) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const int K = out.K;
-    const double2 iwmu = make_double2(0.0, omegas[f] * kMu0);
+    const double2 iwmu = make_double2(0.0, omegas[(size_t)f * om_stride] * kMu0);
     for (int s = 0; s < st.ns; ++s) {
         if (st.cell[s] < 0) continue;
         const double2* w = wr + ((size_t)f * st.ns + s) * 4;
-        const HCache hc = hcs[(size_t)f * st.ns + s];
+        const HCache hc = hcs[(size_t)f * hc_stride + s];
         if (hypot(hc.det.x, hc.det.y) < 1e-30) continue;
         const double2 sx1 = cdiv(csub(cmul(w[0], hc.Hy2), cmul(w[1], hc.Hx2)), hc.det);
         const double2 sy1 = cdiv(csub(cmul(w[2], hc.Hy2), cmul(w[3], hc.Hx2)), hc.det);
@@ -961,33 +964,79 @@ __global__ void k_adjoint_rhs(StationDev st, const double2* __restrict__ wr, con
     }
 }
 
-// one thread per cell, frequencies and polarisations summed in order
+// G consecutive threads per cell (G a power of two >= nf * npol, so a group
+// never straddles a warp), thread k of the group on lane k = npol * f + p:
+// each edge row of E and lambda (K lanes, interleaved) is read as one
+// contiguous segment, and the per-edge scalars are broadcast within the
+// group.  The group's lane terms -omega_f * Im(sum_e lambda_e E_e dMe) are
+// summed by a fixed shuffle tree, so the result is deterministic.
+// compute_sensitivity, forward_solver_fv.cpp:989-1059.
+template <int G>
 __global__ void k_sensitivity(MeshDev m, const double* __restrict__ sigma, VecK E, VecK lam,
                               const double* __restrict__ omegas, int nf, int npol, double* g) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= m.nc) return;
-    const double sc = sigma[c];
-    double acc = g[c];
-    for (int f = 0; f < nf; ++f) {
-        double gsum = 0.0;
-        for (int p = 0; p < npol; ++p) {
-            const int kE = npol * f + p;
-            double2 s = zero2();
+    const long total = ((long)m.nc * G + 31) / 32 * 32;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int nl = nf * npol;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int c = (int)(t / G);
+        const int k = (int)(t % G);
+        const bool live = c < m.nc;
+        double v = 0.0;
+        if (live && k < nl) {
+            const double sc = sigma[c];
+            double sy = 0.0;
             for (int q = m.cell_ptr[c]; q < m.cell_ptr[c + 1]; ++q) {
                 const int e = m.cell_edge[q];
                 if (m.flags[e] & kFlagSensFixed) continue;
                 const int na = m.nadj[e];
                 if (na == 0) continue;
                 const double dMe = sc * m.adual[e] * m.elen[e] / na;
-                const double2 le = cmul(lam.p[(size_t)e * lam.K + kE], E.p[(size_t)e * E.K + kE]);
-                s.x += le.x * dMe;
-                s.y += le.y * dMe;
+                const double2 le = cmul(lam.p[(size_t)e * lam.K + k], E.p[(size_t)e * E.K + k]);
+                sy += le.y * dMe;
             }
-            gsum += -omegas[f] * s.y;   // Re(i omega s)
+            v = -omegas[k / npol] * sy;   // Re(i omega s)
         }
-        acc += gsum;
+        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+        if (live && k == 0) g[c] += v;
     }
-    g[c] = acc;
+}
+
+// Per-source sensitivities: lambda lanes 2j + p (source j, polarisation p)
+// against the forward field's lanes e0 + p at one frequency; g[j][c] is the
+// sum over the two polarisations of Re(i omega sum_e lambda_e E_e dMe)
+// (compute_sensitivity, forward_solver_fv.cpp:989-1059, per polarisation,
+// summed as inversion_fv.cpp:280-290 sums them).  Same thread layout as
+// k_sensitivity; a source's two lanes are neighbours in the group.
+template <int G>
+__global__ void k_sensitivity_src(MeshDev m, const double* __restrict__ sigma, VecK E, int e0, VecK lam,
+                                  const double* __restrict__ omega, int n_src, double* __restrict__ g) {
+    const long total = ((long)m.nc * G + 31) / 32 * 32;
+    const long stride = (long)gridDim.x * blockDim.x;
+    const int nl = 2 * n_src;
+    const double om = omega[0];
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int c = (int)(t / G);
+        const int k = (int)(t % G);
+        const bool live = c < m.nc && k < nl;
+        double v = 0.0;
+        if (live) {
+            const double sc = sigma[c];
+            const int kE = e0 + (k & 1);
+            double sy = 0.0;
+            for (int q = m.cell_ptr[c]; q < m.cell_ptr[c + 1]; ++q) {
+                const int e = m.cell_edge[q];
+                if (m.flags[e] & kFlagSensFixed) continue;
+                const int na = m.nadj[e];
+                if (na == 0) continue;
+                const double dMe = sc * m.adual[e] * m.elen[e] / na;
+                const double2 le = cmul(lam.p[(size_t)e * lam.K + k], E.p[(size_t)e * E.K + kE]);
+                sy += le.y * dMe;
+            }
+            v = -om * sy;
+        }
+        const double w = __shfl_xor_sync(0xffffffffu, v, 1, G);
+        if (live && (k & 1) == 0) g[(size_t)(k >> 1) * m.nc + c] = v + w;
+    }
 }
 
 __global__ void k_pert_rhs(MeshDev m, const double* __restrict__ sigma, const double* __restrict__ dsig,
@@ -1284,13 +1333,38 @@ void pick_pol_lanes(long n_pad, int K, const double2* a, const double2* b, doubl
 void adjoint_rhs(const StationDev& st, const MeshDev& m, const double2* wr, const HCache* hc,
                  const double* omegas, int nf, VecK out, cudaStream_t s) {
     (void)m;
-    k_adjoint_rhs<<<1, 32, 0, s>>>(st, wr, hc, omegas, nf, out);
+    k_adjoint_rhs<<<1, 32, 0, s>>>(st, wr, hc, omegas, nf, st.ns, 1, out);
+    ck();
+}
+
+void adjoint_rhs_sources(const StationDev& st, const double2* wr, const HCache* hc, const double* omega, int n_src,
+                         VecK out, cudaStream_t s) {
+    if (n_src < 1 || 2 * n_src > out.K) throw std::invalid_argument("adjoint sources: 1 .. K/2");
+    k_adjoint_rhs<<<1, 32, 0, s>>>(st, wr, hc, omega, n_src, 0, 0, out);
     ck();
 }
 
 void sensitivity(const MeshDev& m, const double* sigma, VecK E, VecK lam, const double* omegas, int nf,
                  int npol, double* g, cudaStream_t s) {
-    k_sensitivity<<<grid1(m.nc), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    const int nl = nf * npol;
+    if (nl < 1 || nl > dev::kMaxRhs) throw std::invalid_argument("sensitivity: 1..16 lanes");
+    const long n = (long)m.nc * 16;
+    if (nl == 1) k_sensitivity<1><<<grid1(n / 16), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    else if (nl == 2) k_sensitivity<2><<<grid1(n / 8), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    else if (nl <= 4) k_sensitivity<4><<<grid1(n / 4), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    else if (nl <= 8) k_sensitivity<8><<<grid1(n / 2), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    else k_sensitivity<16><<<grid1(n), kBlock, 0, s>>>(m, sigma, E, lam, omegas, nf, npol, g);
+    ck();
+}
+
+void sensitivity_sources(const MeshDev& m, const double* sigma, VecK E, int e0, VecK lam, const double* omega,
+                         int n_src, double* g, cudaStream_t s) {
+    if (n_src < 1 || 2 * n_src > dev::kMaxRhs) throw std::invalid_argument("sensitivity: 1 .. 8 sources");
+    const long n = (long)m.nc * 16;
+    if (n_src == 1) k_sensitivity_src<2><<<grid1(n / 8), kBlock, 0, s>>>(m, sigma, E, e0, lam, omega, n_src, g);
+    else if (n_src == 2) k_sensitivity_src<4><<<grid1(n / 4), kBlock, 0, s>>>(m, sigma, E, e0, lam, omega, n_src, g);
+    else if (n_src <= 4) k_sensitivity_src<8><<<grid1(n / 2), kBlock, 0, s>>>(m, sigma, E, e0, lam, omega, n_src, g);
+    else k_sensitivity_src<16><<<grid1(n), kBlock, 0, s>>>(m, sigma, E, e0, lam, omega, n_src, g);
     ck();
 }
 

@@ -196,6 +196,15 @@ void weighted_residual(int ns, int nf, int nf_total, int f0, const double2* obs,
 // adjoint source for every frequency: rhs 2f <- pol1, 2f+1 <- pol2 (must be zeroed first).
 void adjoint_rhs(const StationDev& st, const MeshDev& m, const double2* wr, const HCache* hc,
                  const double* omegas, int nf, VecK out, cudaStream_t s);
+// adjoint sources of n_src station residuals at one frequency: wr [n_src][ns][4],
+// one station cache hc [ns] and omega[0]; rhs 2j <- pol1, 2j+1 <- pol2 of
+// source j (must be zeroed first).
+void adjoint_rhs_sources(const StationDev& st, const double2* wr, const HCache* hc, const double* omega, int n_src,
+                         VecK out, cudaStream_t s);
+// g[j][c] = sum_p Re(i omega sum_e lambda_e E_e dMe), lambda rhs 2j+p against
+// E rhs e0+p, for n_src <= 8 sources at one frequency (g [n_src][nc], written).
+void sensitivity_sources(const MeshDev& m, const double* sigma, VecK E, int e0, VecK lam, const double* omega,
+                         int n_src, double* g, cudaStream_t s);
 // g[c] (+)= sum_f Re(i omega_f sum_e lambda_e E_e dMe) over both polarisations
 // (compute_sensitivity :989-1059 summed as in inversion_fv.cpp:282-288).
 // E rhs 2f+p pairs with lambda rhs 2f+p; npol = 1 uses rhs f only.

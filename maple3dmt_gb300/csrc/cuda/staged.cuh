@@ -55,6 +55,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
 }
 
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -195,8 +199,21 @@ __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__
     auto wait_stage = [&](int stg, unsigned parity) {
         return no_wait ? mbar_test_wait(&bar[stg], parity) : mbar_wait_bounded(&bar[stg], parity);
     };
+    // every exit leaves the barriers invalidated, so that a kernel may run
+    // the pipeline again (one sweep group after another)
+    auto finish = [&]() {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_inval(&bar[0]);
+            mbar_inval(&bar[1]);
+        }
+        __syncthreads();
+    };
     long i = blockIdx.x;
-    if (i >= n_items) return;   // uniform: the whole block has no item
+    if (i >= n_items) {   // uniform: the whole block has no item
+        finish();
+        return;
+    }
     if (threadIdx.x == 0) issue(i, 0);
     // outcome of the wait for the item about to be consumed, block-uniform
     bool fail = __syncthreads_or(!wait_stage(0, 0u)) != 0;
@@ -210,7 +227,7 @@ __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__
                 atomicOr(err, kErrCopyTimeout);
                 mbar_wait_bounded(&bar[stg], (unsigned)(k >> 1) & 1u);
             }
-            __syncthreads();
+            finish();
             return;
         }
         const long next = i + gridDim.x;
@@ -219,12 +236,44 @@ __device__ __forceinline__ void slice_pipeline(const unsigned char* __restrict__
             issue(next, stg ^ 1);
         }
         body(unpack(wk[stg]), dsm + (size_t)stg * stage_bytes);
-        if (next >= n_items) break;
+        if (next >= n_items) {
+            finish();
+            return;
+        }
         // wait for the next item's stage; the same barrier ends this item
         fail = __syncthreads_or(!wait_stage(stg ^ 1, (unsigned)((k + 1) >> 1) & 1u)) != 0;
         i = next;
         ++k;
     }
+}
+
+// Barrier over all blocks of a cooperative launch (every block resident):
+// an arrival counter and a generation word in global memory, the wait
+// bounded by kWaitCycles; a timeout sets kErrCopyTimeout in *err and lets the
+// block go on (the call's results are then invalid).  The last block to
+// arrive resets the counter before it moves the generation on.
+__device__ __forceinline__ void grid_barrier(unsigned* count, unsigned* gen, unsigned* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+        if (atomicAdd(count, 1u) == nb - 1) {
+            *reinterpret_cast<volatile unsigned*>(count) = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*vgen == g)
+                if (clock64() - t0 > kWaitCycles) {
+                    atomicOr(err, kErrCopyTimeout);
+                    break;
+                }
+        }
+        __threadfence();
+    }
+    __syncthreads();
 }
 
 // Four values of a staged row from shared memory.
@@ -237,6 +286,44 @@ __device__ __forceinline__ void lds4(const double* p, double (&a)[4]) {
     const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
     a[0] = q0.x; a[1] = q0.y; a[2] = q1.x; a[3] = q1.y;
 }
+
+// The first eight entries of one staged row [b, e) (b, e multiples of 4):
+// values read from shared memory and the gathers v[c_j][rhs] issued, summed
+// later by sum() in entry order (entries past e are zero).  A sweep loads the
+// heads of all its passes' rows before it writes the first one, so the
+// gathers of every pass are in flight together; the rows of one colour are
+// independent, which makes the early loads exact.
+template <class R, int K>
+struct RowHead {
+    R a[8];
+    cplx<R> x[8];
+    __device__ __forceinline__ void load(const int* __restrict__ col, const R* __restrict__ val, int b, int e,
+                                         const cplx<R>* v, int rhs) {
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+            const int k = b + 4 * g;
+            if (k < e) {
+                const int4 c = *reinterpret_cast<const int4*>(col + k);
+                R q[4];
+                lds4(val + k, q);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) a[4 * g + u] = q[u];
+                x[4 * g + 0] = v[(size_t)c.x * K + rhs];
+                x[4 * g + 1] = v[(size_t)c.y * K + rhs];
+                x[4 * g + 2] = v[(size_t)c.z * K + rhs];
+                x[4 * g + 3] = v[(size_t)c.w * K + rhs];
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) { a[4 * g + u] = (R)0; x[4 * g + u] = cm<R>(0, 0); }
+            }
+        }
+    }
+    __device__ __forceinline__ cplx<R> sum(cplx<R> s) const {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) { s.x += a[u] * x[u].x; s.y += a[u] * x[u].y; }
+        return s;
+    }
+};
 
 // s + sum over one staged row's entries [b, e) (b, e multiples of 4) of
 // a_j * v[c_j][rhs]: 16-byte shared-memory reads, eight gathers in flight,

@@ -101,8 +101,11 @@ __global__ void k_fg_add64(double2* __restrict__ x, const float2* __restrict__ d
 }
 
 // part[q][block][k] = sum over this block's elements of conj(V_q) w, q < nv
-// (V_q at V + q * ld), and for q = nv (with_self) of conj(w) w; FP64 sums,
-// lanes reduced in a fixed tree.
+// (V_q at V + q * ld), and for q = nv (with_self) of conj(w) w.  Each thread
+// sums its strided elements (about n / 262144, all of one lane) in FP32, the
+// precision of the vectors, and the block reduces the threads' sums in FP64
+// in a fixed tree: FP64 arithmetic runs at a small fraction of FP32 on this
+// GPU and would bound the pass otherwise.
 constexpr int kFgMaxV = 48;
 __global__ void __launch_bounds__(256) k_fg_mdot(const float2* __restrict__ V, long ld, int nv, int with_self,
                                                  const float2* __restrict__ w, int K, long n,
@@ -110,14 +113,14 @@ __global__ void __launch_bounds__(256) k_fg_mdot(const float2* __restrict__ V, l
     __shared__ double2 sh[256];
     const int nb = gridDim.x;
     for (int q = 0; q < nv + with_self; ++q) {
-        double2 acc = make_double2(0.0, 0.0);
+        float2 acc = make_float2(0.0f, 0.0f);
         const float2* vq = q < nv ? V + (size_t)q * ld : w;
         for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)nb * blockDim.x) {
             const float2 a = vq[i], b = w[i];
-            acc.x += (double)a.x * b.x + (double)a.y * b.y;
-            acc.y += (double)a.x * b.y - (double)a.y * b.x;
+            acc.x += a.x * b.x + a.y * b.y;
+            acc.y += a.x * b.y - a.y * b.x;
         }
-        sh[threadIdx.x] = acc;
+        sh[threadIdx.x] = make_double2((double)acc.x, (double)acc.y);
         __syncthreads();
         // threads t and t + s hold the same lane when K divides s
         for (int s = 128; s >= K; s >>= 1) {

@@ -211,7 +211,8 @@ void GpuSolver::free_all() {
     dfree(d_op_rp); dfree(d_op_rs); dfree(d_col); dfree(d_val); dfree(d_val32);
     dfree(d_seg64); dfree(d_seg32); dfree(d_work64); dfree(d_work32); dfree(d_seg_err);
     seg64 = dev::SegView<double>{}; seg32 = dev::SegView<float>{};
-    dfree(d_colour_list);
+    dfree(d_colour_list); dfree(d_colour_ptr); dfree(d_gridbar);
+    dfree(d_src_wr); dfree(d_src_g); src_ns = -1;
     dfree(d_sigma); dfree(d_Me); dfree(d_me_dc);
     dfree(d_diag); dfree(d_diag32); dfree(d_omegas);
     dfree(red.partial); dfree(red.final_); dfree(red.counter);
@@ -356,28 +357,41 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     // whole slices.  A row's neighbours then sit in the same block or the next
     // one, so gathers stay inside a small, cache-resident window, while each
     // SSOR colour sweep walks its slice list across all blocks.
+    //
+    // Sweep groups: with sweep_rows > 0 the reference order is also cut into
+    // super-blocks of about sweep_rows edges, and the SSOR ordering becomes
+    // (super-block, colour): a sweep runs every colour of one super-block
+    // before the next one, so the rows it gathers stay in L2 while the
+    // super-block is swept.  A group (super-block, colour) is what a colour
+    // was: independent rows, one sweep step.  sweep_rows = 0: one super-block.
     constexpr int kRowBlock = 16384;
+    const int blocks_per_sb = P.sweep_rows > 0 ? std::max(1, P.sweep_rows / kRowBlock) : (1 << 30);
+    const int n_sb = (int)(((long)(ne + kRowBlock - 1) / kRowBlock + blocks_per_sb - 1) / blocks_per_sb);
+    auto group_of = [&](int e) { return (e / kRowBlock / blocks_per_sb) * n_col + colour[e]; };
+    const int n_grp = n_sb * n_col;
     perm.clear();
-    std::vector<std::vector<int>> slices_of(n_col);
+    std::vector<std::vector<int>> slices_of(n_grp);
     {
         std::vector<std::vector<int>> byc(n_col);
         for (int b0 = 0; b0 < ne; b0 += kRowBlock) {
             for (auto& v : byc) v.clear();
             for (int e = b0; e < std::min(ne, b0 + kRowBlock); ++e) byc[colour[e]].push_back(e);
+            const int g0 = (b0 / kRowBlock / blocks_per_sb) * n_col;
             for (int c = 0; c < n_col; ++c) {
                 if (byc[c].empty()) continue;
                 const int s0 = (int)(perm.size() / dev::kSlice);
                 for (int e : byc[c]) perm.push_back(e);
                 while (perm.size() % dev::kSlice) perm.push_back(-1);
                 const int s1 = (int)(perm.size() / dev::kSlice);
-                for (int s = s0; s < s1; ++s) slices_of[c].push_back(s);
+                for (int s = s0; s < s1; ++s) slices_of[g0 + c].push_back(s);
             }
         }
     }
     colour_ptr.assign(1, 0);
     colour_list.clear();
-    for (int c = 0; c < n_col; ++c) {
-        colour_list.insert(colour_list.end(), slices_of[c].begin(), slices_of[c].end());
+    for (int g = 0; g < n_grp; ++g) {
+        if (slices_of[g].empty()) continue;
+        colour_list.insert(colour_list.end(), slices_of[g].begin(), slices_of[g].end());
         colour_ptr.push_back((int)colour_list.size());
     }
     n_pad = (int)perm.size();
@@ -386,7 +400,8 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     for (int r = 0; r < n_pad; ++r) if (perm[r] >= 0) iperm[perm[r]] = r;
 
     // Split CSR of the free-free off-diagonal part in permuted row order:
-    // lower (earlier colour) entries, then upper, each in reference column order.
+    // lower (earlier sweep group) entries, then upper, each in reference
+    // column order.
     std::vector<int> op_rp(n_pad + 1, 0), op_rs(n_pad, 0), ecol;
     std::vector<double> eval;
     {
@@ -401,7 +416,7 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
                 for (int k = L.s_ptr[e]; k < L.s_ptr[e + 1]; ++k) {
                     const int j = L.s_idx[k];
                     if (j == e || !free_row(j)) continue;
-                    if (colour[j] < colour[e]) { ecol.push_back(iperm[j]); eval.push_back(L.s_val[k]); }
+                    if (group_of(j) < group_of(e)) { ecol.push_back(iperm[j]); eval.push_back(L.s_val[k]); }
                     else { up_c.push_back(iperm[j]); up_v.push_back(L.s_val[k]); }
                 }
             op_rs[r] = (int)ecol.size();
@@ -539,6 +554,8 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     d_op_rp = dupload(op_rp, stream); d_op_rs = dupload(op_rs, stream);
     d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
     d_colour_list = dupload(colour_list, stream);
+    d_colour_ptr = dupload(colour_ptr, stream);
+    d_gridbar = dalloc_zero<unsigned>(2, stream);
     build_segments(op_rp, op_rs, ecol, eval);
     {
         std::vector<float> ev32(eval.begin(), eval.end());
@@ -998,6 +1015,9 @@ KrylovCtx<double> GpuSolver::kctx(int K, const int* fmap) const {
     c.n_freq = (int)(std::unique(fs.begin(), fs.end()) - fs.begin());
     c.seg = seg64;
     c.row_kernels = P.row_kernels;
+    c.coop = P.coop_sweep;
+    c.colour_ptr_d = d_colour_ptr;
+    c.gridbar = d_gridbar;
     return c;
 }
 
@@ -1167,6 +1187,9 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     f.row_kernels = c.row_kernels;
     f.eis_partial = d_eis_partial;
     f.eis_slots = eis_slots;
+    f.coop = c.coop;
+    f.colour_ptr_d = c.colour_ptr_d;
+    f.gridbar = c.gridbar;
     return f;
 }
 
@@ -1848,6 +1871,75 @@ void GpuSolver::solve_rhs_batch(const double* rhs_h, int n_rhs, double* out) {
                                     cudaMemcpyDeviceToHost, stream), "out");
             sync();   // the staging buffer is reused by the next lane
         }
+    }
+    stats.total_iterations = (int)it_total;
+    stats.n_rhs = (int)all_it.size();
+    for (size_t k = 0; k < all_it.size() && k < 64; ++k) {
+        stats.iterations[k] = all_it[k];
+        stats.status[k] = all_st[k];
+        stats.true_residual[k] = all_tr[k];
+    }
+    stats.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    end_call();
+}
+
+// Gradients of many residual sources at the solved single frequency, one per
+// source: for source j, build_adjoint_rhs_from_residual(wr_j)
+// (forward_solver_fv.cpp:1804-2013), both polarisations' adjoint solves
+// (adjoint_solve_complex -> solve_with_divcorr_, :914-924) and
+// compute_sensitivity_complex (:989-1059) of each, summed over the two
+// polarisations as InversionFV::compute_gradient_ sums them
+// (inversion_fv.cpp:280-290).  With wr_j non-zero at one station this is
+// that station's row of J^T W^2 r.  Eight sources (sixteen right-hand sides)
+// per batch, built, solved and reduced on the device: only wr goes in and g
+// comes out.  wr [n_src][ns][4] complex, g [n_src][nc].
+void GpuSolver::station_gradients(const double* wr_h, int n_src, double* g_out) {
+    if (E_nf != 1 || !d_hc || fz_freqs.empty())
+        throw std::logic_error("station gradients need a solved single frequency");
+    if (n_src < 0) throw std::invalid_argument("n_src < 0");
+    const auto t0 = std::chrono::steady_clock::now();
+    begin_call();
+    const int ns = sd.ns;
+    const int fslot = (int)fz_freqs.size() - 1;
+    if (src_ns != ns) {
+        dfree(d_src_wr); dfree(d_src_g);
+        d_src_wr = dalloc<double2>((size_t)8 * std::max(1, ns) * 4);
+        d_src_g = dalloc<double>((size_t)8 * L.nc);
+        src_ns = ns;
+    }
+    std::vector<int> all_it, all_st;
+    std::vector<double> all_tr;
+    long long it_total = 0;
+    for (int j0 = 0; j0 < n_src; j0 += 8) {
+        const int g = std::min(8, n_src - j0);
+        const int K = pow2_at_least(2 * g);
+        ensure_fields(K);
+        ensure_vecs(K);
+        cuda_ok(cudaMemcpyAsync(d_src_wr, wr_h + (size_t)j0 * ns * 8, sizeof(double2) * (size_t)g * ns * 4,
+                                cudaMemcpyHostToDevice, stream), "wr");
+        cuda_ok(cudaMemsetAsync(d_adj, 0, sizeof(double2) * (size_t)n_pad * K, stream), "memset");
+        phys::adjoint_rhs_sources(sd, d_src_wr, d_hc, d_omegas + fslot, g, VecK{d_adj, K}, stream);
+        ++launches;
+        std::vector<int> fmap(K, fslot), pol(K, -1), active(K, 0);
+        for (int k = 0; k < 2 * g; ++k) active[k] = 1;
+        RhsInfo info = rhs_info(K, fmap, pol, fz_freqs);
+        run_adjoint(K, fmap.data(), info, d_adj, d_lam, active);
+        it_total += stats.total_iterations;
+        for (int k = 0; k < stats.n_rhs; ++k) {
+            all_it.push_back(stats.iterations[k]);
+            all_st.push_back(stats.status[k]);
+            all_tr.push_back(stats.true_residual[k]);
+        }
+        {
+            const int ts = timer.on ? timer.begin(kClsSens, sens_bytes(2 * g), K) : -1;
+            phys::sensitivity_sources(md, d_sigma, VecK{d_E, E_K}, 0, VecK{d_lam, K}, d_omegas + fslot, g, d_src_g,
+                                      stream);
+            timer.end(ts);
+        }
+        ++launches;
+        cuda_ok(cudaMemcpyAsync(g_out + (size_t)j0 * L.nc, d_src_g, sizeof(double) * (size_t)g * L.nc,
+                                cudaMemcpyDeviceToHost, stream), "g");
+        sync();
     }
     stats.total_iterations = (int)it_total;
     stats.n_rhs = (int)all_it.size();

@@ -90,6 +90,7 @@ public:
     void jtjv_batch(const double* freqs, int nf, const double* dsigma, const double* err, double inner_tol,
                     double* out);
     void solve_rhs_batch(const double* rhs, int n_rhs, double* out);
+    void station_gradients(const double* wr, int n_src, double* g);
     // octree model regularisation (RegularizationOctree) on this mesh
     RegHost reg_host;
     RegDev reg{};
@@ -135,6 +136,8 @@ private:
     // host-side structure
     std::vector<int> perm, iperm, colour_ptr, colour_list;
     int* d_colour_list = nullptr;
+    int* d_colour_ptr = nullptr;        // device copy of colour_ptr (cooperative sweeps)
+    unsigned* d_gridbar = nullptr;      // grid barrier of the cooperative sweeps
     std::vector<unsigned char> flags_ref;  // reference order
     int n_pad = 0, n_slices = 0;
     bool hp_sequential = false;
@@ -221,6 +224,9 @@ private:
     int fwd_cap = 0;
     int E_cap = 0;       // capacity (lanes) of d_E, grown only by its writers
     int jtj_ns = -1;     // station count the jtjv_batch station buffers were sized for
+    double2* d_src_wr = nullptr;   // [8][ns][4] residuals of one batch of station sources
+    double* d_src_g = nullptr;     // [8][nc] their gradients
+    int src_ns = -1;               // station count d_src_wr was sized for
 
     // divergence correction
     phys::DcWork dc{};

@@ -152,6 +152,15 @@ class ForwardSolverFV:
         self._ck(self.lib.m3d_solve_rhs_batch(self.h, pr, int(r.shape[0]), out.ctypes.data_as(c_double_p)))
         return out
 
+    def station_gradients(self, wr):
+        """Gradients of residual sources wr [n_src][n_stations][4] complex at the
+        solved single frequency, one per source: g [n_src][n_cells]
+        (m3d_station_gradients)."""
+        w, pw = _c(np.asarray(wr).reshape(-1, self.ns, 4))
+        g = np.zeros((w.shape[0], self.nc))
+        self._ck(self.lib.m3d_station_gradients(self.h, pw, int(w.shape[0]), g.ctypes.data_as(c_double_p)))
+        return g
+
     def compute_sensitivity_complex(self, E, lam):
         e, pe = _c(E)
         l, pl = _c(lam)
@@ -328,3 +337,30 @@ def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:
     s.set_sigma(sv.sigma)
     s.set_stations(sv.stations)
     return s
+
+
+def group_station_gradients(solvers, freqs, wr, max_concurrent=0):
+    """Per-frequency meshes run concurrently on one device
+    (m3d_group_station_gradients): solvers[m] at freqs[m], residual sources
+    wr[m] [n_src][n_stations][4].  Returns (Z [m] [n_stations][4],
+    g [m] [n_src][n_cells(m)], status [m])."""
+    n = len(solvers)
+    if n < 1 or len(freqs) != n or len(wr) != n:
+        raise ValueError("one frequency and one source set per solver")
+    lib = solvers[0].lib
+    hs = (C.c_void_p * n)(*[s.h for s in solvers])
+    fr = np.ascontiguousarray(np.asarray(freqs, np.float64))
+    ws = [np.ascontiguousarray(np.asarray(w, np.complex128).reshape(-1, s.ns, 4)) for w, s in zip(wr, solvers)]
+    ns = (C.c_int * n)(*[w.shape[0] for w in ws])
+    Z = [np.zeros((s.ns, 4), np.complex128) for s in solvers]
+    g = [np.zeros((w.shape[0], s.nc)) for w, s in zip(ws, solvers)]
+    pw = (c_double_p * n)(*[w.ctypes.data_as(c_double_p) for w in ws])
+    pz = (c_double_p * n)(*[z.ctypes.data_as(c_double_p) for z in Z])
+    pg = (c_double_p * n)(*[a.ctypes.data_as(c_double_p) for a in g])
+    st = (C.c_int * n)()
+    rc = lib.m3d_group_station_gradients(hs, n, fr.ctypes.data_as(c_double_p), pw, ns, pz, pg, int(max_concurrent), st)
+    status = list(st)
+    if rc != 0:
+        m = next(i for i, v in enumerate(status) if v != 0)
+        raise SolverError(rc, f"mesh {m}: " + lib.m3d_last_error(solvers[m].h).decode(errors="replace"))
+    return Z, g, status

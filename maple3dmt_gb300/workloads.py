@@ -141,3 +141,19 @@ class SurveySpec:
 C1 = SurveySpec("C1 halfspace", 3, 5, 5, 2000.0, (1.0,))
 C2 = SurveySpec("C2 layered+block", 6, 7, 11, 1000.0, tuple(np.logspace(-2, 2, 8).tolist()))
 C5 = SurveySpec("C5 layered+block at scale", 6, 8, 20, 1000.0, tuple(np.logspace(-3, 3, 24).tolist()))
+# one mesh per frequency (skin-depth refinement at that frequency only),
+# log10 sigma of earth cells perturbed by N(0, 0.3^2)
+C3 = SurveySpec("C3 per-frequency meshes", 6, 7, 11, 1000.0, tuple(np.logspace(-3, 3, 16).tolist()))
+C3_NOISE_STD = 0.3
+
+
+def station_sources(ns, rng, level=0.05):
+    """Adjoint sources of the per-station Jacobian rows: source s has
+    w^2 conj(r) at station s only, r a synthetic 5 % residual of a unit-scale
+    response on the off-diagonal impedances (Zxy, Zyx) with unit weight.
+    Returns wr [ns][ns][4] complex."""
+    wr = np.zeros((ns, ns, 4), np.complex128)
+    for k in (1, 2):
+        r = level * (rng.normal(size=ns) + 1j * rng.normal(size=ns)) / math.sqrt(2)
+        wr[np.arange(ns), np.arange(ns), k] = np.conj(r)
+    return wr
