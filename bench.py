@@ -94,6 +94,10 @@ def parse():
     ap.add_argument("--gradcorr-overlap", type=int, default=1, choices=[0, 1])
     ap.add_argument("--sweep-rows", type=int, default=0,
                     help="SSOR ordering by (super-block, colour), super-blocks of about this many edges (0: off)")
+    ap.add_argument("--ssor-relax", type=float, default=1.0,
+                    help="SSOR relaxation factor of the FP32 inner solve (1: the reference's symmetric GS)")
+    ap.add_argument("--cuda-graphs", type=int, default=1, choices=[0, 1],
+                    help="replay the inner solve's 10-iteration chunks from CUDA graphs")
     ap.add_argument("--coop-sweep", type=int, default=0, choices=[0, 1],
                     help="1: each staged SSOR sweep as one cooperative launch over its groups")
     ap.add_argument("--learned-steps", type=int, default=1,
@@ -388,7 +392,7 @@ def solver_params(args, plain):
                  gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
                  inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
                  gradcorr_overlap=args.gradcorr_overlap, sweep_rows=args.sweep_rows,
-                 coop_sweep=args.coop_sweep)
+                 coop_sweep=args.coop_sweep, ssor_relax=args.ssor_relax, cuda_graphs=args.cuda_graphs)
     return p
 
 
@@ -411,7 +415,8 @@ def solver_label(args, p, freqs):
                          + (", V-cycle on a second stream" if p["gradcorr_overlap"] else "")) if p["gradcorr"]
             else "off",
             "residual_replacement": bool(p["residual_replacement"]),
-            "sweep_rows": p["sweep_rows"], "coop_sweep": bool(p["coop_sweep"])}
+            "sweep_rows": p["sweep_rows"], "coop_sweep": bool(p["coop_sweep"]), "ssor_relax": p["ssor_relax"],
+            "cuda_graphs": bool(p["cuda_graphs"])}
 
 
 def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False):
@@ -497,7 +502,7 @@ def run_learned(args, sv, obs, err, local_rank):
     """The learned arm on the same step: a 6-layer 32-channel network on a
     32^3 grid, trained on the GPU from (residual -> error) pairs that the
     plain FP64 SSOR-BiCGStab records while solving the step's frequencies
-    from 0.5 Hz up (untimed, reported), then the step with flexible GMRES
+    from 0.1 Hz up (untimed, reported), then the step with flexible GMRES
     whose every second direction is the two-level step with the network as
     coarse solve, and the same FGMRES without the network (the gain)."""
     from maple3dmt_gb300.solver import solver_for_survey
@@ -507,9 +512,9 @@ def run_learned(args, sv, obs, err, local_rank):
     try:
         t0 = time.perf_counter()
         s.learn_setup(grid_level=5, layers=6, hidden=32, seed=1, max_samples=args.learned_pairs)
-        n = s.learn_collect(sv.freqs[sv.freqs >= 0.5])
+        n = s.learn_collect(sv.freqs[sv.freqs >= 0.1])
         t1 = time.perf_counter()
-        hist, val = s.learn_train(epochs=4, lr=1e-3, batch=16, seed=3, val_frac=0.1)
+        hist, val = s.learn_train(epochs=8, lr=1e-3, batch=16, seed=3, val_frac=0.1)
         t2 = time.perf_counter()
         out = {"unit": UNIT, "steps": args.learned_steps, "warmup": 1, "network": "6 x conv3x3x3, 32 channels, "
                "BF16 tcgen05 kernels, 32^3 grid", "krylov": f"FGMRES({args.fgmres_m}), network every 2nd direction",

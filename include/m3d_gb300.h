@@ -149,6 +149,12 @@ typedef struct m3d_params {
                                  edges, so a sweep's gathers stay in L2; 0: colour order over the mesh */
     int coop_sweep;           /* 1: each staged SSOR sweep is one cooperative launch over all its groups
                                  (bounded grid barriers between groups); 0: one launch per group */
+    int cuda_graphs;          /* 1 (default): the mixed-precision inner solve captures its 10-iteration
+                                 chunk (every launch of ten BiCGStab iterations, both streams) once per
+                                 batch shape in a CUDA graph and replays it; 0: launches issued one by one */
+    double ssor_relax;        /* relaxation factor omega of the SSOR sweeps of the mixed-precision inner
+                                 solve, 0 < omega < 2 (1: the reference's symmetric Gauss-Seidel,
+                                 ssor.h:58-78); the FP64 path always uses 1 */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;
@@ -171,6 +177,8 @@ typedef struct m3d_stats {
     long long divcorr_cg_sweeps;      /* batched PCG iterations run (each serves every rhs of a batch) */
     double divcorr_setup_ms;          /* host time of the last multigrid setup of the PCG */
     int replacements;                 /* residual replacements of the inner solves */
+    int graphs_failed;                /* 1: a chunk capture failed, chunks run as direct launches */
+    long long graph_replays;          /* CUDA-graph chunk replays since the handle was created */
 } m3d_stats;
 
 void m3d_params_default(m3d_params* p);

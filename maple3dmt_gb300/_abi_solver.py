@@ -39,6 +39,8 @@ class Params(C.Structure):
         ("learned_period", C.c_int),
         ("sweep_rows", C.c_int),
         ("coop_sweep", C.c_int),
+        ("cuda_graphs", C.c_int),
+        ("ssor_relax", C.c_double),
     ]
 
 
@@ -61,6 +63,8 @@ class Stats(C.Structure):
         ("divcorr_cg_sweeps", C.c_longlong),
         ("divcorr_setup_ms", C.c_double),
         ("replacements", C.c_int),
+        ("graphs_failed", C.c_int),
+        ("graph_replays", C.c_longlong),
     ]
 
 

@@ -48,18 +48,29 @@ cudaEvent_t KernelTimer::get() {
     return e;
 }
 
+// Inside a stream capture a plain event record only marks a dependency; the
+// timer's records become event-record nodes of the graph (re-recorded at
+// every replay) with cudaEventRecordExternal.
+static void timer_record(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else
+        cudaEventRecord(e, s);
+}
+
 int KernelTimer::begin(int cls, double algorithmic_bytes, int K, cudaStream_t s) {
     if (!on) return -1;
     const int kb = K == 2 ? 0 : K == 4 ? 1 : K == 8 ? 2 : K == 16 ? 3 : 4;
     Pair p{cls, kb, get(), get(), algorithmic_bytes};
-    cudaEventRecord(p.a, s ? s : stream);
+    timer_record(p.a, s ? s : stream);
     open.push_back(p);
     return (int)open.size() - 1;
 }
 
 void KernelTimer::end(int h, cudaStream_t s) {
     if (h < 0) return;
-    cudaEventRecord(open[h].b, s ? s : stream);
+    timer_record(open[h].b, s ? s : stream);
 }
 
 void KernelTimer::set_bytes(int h, double algorithmic_bytes) {
@@ -85,6 +96,38 @@ void KernelTimer::collect() {
     }
     open.clear();
     cudaGetLastError();
+}
+
+std::vector<KernelTimer::Pair> KernelTimer::take(size_t from) {
+    std::vector<Pair> ps;
+    if (from < open.size()) {
+        ps.assign(open.begin() + (long)from, open.end());
+        open.resize(from);
+    }
+    return ps;
+}
+
+void KernelTimer::fold(const std::vector<Pair>& ps) {
+    for (const Pair& p : ps) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+            ms[p.cls] += t;
+            bytes[p.cls] += p.bytes;
+            launches[p.cls] += 1;
+            ms_k[p.cls][p.kb] += t;
+            bytes_k[p.cls][p.kb] += p.bytes;
+            launches_k[p.cls][p.kb] += 1;
+        }
+    }
+    cudaGetLastError();
+}
+
+void KernelTimer::release(std::vector<Pair>& ps) {
+    for (const Pair& p : ps) {
+        pool.push_back(p.a);
+        pool.push_back(p.b);
+    }
+    ps.clear();
 }
 
 void KernelTimer::reset() {
@@ -325,7 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_ssor_fwd(OpView<R> A, DiagView<R> D,
         const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
         const C s = row_dot<R, K>(A, A.rp[row], A.rs[row], y, rhs);
         const size_t i = (size_t)row * K + rhs;
-        y[i] = cmul(csub(in[i], s), inv_c(diag_of(D, row, om)));
+        y[i] = cmul(csub(in[i], s), cscale(inv_c(diag_of(D, row, om)), (R)B.relax));
     }
 }
 
@@ -348,7 +391,7 @@ __global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D,
         const int row = list[t / GPS] * kSlice + (int)(t % GPS) * RPW + sub;
         const C s = row_dot<R, K>(A, A.rs[row], A.rp[row + 1], out, rhs);
         const size_t i = (size_t)row * K + rhs;
-        out[i] = csub(y[i], cmul(s, inv_c(diag_of(D, row, om))));
+        out[i] = csub(y[i], cmul(s, cscale(inv_c(diag_of(D, row, om)), (R)B.relax)));
     }
 }
 
@@ -435,7 +478,8 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
 // (ssor.h:58-66); items work_col[0..count) of the colour.
 template <class R, int K>
 __device__ __forceinline__ void ssor_fwd_rows(const SegItem& it, const unsigned char* base, const DiagView<R>& D,
-                                              R om, int rhs, int lr0, const cplx<R>* __restrict__ in, cplx<R>* y) {
+                                              R om, R rx, int rhs, int lr0, const cplx<R>* __restrict__ in,
+                                              cplx<R>* y) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
     SegRows<R> lo;
@@ -458,7 +502,7 @@ __device__ __forceinline__ void ssor_fwd_rows(const SegItem& it, const unsigned 
         C s = h[ps].sum(cm<R>(0, 0));
         const int b = lo.begin_of(lr) + 8, e = lo.end[lr];
         if (b < e) s = seg_row_dot<R, K>(lo.col, lo.val, b, e, y, rhs, s);
-        y[(size_t)row * K + rhs] = cmul(csub(iv[ps], s), inv_c(dv[ps]));
+        y[(size_t)row * K + rhs] = cmul(csub(iv[ps], s), cscale(inv_c(dv[ps]), rx));
     }
 }
 
@@ -473,7 +517,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
     slice_pipeline<1>(S.seg, work, count, S.stage_lo, S.err, [&](const SegItem& it, const unsigned char* base) {
-        ssor_fwd_rows<R, K>(it, base, D, om, rhs, lr0, in, y);
+        ssor_fwd_rows<R, K>(it, base, D, om, (R)B.relax, rhs, lr0, in, y);
     });
 }
 
@@ -484,7 +528,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
 // later colours' w from there.
 template <class R, int K, bool GC>
 __device__ __forceinline__ void ssor_bwd_rows(const SegItem& it, const unsigned char* base, const DiagView<R>& D,
-                                              R om, int rhs, int lr0, cplx<R>* y, cplx<R>* out,
+                                              R om, R rx, int rhs, int lr0, cplx<R>* y, cplx<R>* out,
                                               const GcRowTerm& gt) {
     using C = cplx<R>;
     using Sh = StagedShape<K>;
@@ -534,7 +578,7 @@ __device__ __forceinline__ void ssor_bwd_rows(const SegItem& it, const unsigned 
         C s = h[ps].sum(cm<R>(0, 0));
         const int b = up.begin_of(lr) + 8, e = up.end[lr];
         if (b < e) s = seg_row_dot<R, K>(up.col, up.val, b, e, GC ? y : out, rhs, s);
-        const C w = csub(yv[ps], cmul(s, inv_c(dv[ps])));
+        const C w = csub(yv[ps], cmul(s, cscale(inv_c(dv[ps]), rx)));
         if (GC) {
             y[i] = w;
             const float sc = gt.s[rhs];
@@ -557,7 +601,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
     const int lr0 = warp * RPW + lane / K;
     const R om = (R)B.omega[rhs];
     slice_pipeline<2>(S.seg, work, count, S.stage_up, S.err, [&](const SegItem& it, const unsigned char* base) {
-        ssor_bwd_rows<R, K, GC>(it, base, D, om, rhs, lr0, y, out, gt);
+        ssor_bwd_rows<R, K, GC>(it, base, D, om, (R)B.relax, rhs, lr0, y, out, gt);
     });
 }
 
@@ -579,7 +623,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
         const int s0 = gptr[g], s1 = gptr[g + 1];
         slice_pipeline<1>(S.seg, work + s0, s1 - s0, S.stage_lo, S.err,
                           [&](const SegItem& it, const unsigned char* base) {
-                              ssor_fwd_rows<R, K>(it, base, D, om, rhs, lr0, in, y);
+                              ssor_fwd_rows<R, K>(it, base, D, om, (R)B.relax, rhs, lr0, in, y);
                           });
     }
 }
@@ -598,7 +642,7 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) 
         const int s0 = gptr[g], s1 = gptr[g + 1];
         slice_pipeline<2>(S.seg, work + s0, s1 - s0, S.stage_up, S.err,
                           [&](const SegItem& it, const unsigned char* base) {
-                              ssor_bwd_rows<R, K, GC>(it, base, D, om, rhs, lr0, y, out, gt);
+                              ssor_bwd_rows<R, K, GC>(it, base, D, om, (R)B.relax, rhs, lr0, y, out, gt);
                           });
     }
 }

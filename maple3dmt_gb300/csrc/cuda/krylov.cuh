@@ -68,6 +68,7 @@ struct BatchView {
     int K;
     int fmap[dev::kMaxRhs];
     double omega[dev::kMaxRhs];   // angular frequency of each right-hand side
+    double relax = 1.0;           // SSOR relaxation factor of the sweeps (1: the reference's symmetric GS)
 };
 
 // Per-row gradient-space term of the right-preconditioned FP32 iteration
@@ -118,6 +119,12 @@ struct KernelTimer {
     void set_bytes(int handle, double algorithmic_bytes);
     void collect();   // synchronises and folds finished pairs into the totals
     void reset();
+    // pairs recorded inside a CUDA-graph capture: taken out of the open list
+    // (they belong to the graph), folded into the totals after every replay
+    // has finished, and their events returned when the graph is destroyed
+    std::vector<Pair> take(size_t from);
+    void fold(const std::vector<Pair>& ps);
+    void release(std::vector<Pair>& ps);
     ~KernelTimer();
 };
 

@@ -964,12 +964,45 @@ __global__ void k_adjoint_rhs(StationDev st, const double2* __restrict__ wr, con
     }
 }
 
+// sum over cell c's edges of Im(lambda_e E_e) * w_e (w_e = A_dual L / n_adj,
+// 0 for skipped edges) for one lane pair; the edges go four at a time with
+// all their loads issued before the first product, so a thread has twelve
+// independent loads in flight instead of a chain per edge.  Edge order of
+// the sums is the cell's edge order.
+__device__ __forceinline__ double cell_im_sum(const MeshDev& m, int c, const VecK& lam, int kl, const VecK& E,
+                                              int kE) {
+    const int q0 = m.cell_ptr[c], q1 = m.cell_ptr[c + 1];
+    double sy = 0.0;
+    for (int q = q0; q < q1; q += 4) {
+        int e[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) e[u] = q + u < q1 ? m.cell_edge[q + u] : -1;
+        double w[4];
+        double2 l[4], f[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (e[u] >= 0) {
+                w[u] = m.sens_w[e[u]];
+                l[u] = lam.p[(size_t)e[u] * lam.K + kl];
+                f[u] = E.p[(size_t)e[u] * E.K + kE];
+            } else {
+                w[u] = 0.0;
+                l[u] = f[u] = zero2();
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (w[u] != 0.0) sy += cmul(l[u], f[u]).y * w[u];
+    }
+    return sy;
+}
+
 // G consecutive threads per cell (G a power of two >= nf * npol, so a group
 // never straddles a warp), thread k of the group on lane k = npol * f + p:
 // each edge row of E and lambda (K lanes, interleaved) is read as one
-// contiguous segment, and the per-edge scalars are broadcast within the
-// group.  The group's lane terms -omega_f * Im(sum_e lambda_e E_e dMe) are
-// summed by a fixed shuffle tree, so the result is deterministic.
+// contiguous segment, and the per-edge data are broadcast within the
+// group.  The group's lane terms -omega_f sigma_c Im(sum_e lambda_e E_e w_e)
+// are summed by a fixed shuffle tree, so the result is deterministic.
 // compute_sensitivity, forward_solver_fv.cpp:989-1059.
 template <int G>
 __global__ void k_sensitivity(MeshDev m, const double* __restrict__ sigma, VecK E, VecK lam,
@@ -982,20 +1015,7 @@ __global__ void k_sensitivity(MeshDev m, const double* __restrict__ sigma, VecK 
         const int k = (int)(t % G);
         const bool live = c < m.nc;
         double v = 0.0;
-        if (live && k < nl) {
-            const double sc = sigma[c];
-            double sy = 0.0;
-            for (int q = m.cell_ptr[c]; q < m.cell_ptr[c + 1]; ++q) {
-                const int e = m.cell_edge[q];
-                if (m.flags[e] & kFlagSensFixed) continue;
-                const int na = m.nadj[e];
-                if (na == 0) continue;
-                const double dMe = sc * m.adual[e] * m.elen[e] / na;
-                const double2 le = cmul(lam.p[(size_t)e * lam.K + k], E.p[(size_t)e * E.K + k]);
-                sy += le.y * dMe;
-            }
-            v = -omegas[k / npol] * sy;   // Re(i omega s)
-        }
+        if (live && k < nl) v = -omegas[k / npol] * (sigma[c] * cell_im_sum(m, c, lam, k, E, k));   // Re(i omega s)
         for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
         if (live && k == 0) g[c] += v;
     }
@@ -1019,21 +1039,7 @@ __global__ void k_sensitivity_src(MeshDev m, const double* __restrict__ sigma, V
         const int k = (int)(t % G);
         const bool live = c < m.nc && k < nl;
         double v = 0.0;
-        if (live) {
-            const double sc = sigma[c];
-            const int kE = e0 + (k & 1);
-            double sy = 0.0;
-            for (int q = m.cell_ptr[c]; q < m.cell_ptr[c + 1]; ++q) {
-                const int e = m.cell_edge[q];
-                if (m.flags[e] & kFlagSensFixed) continue;
-                const int na = m.nadj[e];
-                if (na == 0) continue;
-                const double dMe = sc * m.adual[e] * m.elen[e] / na;
-                const double2 le = cmul(lam.p[(size_t)e * lam.K + k], E.p[(size_t)e * E.K + kE]);
-                sy += le.y * dMe;
-            }
-            v = -om * sy;
-        }
+        if (live) v = -om * (sigma[c] * cell_im_sum(m, c, lam, k, E, e0 + (k & 1)));
         const double w = __shfl_xor_sync(0xffffffffu, v, 1, G);
         if (live && (k & 1) == 0) g[(size_t)(k >> 1) * m.nc + c] = v + w;
     }

@@ -55,6 +55,7 @@ struct MeshDev {
     // cells
     int* cell_ptr;      // [nc + 1] cell -> edges (StaggeredGrid::cell_edges order), permuted rows
     int* cell_edge;
+    double* sens_w;     // [n_pad] A_dual * L / n_adj of rows the sensitivity sums, 0 for the others
 };
 
 // Per station data, built by the host at m3d_set_stations.

@@ -202,10 +202,11 @@ GpuSolver::~GpuSolver() {
 
 void GpuSolver::free_all() {
     if (stream) cudaStreamSynchronize(stream);
+    graphs_clear();
     learn_free();
     dfree(md.perm); dfree(md.iperm); dfree(md.flags); dfree(md.dir); dfree(md.ez); dfree(md.s_diag);
     dfree(md.me_geom); dfree(md.adual); dfree(md.elen); dfree(md.nadj); dfree(md.adj_ptr); dfree(md.adj_cell);
-    dfree(md.lift_ptr); dfree(md.lift_col); dfree(md.lift_val); dfree(md.hp);
+    dfree(md.lift_ptr); dfree(md.lift_col); dfree(md.lift_val); dfree(md.hp); dfree(md.sens_w);
     dfree(md.inc_ptr); dfree(md.inc_edge); dfree(md.inc_other); dfree(md.inc_gv); dfree(md.inc_gw);
     dfree(md.node_bc); dfree(md.e_node); dfree(md.e_g); dfree(md.cell_ptr); dfree(md.cell_edge);
     dfree(d_op_rp); dfree(d_op_rs); dfree(d_col); dfree(d_val); dfree(d_val32);
@@ -551,6 +552,15 @@ void GpuSolver::setup(const m3d_leaves* lv, const m3d_params* params) {
     md.inc_gw = dupload(inc_gw, stream); md.node_bc = dupload(node_bc, stream);
     md.e_node = dupload(e_node, stream); md.e_g = dupload(e_g, stream);
     md.cell_ptr = dupload(L.cell_ptr, stream); md.cell_edge = dupload(cell_edge, stream);
+    {
+        // per-edge factor of dMe/dsigma_c (compute_sensitivity,
+        // forward_solver_fv.cpp:1010-1030): constrained edges and edges
+        // without adjacent cells are skipped there and weigh 0 here
+        std::vector<double> sens_w(n_pad, 0.0);
+        for (int r = 0; r < n_pad; ++r)
+            if (!(flags[r] & kFlagSensFixed) && nadj[r] > 0) sens_w[r] = adual[r] * elen[r] / nadj[r];
+        md.sens_w = dupload(sens_w, stream);
+    }
     d_op_rp = dupload(op_rp, stream); d_op_rs = dupload(op_rs, stream);
     d_col = dupload(ecol, stream); d_val = dupload(eval, stream);
     d_colour_list = dupload(colour_list, stream);
@@ -1171,6 +1181,7 @@ KrylovCtx<float> GpuSolver::kctx32(int K, const int* fmap) const {
     f.A = OpView<float>{d_op_rp, d_op_rs, d_col, d_val32, n_pad};
     f.D = DiagView<float>{d_diag32};
     f.B = c.B;
+    f.B.relax = P.ssor_relax;   // the FP64 context keeps the reference's 1
     f.colour_ptr = c.colour_ptr;
     f.colour_list = c.colour_list;
     f.n_pad = c.n_pad;
@@ -1309,8 +1320,73 @@ void GpuSolver::build_segments(const std::vector<int>& op_rp, const std::vector<
 // finished lanes' corrections have been added to the FP64 x.  Converged
 // systems then stop costing vector traffic; the matrix stream is shared by
 // whatever remains.
+// The graph of one 10-iteration chunk for the batch shape (K lanes in vector
+// set x, form, gradient-space term): captured from the chunk's launches on
+// first use, both streams included (the V-cycle branch joins the capture
+// through its fork and join events), instantiated and kept until the end of
+// the refinement step.  Every kernel argument of the chunk is fixed for a
+// shape within a step (vectors, Krylov scalars and lane data stay where they
+// are; a compaction changes the shape).  Returns the graph's index, or -1 if
+// the capture failed, in which case nothing ran and chunks are launched
+// directly from then on.
+int GpuSolver::chunk_graph(int K, const void* x, bool eis, bool gc, const std::function<void()>& body) {
+    for (size_t i = 0; i < chunk_graphs.size(); ++i) {
+        const ChunkGraph& g = chunk_graphs[i];
+        if (g.K == K && g.x == x && g.eis == eis && g.gc == gc) return (int)i;
+    }
+    const size_t t0 = timer.open.size();
+    const long long l0 = launches;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        graphs_error = cudaGetErrorString(cudaGetLastError());
+        graphs_failed = true;
+        return -1;
+    }
+    std::string what;
+    try {
+        body();
+    } catch (const std::exception& e) {
+        what = e.what();
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(stream, &graph);
+    std::vector<KernelTimer::Pair> pairs = timer.take(t0);
+    const long long nl = launches - l0;
+    launches = l0;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ei = cudaErrorUnknown;
+    if (what.empty() && ec == cudaSuccess && graph) ei = cudaGraphInstantiate(&exec, graph, 0ULL);
+    if (graph) cudaGraphDestroy(graph);
+    if (!what.empty() || ec != cudaSuccess || ei != cudaSuccess) {
+        graphs_error = !what.empty() ? what : cudaGetErrorString(ec != cudaSuccess ? ec : ei);
+        cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        timer.release(pairs);
+        graphs_failed = true;
+        return -1;
+    }
+    ChunkGraph g;
+    g.K = K;
+    g.x = x;
+    g.eis = eis;
+    g.gc = gc;
+    g.exec = exec;
+    g.launches = nl;
+    g.pairs = std::move(pairs);
+    chunk_graphs.push_back(std::move(g));
+    return (int)chunk_graphs.size() - 1;
+}
+
+void GpuSolver::graphs_clear() {
+    for (ChunkGraph& g : chunk_graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        timer.release(g.pairs);
+    }
+    chunk_graphs.clear();
+}
+
 BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, double2* x,
                                          const std::vector<int>& active, double tol, int maxiter) {
+    graphs_clear();   // graphs hold the arguments of the step that captured them
     ensure_vecs(K);
     ensure_vecs32(K);
     ensure_vecs32b(std::max(2, K / 2));
@@ -1384,7 +1460,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                     const double om = 2.0 * kPi * fz_freqs[fmap[lanes[j]]];
                     use_gc |= om > 0.0 && om <= gc.omega_max;
                 }
-        const bool eis = !use_gc && P.ssor_form == 1 && P.row_kernels == kRowsStaged;
+        const bool eis = !use_gc && P.ssor_form == 1 && P.row_kernels == kRowsStaged && P.ssor_relax == 1.0;
         // residual replacement needs the untransformed residual of the
         // right-preconditioned form
         const bool replace = P.residual_replacement == 1 && !eis;
@@ -1450,9 +1526,14 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             R.iters[k] += ls[j].iter;
             if (ls[j].status == kBreakdown) R.status[k] = kBreakdown;
         };
+        int pending_graph = -1;   // replayed graph whose timer pairs wait for this poll
         for (;;) {
             cuda_ok(cudaMemcpyAsync(ls.data(), d_states, sizeof(BicgState) * Kc, cudaMemcpyDeviceToHost, stream), "states");
             sync();
+            if (pending_graph >= 0) {
+                if (timer.on) timer.fold(chunk_graphs[pending_graph].pairs);
+                pending_graph = -1;
+            }
             int nrun = 0;
             for (int j = 0; j < Kc; ++j) nrun += (lanes[j] >= 0 && ls[j].status == kRunning);
             if (nrun == 0 || it >= maxiter) break;
@@ -1519,15 +1600,32 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 c32 = kctx32(Kc, fm.data());
                 if (use_gc) attach_gc(c32);
             }
-            for (int i = 0; i < chunk && it < maxiter; ++i, ++it) {
-                if (eis) eis_iteration(c32, cur, d_states);
-                else bicg_iteration(c32, cur, d_states);
+            auto body = [&]() {
+                for (int i = 0; i < chunk; ++i) {
+                    if (eis) eis_iteration(c32, cur, d_states);
+                    else bicg_iteration(c32, cur, d_states);
+                }
+            };
+            const int gi = (P.cuda_graphs && !graphs_failed && maxiter - it >= chunk)
+                               ? chunk_graph(Kc, cur.x, eis, use_gc, body) : -1;
+            if (gi >= 0) {
+                cuda_ok(cudaGraphLaunch(chunk_graphs[gi].exec, stream), "graph launch");
+                launches += chunk_graphs[gi].launches;
+                ++graph_replays;
+                pending_graph = gi;
+                it += chunk;
+            } else {
+                for (int i = 0; i < chunk && it < maxiter; ++i, ++it) {
+                    if (eis) eis_iteration(c32, cur, d_states);
+                    else bicg_iteration(c32, cur, d_states);
+                }
             }
         }
         for (int j = 0; j < dev::kMaxRhs; ++j) add[j] = (j < Kc && lanes[j] >= 0) ? 1 : 0;
         flush(c32, cur, Kc);
         for (int j = 0; j < Kc; ++j) record(j);
         if (step > 0) ++stats.refinements;
+        graphs_clear();
     }
     timer.collect();
     return R;
@@ -1542,6 +1640,8 @@ void GpuSolver::begin_call() {
 }
 
 void GpuSolver::end_call() {
+    stats.graphs_failed = graphs_failed ? 1 : 0;
+    stats.graph_replays = graph_replays;
     stats.divcorr_calls = dcc.calls;
     stats.divcorr_outer = dcc.outer;
     stats.divcorr_cg_iterations = dcc.cg_iterations;

@@ -6,6 +6,7 @@
 
 #include <complex>
 #include <memory>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -113,6 +114,22 @@ public:
 
     m3d_stats stats{};
     KernelTimer timer;
+    // CUDA graphs of the mixed-precision inner solve's 10-iteration chunk, one
+    // per batch shape of the running refinement step (destroyed at its end)
+    struct ChunkGraph {
+        int K = 0;
+        const void* x = nullptr;   // the vector set the batch runs in
+        bool eis = false, gc = false;
+        cudaGraphExec_t exec = nullptr;
+        long long launches = 0;    // kernel launches one replay issues
+        std::vector<KernelTimer::Pair> pairs;
+    };
+    std::vector<ChunkGraph> chunk_graphs;
+    bool graphs_failed = false;    // a capture failed: chunks run as direct launches from then on
+    std::string graphs_error;
+    long long graph_replays = 0;
+    int chunk_graph(int K, const void* x, bool eis, bool gc, const std::function<void()>& body);
+    void graphs_clear();
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     void timer_start();
     void begin_call();

@@ -327,7 +327,7 @@ class ForwardSolverFV:
                     divcorr_cg_iterations=s.divcorr_cg_iterations,
                     forward_iterations=s.forward_iterations, adjoint_iterations=s.adjoint_iterations,
                     divcorr_cg_sweeps=s.divcorr_cg_sweeps, divcorr_setup_ms=s.divcorr_setup_ms,
-                    replacements=s.replacements)
+                    replacements=s.replacements, graphs_failed=s.graphs_failed, graph_replays=s.graph_replays)
 
 
 def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:

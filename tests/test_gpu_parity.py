@@ -111,6 +111,40 @@ def test_residual_replacement_matches_reference(g_small, replacement):
         assert st["replacements"] > 0
 
 
+def test_cuda_graph_chunks_match_direct_launches(g_small):
+    """The mixed-precision inner solve's 10-iteration chunks replayed from
+    CUDA graphs (both streams captured) run the same kernels in the same
+    order as the launches issued one by one: bit-identical impedances and
+    gradient, the same iteration counts, and the replays are counted."""
+    g = g_small
+    out = {}
+    for graphs in (0, 1):
+        s = _gpu(g, precision=1, forward_interleaved=1, gradcorr=1, cuda_graphs=graphs)
+        Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
+        out[graphs] = (Z, grad, s.stats())
+    assert out[1][2]["graphs_failed"] == 0
+    assert out[1][2]["graph_replays"] > 0 and out[0][2]["graph_replays"] == 0
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2]["total_iterations"] == out[1][2]["total_iterations"]
+    ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
+    assert rel(out[1][0], g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
+
+
+@pytest.mark.parametrize("relax", [0.8, 1.3])
+def test_ssor_relaxation_matches_reference(g_small, relax):
+    """Over- and under-relaxed SSOR in the FP32 inner solve is another
+    preconditioner of the same system: the FP64 true residual still decides,
+    and impedances and gradient match the reference's."""
+    g = g_small
+    s = _gpu(g, precision=1, forward_interleaved=1, ssor_relax=relax)
+    Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
+    st = s.stats()
+    assert all(t <= 1e-10 for t in st["true_residual"][:st["n_rhs"]]), st
+    ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
+    assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
+    assert rel(grad, g["ref_grad"]) < G_TOL
+
+
 def test_forward_matches_reference_golden(g_small):
     g = g_small
     s = _gpu(g)
