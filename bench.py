@@ -104,6 +104,8 @@ def parse():
                     help="timed steps of the learned arm (FGMRES with the trained network; 0: skip)")
     ap.add_argument("--learned-pairs", type=int, default=1024, help="training pairs the learned arm collects")
     ap.add_argument("--fgmres-m", type=int, default=40, help="FGMRES restart length of the learned arm")
+    ap.add_argument("--kernel-timing", type=int, default=1, choices=[0, 1],
+                    help="CUDA events around every launch in the timed steps (kernel classes, roofline)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--cpu-procs", type=int, default=0, help="CPU worker processes (0: all host cores)")
     return ap.parse_args()
@@ -419,7 +421,7 @@ def solver_label(args, p, freqs):
             "cuda_graphs": bool(p["cuda_graphs"])}
 
 
-def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False):
+def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False, timing=True):
     """Warm-up, then `steps` timed gradient steps; returns timing and stats.
     per_freq: one gradient_batch call per frequency (the plain arm)."""
     import numpy as np
@@ -462,7 +464,7 @@ def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, pe
     barrier()
     if clocks:
         clocks.start()
-    s.set_kernel_timing(True)
+    s.set_kernel_timing(timing)
     launches0 = s.stats()["kernel_launches"]
     dev_ms, e2e_s, solves = 0.0, 0.0, 0
     iters, st = [], None
@@ -557,7 +559,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
     r = run_steps(s, sv, obs, err, args.steps, args.warmup, rank, world, dist, ClockSampler(local_rank),
-                  per_freq=plain_main)
+                  per_freq=plain_main, timing=bool(args.kernel_timing))
     t_dev, e2e_s = r["t_dev"], r["e2e_s"]
     solves = r["solves"]
     if dist:
@@ -655,7 +657,7 @@ def run_c3(args, rank, world, local_rank):
     every mesh's results are on the host); host copies are inside."""
     import numpy as np
     from maple3dmt_gb300 import mesh, workloads
-    from maple3dmt_gb300.solver import group_station_gradients, solver_for_survey
+    from maple3dmt_gb300.solver import group_station_gradients, solvers_for_surveys
     if world > 1:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "unavailable": "c3 runs on one GPU"}), flush=True)
@@ -666,7 +668,7 @@ def run_c3(args, rank, world, local_rank):
     t0 = time.perf_counter()
     svs = mesh.c3_surveys(freqs)
     p = solver_params(args, False)
-    solvers = [solver_for_survey(sv, device=local_rank, **p) for sv in svs]
+    solvers = solvers_for_surveys(svs, device=local_rank, **p)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(42)
     wr = [workloads.station_sources(s.ns, rng)[:args.c3_sources] for s in solvers]

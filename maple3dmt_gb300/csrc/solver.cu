@@ -1527,6 +1527,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
             if (ls[j].status == kBreakdown) R.status[k] = kBreakdown;
         };
         int pending_graph = -1;   // replayed graph whose timer pairs wait for this poll
+        int chunks_of_shape = 0;  // chunks run since the batch shape last changed
         for (;;) {
             cuda_ok(cudaMemcpyAsync(ls.data(), d_states, sizeof(BicgState) * Kc, cudaMemcpyDeviceToHost, stream), "states");
             sync();
@@ -1599,6 +1600,7 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                 Kc = Kn;
                 c32 = kctx32(Kc, fm.data());
                 if (use_gc) attach_gc(c32);
+                chunks_of_shape = 0;
             }
             auto body = [&]() {
                 for (int i = 0; i < chunk; ++i) {
@@ -1606,7 +1608,10 @@ BatchResult GpuSolver::solve_batch_mixed(int K, const int* fmap, double2* b, dou
                     else bicg_iteration(c32, cur, d_states);
                 }
             };
-            const int gi = (P.cuda_graphs && !graphs_failed && maxiter - it >= chunk)
+            // a shape is captured at its third chunk: short bursts (a few chunks
+            // between divergence corrections) would not repay the capture
+            ++chunks_of_shape;
+            const int gi = (P.cuda_graphs && !graphs_failed && maxiter - it >= chunk && chunks_of_shape >= 3)
                                ? chunk_graph(Kc, cur.x, eis, use_gc, body) : -1;
             if (gi >= 0) {
                 cuda_ok(cudaGraphLaunch(chunk_graphs[gi].exec, stream), "graph launch");

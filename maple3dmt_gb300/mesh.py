@@ -143,21 +143,25 @@ def layered_block_survey(*, half_width=50000.0, min_level=5, max_level=7, n_side
                   {"station_refine_radius": radius})
 
 
-def c3_surveys(freqs=None, *, min_level=None, max_level=None, seed=11, lib=None) -> list:
+def c3_surveys(freqs=None, *, min_level=None, max_level=None, seed=11, lib=None, workers=8) -> list:
     """C3: one survey per frequency, each mesh refined for that frequency's
     skin depth alone (so the meshes differ in size), the C2 earth with log10
     sigma of earth cells perturbed by seeded N(0, 0.3^2) noise, 121 stations
-    on an 11 x 11 grid at 1 km."""
+    on an 11 x 11 grid at 1 km.  The meshes are built on `workers` host
+    threads (the leaf builder is native code and runs outside the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
     from . import workloads
     sp = workloads.C3
     fr = np.asarray(sp.freqs if freqs is None else freqs, dtype=np.float64).reshape(-1)
-    out = []
-    for i, f in enumerate(fr):
-        out.append(layered_block_survey(min_level=sp.min_level if min_level is None else min_level,
-                                        max_level=sp.max_level if max_level is None else max_level,
-                                        n_side=sp.n_side, spacing=sp.spacing, freqs=np.array([f]),
-                                        noise_std=workloads.C3_NOISE_STD, seed=seed + i, lib=lib))
-    return out
+    lib = lib or _loader.load()
+
+    def one(i):
+        return layered_block_survey(min_level=sp.min_level if min_level is None else min_level,
+                                    max_level=sp.max_level if max_level is None else max_level,
+                                    n_side=sp.n_side, spacing=sp.spacing, freqs=np.array([fr[i]]),
+                                    noise_std=workloads.C3_NOISE_STD, seed=seed + i, lib=lib)
+    with ThreadPoolExecutor(max_workers=max(1, min(workers, len(fr)))) as ex:
+        return list(ex.map(one, range(len(fr))))
 
 
 def c5_survey(*, seed=7, rho_start=100.0, lib=None) -> Survey:

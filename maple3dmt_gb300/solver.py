@@ -339,6 +339,16 @@ def solver_for_survey(sv: mesh.Survey, device=0, **params) -> ForwardSolverFV:
     return s
 
 
+def solvers_for_surveys(surveys, device=0, workers=8, **params) -> list:
+    """One handle per survey (e.g. C3's per-frequency meshes), set up on
+    `workers` host threads: each set-up (layout, colouring, segments,
+    multigrid aggregation, uploads) is native code on its own handle and
+    stream and runs outside the GIL."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=max(1, min(workers, len(surveys)))) as ex:
+        return list(ex.map(lambda sv: solver_for_survey(sv, device=device, **params), surveys))
+
+
 def group_station_gradients(solvers, freqs, wr, max_concurrent=0):
     """Per-frequency meshes run concurrently on one device
     (m3d_group_station_gradients): solvers[m] at freqs[m], residual sources

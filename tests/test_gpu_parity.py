@@ -111,23 +111,47 @@ def test_residual_replacement_matches_reference(g_small, replacement):
         assert st["replacements"] > 0
 
 
-def test_cuda_graph_chunks_match_direct_launches(g_small):
+def test_cuda_graph_chunks_match_direct_launches(lib):
     """The mixed-precision inner solve's 10-iteration chunks replayed from
-    CUDA graphs (both streams captured) run the same kernels in the same
-    order as the launches issued one by one: bit-identical impedances and
-    gradient, the same iteration counts, and the replays are counted."""
-    g = g_small
+    CUDA graphs (both streams captured; a batch shape is captured at its third
+    chunk) run the same kernels in the same order as the launches issued one
+    by one: bit-identical impedances and fields, the same iteration counts,
+    and the replays are counted."""
+    from maple3dmt_gb300 import mesh
+    from maple3dmt_gb300.solver import solver_for_survey
+    sv = mesh.layered_block_survey(min_level=5, max_level=6, freqs=np.array([0.1, 10.0]))
     out = {}
     for graphs in (0, 1):
-        s = _gpu(g, precision=1, forward_interleaved=1, gradcorr=1, cuda_graphs=graphs)
-        Z, grad = s.gradient_batch(g["freqs"], g["obs_Z"], g["obs_err"])
-        out[graphs] = (Z, grad, s.stats())
+        s = solver_for_survey(sv, bicgstab_tol=1e-9, bicgstab_maxiter=5000, precision=1, cuda_graphs=graphs)
+        Z, E = s.forward_batch(sv.freqs, with_fields=True)
+        out[graphs] = (Z, E, s.stats())
     assert out[1][2]["graphs_failed"] == 0
     assert out[1][2]["graph_replays"] > 0 and out[0][2]["graph_replays"] == 0
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
     assert out[0][2]["total_iterations"] == out[1][2]["total_iterations"]
-    ns, nf = g["stations"].shape[0], g["freqs"].shape[0]
-    assert rel(out[1][0], g["ref_Z"].reshape(nf, ns, 4)) < Z_TOL
+    assert all(t <= 1e-9 for t in out[1][2]["true_residual"][:out[1][2]["n_rhs"]])
+
+
+@pytest.mark.parametrize("sweep_rows,coop", [(0, 1), (16384, 0), (16384, 1)])
+def test_sweep_groups_match_default_order(lib, sweep_rows, coop):
+    """SSOR sweep groups (super-blocks of about sweep_rows edges, colours
+    inside) and whole sweeps as one cooperative launch with grid barriers
+    are other orderings of the same multicolour SSOR: at the 1e-10 solve the
+    impedances match the default ordering's."""
+    from maple3dmt_gb300 import mesh
+    from maple3dmt_gb300.solver import solver_for_survey
+    sv = mesh.layered_block_survey(min_level=5, max_level=6, freqs=np.array([0.1, 10.0]))
+    base = solver_for_survey(sv, bicgstab_tol=1e-10, bicgstab_maxiter=5000, precision=1)
+    assert base.ne > 4 * 16384
+    Z0 = base.forward_batch(sv.freqs)
+    s = solver_for_survey(sv, bicgstab_tol=1e-10, bicgstab_maxiter=5000, precision=1, sweep_rows=sweep_rows,
+                          coop_sweep=coop)
+    if sweep_rows:
+        assert s.n_colours > base.n_colours
+    Z = s.forward_batch(sv.freqs)
+    st = s.stats()
+    assert all(t <= 1e-10 for t in st["true_residual"][:st["n_rhs"]]), st
+    assert rel(Z, Z0) < 1e-7
 
 
 @pytest.mark.parametrize("relax", [0.8, 1.3])
