@@ -96,7 +96,7 @@ def parse():
                     help="SSOR ordering by (super-block, colour), super-blocks of about this many edges (0: off)")
     ap.add_argument("--ssor-relax", type=float, default=1.0,
                     help="SSOR relaxation factor of the FP32 inner solve (1: the reference's symmetric GS)")
-    ap.add_argument("--cuda-graphs", type=int, default=1, choices=[0, 1],
+    ap.add_argument("--cuda-graphs", type=int, default=0, choices=[0, 1],
                     help="replay the inner solve's 10-iteration chunks from CUDA graphs")
     ap.add_argument("--coop-sweep", type=int, default=0, choices=[0, 1],
                     help="1: each staged SSOR sweep as one cooperative launch over its groups")

@@ -149,9 +149,11 @@ typedef struct m3d_params {
                                  edges, so a sweep's gathers stay in L2; 0: colour order over the mesh */
     int coop_sweep;           /* 1: each staged SSOR sweep is one cooperative launch over all its groups
                                  (bounded grid barriers between groups); 0: one launch per group */
-    int cuda_graphs;          /* 1 (default): the mixed-precision inner solve captures its 10-iteration
-                                 chunk (every launch of ten BiCGStab iterations, both streams) once per
-                                 batch shape in a CUDA graph and replays it; 0: launches issued one by one */
+    int cuda_graphs;          /* 1: the mixed-precision inner solve captures its 10-iteration chunk (every
+                                 launch of ten BiCGStab iterations, both streams) in a CUDA graph once per
+                                 batch shape and refinement step, from the shape's third chunk on, and
+                                 replays it; 0 (default): launches issued one by one (measured as fast on
+                                 C2 and faster with several meshes at once) */
     double ssor_relax;        /* relaxation factor omega of the SSOR sweeps of the mixed-precision inner
                                  solve, 0 < omega < 2 (1: the reference's symmetric Gauss-Seidel,
                                  ssor.h:58-78); the FP64 path always uses 1 */

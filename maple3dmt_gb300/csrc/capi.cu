@@ -104,7 +104,7 @@ extern "C" void m3d_params_default(m3d_params* p) {
     p->learned_period = 2;
     p->sweep_rows = 0;
     p->coop_sweep = 0;
-    p->cuda_graphs = 1;
+    p->cuda_graphs = 0;
     p->ssor_relax = 1.0;
 }
 
