@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kBlock) k_ssor_bwd(OpView<R> A, DiagView<R> D,
 
 // SpMV over slice-staged rows, same modes and reductions as k_spmv.
 template <class R, int K, int MODE>
-__global__ void __launch_bounds__(StagedShape<K>::NT, SpmvMinBlocks<R, K>::v) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
+__global__ void __launch_bounds__(StagedShape<K>::NT, StagedMinBlocks<R, K>::v) k_spmv_st(SegView<R> S, long n_slices, DiagView<R> D,
                                                                 BatchView B, const cplx<R>* __restrict__ x,
                                                                 cplx<R>* __restrict__ y,
                                                                 const cplx<R>* __restrict__ aux,
@@ -423,38 +423,15 @@ __global__ void __launch_bounds__(StagedShape<K>::NT, SpmvMinBlocks<R, K>::v) k_
         SegRows<R> lo, up;
         lo.bind(base);
         up.bind(base + (size_t)it.lo_len * 16);
-        // complex FP32 with two passes: every pass's row heads (first eight
-        // lower and eight upper entries) are gathered before the first row is
-        // summed; sums keep entry order, so results equal the one-pass form
-        constexpr int NP = Sh::PASSES;
-        constexpr bool HEADS = SpmvMinBlocks<R, K>::heads;
-        RowGather<R, K> hl[HEADS ? NP : 1], hu[HEADS ? NP : 1];
-        if constexpr (HEADS) {
 #pragma unroll
-            for (int ps = 0; ps < NP; ++ps) {
-                const int lr = ps * Sh::ROWS_PER_PASS + lr0;
-                hl[ps].load(lo.col, lo.begin_of(lr), lo.end[lr], x, rhs);
-                hu[ps].load(up.col, up.begin_of(lr), up.end[lr], x, rhs);
-            }
-        }
-#pragma unroll
-        for (int ps = 0; ps < NP; ++ps) {
+        for (int ps = 0; ps < Sh::PASSES; ++ps) {
             const int lr = ps * Sh::ROWS_PER_PASS + lr0;
             const int row = it.slice * kSlice + lr;
             const size_t i = (size_t)row * K + rhs;
             const C xi = x[i];
             const C av = (MODE != kSpmvPlain) ? aux[i] : cm<R>(0, 0);
             const C d = diag_of(D, row, om);
-            C s;
-            if constexpr (HEADS) {
-                const int bl = lo.begin_of(lr), el = lo.end[lr], bu = up.begin_of(lr), eu = up.end[lr];
-                s = hl[ps].sum(lo.val, bl, el, cm<R>(0, 0));
-                if (bl + 8 < el) s = seg_row_dot<R, K>(lo.col, lo.val, bl + 8, el, x, rhs, s);
-                s = hu[ps].sum(up.val, bu, eu, s);
-                if (bu + 8 < eu) s = seg_row_dot<R, K>(up.col, up.val, bu + 8, eu, x, rhs, s);
-            } else {
-                s = seg_row_dot_lu<R, K>(lo, up, lr, x, rhs);
-            }
+            const C s = seg_row_dot_lu<R, K>(lo, up, lr, x, rhs);
             const C yv = cadd(s, cmul(d, xi));
             if (MODE == kSpmvPlain) {
                 y[i] = yv;

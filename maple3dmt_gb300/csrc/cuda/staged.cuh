@@ -325,40 +325,6 @@ struct RowHead {
     }
 };
 
-// RowHead without the values: only the gathered v[c_j][rhs] of the first
-// eight entries are held while the gathers are in flight; sum() re-reads the
-// values from shared memory.  Same sums, same order, half the registers.
-template <class R, int K>
-struct RowGather {
-    cplx<R> x[8];
-    __device__ __forceinline__ void load(const int* __restrict__ col, int b, int e, const cplx<R>* v, int rhs) {
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-            const int k = b + 4 * g;
-            if (k < e) {
-                const int4 c = *reinterpret_cast<const int4*>(col + k);
-                x[4 * g + 0] = v[(size_t)c.x * K + rhs];
-                x[4 * g + 1] = v[(size_t)c.y * K + rhs];
-                x[4 * g + 2] = v[(size_t)c.z * K + rhs];
-                x[4 * g + 3] = v[(size_t)c.w * K + rhs];
-            } else {
-#pragma unroll
-                for (int u = 0; u < 4; ++u) x[4 * g + u] = cm<R>(0, 0);
-            }
-        }
-    }
-    __device__ __forceinline__ cplx<R> sum(const R* __restrict__ val, int b, int e, cplx<R> s) const {
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-            R a[4] = {0, 0, 0, 0};
-            if (b + 4 * g < e) lds4(val + b + 4 * g, a);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) { s.x += a[u] * x[4 * g + u].x; s.y += a[u] * x[4 * g + u].y; }
-        }
-        return s;
-    }
-};
-
 // s + sum over one staged row's entries [b, e) (b, e multiples of 4) of
 // a_j * v[c_j][rhs]: 16-byte shared-memory reads, eight gathers in flight,
 // sums in entry order.
@@ -440,14 +406,6 @@ __device__ __forceinline__ cplx<R> seg_row_dot_lu(const SegRows<R>& lo, const Se
 // complex FP32, 512 for complex FP64 (sixteen gathers in flight per thread).
 template <class R, int K> struct StagedMinBlocks {
     static constexpr int t = (sizeof(R) == 8 ? 512 : 768) / StagedShape<K>::NT;
-    static constexpr int v = t > 0 ? t : 1;
-};
-// The staged SpMV holds every pass's lower and upper row heads (sixteen
-// gathers per pass) where a thread has two passes in complex FP32 (K = 16):
-// 512 resident threads per SM there, the sweeps' cap otherwise.
-template <class R, int K> struct SpmvMinBlocks {
-    static constexpr bool heads = sizeof(R) == 4 && StagedShape<K>::PASSES > 1;
-    static constexpr int t = (heads ? 512 : (sizeof(R) == 8 ? 512 : 768)) / StagedShape<K>::NT;
     static constexpr int v = t > 0 ? t : 1;
 };
 
