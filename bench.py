@@ -96,8 +96,6 @@ def parse():
                     help="SSOR ordering by (super-block, colour), super-blocks of about this many edges (0: off)")
     ap.add_argument("--ssor-relax", type=float, default=1.0,
                     help="SSOR relaxation factor of the FP32 inner solve (1: the reference's symmetric GS)")
-    ap.add_argument("--l2-persist", type=int, default=0, choices=[0, 1],
-                    help="keep the V-cycle output in a persisting-L2 window")
     ap.add_argument("--cuda-graphs", type=int, default=0, choices=[0, 1],
                     help="replay the inner solve's 10-iteration chunks from CUDA graphs")
     ap.add_argument("--coop-sweep", type=int, default=0, choices=[0, 1],
@@ -396,8 +394,7 @@ def solver_params(args, plain):
                  gradcorr_presmooth=args.gradcorr_presmooth, divcorr_mixed=args.divcorr_mixed,
                  inner_tol_floor=args.inner_tol_floor, residual_replacement=args.residual_replacement,
                  gradcorr_overlap=args.gradcorr_overlap, sweep_rows=args.sweep_rows,
-                 coop_sweep=args.coop_sweep, ssor_relax=args.ssor_relax, cuda_graphs=args.cuda_graphs,
-                 l2_persist=args.l2_persist)
+                 coop_sweep=args.coop_sweep, ssor_relax=args.ssor_relax, cuda_graphs=args.cuda_graphs)
     return p
 
 
@@ -421,7 +418,7 @@ def solver_label(args, p, freqs):
             else "off",
             "residual_replacement": bool(p["residual_replacement"]),
             "sweep_rows": p["sweep_rows"], "coop_sweep": bool(p["coop_sweep"]), "ssor_relax": p["ssor_relax"],
-            "cuda_graphs": bool(p["cuda_graphs"]), "l2_persist": bool(p["l2_persist"])}
+            "cuda_graphs": bool(p["cuda_graphs"])}
 
 
 def run_steps(s, sv, obs, err, steps, warmup, rank, world, dist, clocks=None, per_freq=False, timing=True):

@@ -157,10 +157,6 @@ typedef struct m3d_params {
     double ssor_relax;        /* relaxation factor omega of the SSOR sweeps of the mixed-precision inner
                                  solve, 0 < omega < 2 (1: the reference's symmetric Gauss-Seidel,
                                  ssor.h:58-78); the FP64 path always uses 1 */
-    int l2_persist;           /* 1: the gradient-space V-cycle's output (gathered by every backward colour
-                                 launch) is kept in L2 by an access-policy window on the solver's streams
-                                 (persisting lines, a set-aside of this process's context, released with
-                                 the handle); 0 (default): plain caching */
 } m3d_params;
 
 typedef struct m3d_solver m3d_solver;

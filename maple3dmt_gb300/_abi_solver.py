@@ -41,7 +41,6 @@ class Params(C.Structure):
         ("coop_sweep", C.c_int),
         ("cuda_graphs", C.c_int),
         ("ssor_relax", C.c_double),
-        ("l2_persist", C.c_int),
     ]
 
 

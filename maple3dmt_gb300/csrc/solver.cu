@@ -203,7 +203,6 @@ GpuSolver::~GpuSolver() {
 void GpuSolver::free_all() {
     if (stream) cudaStreamSynchronize(stream);
     graphs_clear();
-    clear_l2_window();
     learn_free();
     dfree(md.perm); dfree(md.iperm); dfree(md.flags); dfree(md.dir); dfree(md.ez); dfree(md.s_diag);
     dfree(md.me_geom); dfree(md.adual); dfree(md.elen); dfree(md.nadj); dfree(md.adj_ptr); dfree(md.adj_cell);
@@ -840,43 +839,8 @@ void GpuSolver::build_gc() {
         cuda_ok(cudaEventCreateWithFlags(&gc_fork, cudaEventDisableTiming), "event");
         cuda_ok(cudaEventCreateWithFlags(&gc_join, cudaEventDisableTiming), "event");
     }
-    if (P.l2_persist == 1) set_l2_window(gc.out0, (size_t)L.nn * dev::kMaxRhs * sizeof(float2));
     sync();
     gc_ok = true;
-}
-
-// Persisting-L2 window over [base, base + bytes) on the solver's two streams:
-// lines of the window stay in the L2 set-aside (this context's, sized to
-// the window within the device maximum) while the rest of the traffic
-// streams past them.  A performance hint only; released by
-// clear_l2_window with the handle.
-void GpuSolver::set_l2_window(void* base, size_t bytes) {
-    cudaDeviceProp prop{};
-    cuda_ok(cudaGetDeviceProperties(&prop, device), "properties");
-    if (prop.persistingL2CacheMaxSize <= 0 || prop.accessPolicyMaxWindowSize <= 0) return;
-    const size_t persist = std::min<size_t>(bytes, (size_t)prop.persistingL2CacheMaxSize);
-    cuda_ok(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, persist), "persisting L2 size");
-    cudaStreamAttrValue a{};
-    a.accessPolicyWindow.base_ptr = base;
-    a.accessPolicyWindow.num_bytes = std::min<size_t>(bytes, (size_t)prop.accessPolicyMaxWindowSize);
-    a.accessPolicyWindow.hitRatio = std::min(1.0f, (float)persist / (float)a.accessPolicyWindow.num_bytes);
-    a.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
-    a.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
-    for (cudaStream_t s : {stream, gc_stream})
-        if (s) cuda_ok(cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &a), "L2 window");
-    l2_window = true;
-}
-
-void GpuSolver::clear_l2_window() {
-    if (!l2_window) return;
-    cudaStreamAttrValue a{};
-    a.accessPolicyWindow.num_bytes = 0;
-    for (cudaStream_t s : {stream, gc_stream})
-        if (s) cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &a);
-    cudaCtxResetPersistingL2Cache();
-    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-    cudaGetLastError();
-    l2_window = false;
 }
 
 // The gradient-space term on a FP32 batch context; with gradcorr_overlap its

@@ -130,9 +130,6 @@ public:
     long long graph_replays = 0;
     int chunk_graph(int K, const void* x, bool eis, bool gc, const std::function<void()>& body);
     void graphs_clear();
-    bool l2_window = false;   // an access-policy window is set on the streams
-    void set_l2_window(void* base, size_t bytes);
-    void clear_l2_window();
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     void timer_start();
     void begin_call();
