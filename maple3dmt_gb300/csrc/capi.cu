@@ -145,7 +145,7 @@ extern "C" int m3d_solver_setup(m3d_solver* h, const m3d_leaves* leaves, const m
         params->gradcorr_overlap < 0 || params->gradcorr_overlap > 1 || params->krylov < 0 ||
         params->krylov > 1 || params->fgmres_m < 2 || params->fgmres_m > 47 || params->learned_period < 0 || params->sweep_rows < 0 ||
         params->coop_sweep < 0 || params->coop_sweep > 1 || params->cuda_graphs < 0 || params->cuda_graphs > 1 ||
-        !(params->ssor_relax > 0.0 && params->ssor_relax < 2.0) || params->gradcorr_smooth0 < 0 || params->gradcorr_smooth0 > 1)
+        !(params->ssor_relax > 0.0 && params->ssor_relax < 2.0))
         return fail(h, M3D_ERR_ARG, "invalid solver parameters");
     return guarded(h, [&](m3d::GpuSolver& s) { s.setup(leaves, params); });
 }
