@@ -484,25 +484,18 @@ __device__ __forceinline__ void ssor_fwd_rows(const SegItem& it, const unsigned 
     using Sh = StagedShape<K>;
     SegRows<R> lo;
     lo.bind(base);
-    // every pass's gathers are issued before the first row is written
-    RowHead<R, K> h[Sh::PASSES];
-    C iv[Sh::PASSES], dv[Sh::PASSES];
+    // one pass's gathers at a time: at 46 registers the forward sweep keeps
+    // more resident blocks than with both passes' heads held (69 registers),
+    // which measured faster for its short lower rows
 #pragma unroll
     for (int ps = 0; ps < Sh::PASSES; ++ps) {
         const int lr = ps * Sh::ROWS_PER_PASS + lr0;
         const int row = it.slice * kSlice + lr;
-        iv[ps] = in[(size_t)row * K + rhs];
-        dv[ps] = diag_of(D, row, om);
-        h[ps].load(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs);
-    }
-#pragma unroll
-    for (int ps = 0; ps < Sh::PASSES; ++ps) {
-        const int lr = ps * Sh::ROWS_PER_PASS + lr0;
-        const int row = it.slice * kSlice + lr;
-        C s = h[ps].sum(cm<R>(0, 0));
-        const int b = lo.begin_of(lr) + 8, e = lo.end[lr];
-        if (b < e) s = seg_row_dot<R, K>(lo.col, lo.val, b, e, y, rhs, s);
-        y[(size_t)row * K + rhs] = cmul(csub(iv[ps], s), cscale(inv_c(dv[ps]), rx));
+        const size_t i = (size_t)row * K + rhs;
+        const C iv = in[i];
+        const C d = diag_of(D, row, om);
+        const C s = seg_row_dot<R, K>(lo.col, lo.val, lo.begin_of(lr), lo.end[lr], y, rhs, cm<R>(0, 0));
+        y[i] = cmul(csub(iv, s), cscale(inv_c(d), rx));
     }
 }
 
