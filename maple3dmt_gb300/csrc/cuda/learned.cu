@@ -12,6 +12,9 @@
 //                    accumulator and frees the stage with tcgen05.commit;
 //   all 4 warps      epilogue: tcgen05.ld of their 32 TMEM lanes, bias,
 //                    ReLU or the ReLU mask of the backward pass, BF16 store.
+// Grids up to 64 voxels wide use k_conv3d_halo instead: each tile's input
+// and its border arrive once per x shift and the taps are line offsets into
+// those boxes (see the kernel's comment).
 // GEMM view: M = voxels, N = output channels, K = 27 taps x 32 channels.
 // Weight gradient: dW[t] = sum_v dY[v]^T X[v + off_t] as one GEMM with
 // M = 27 x 32 (tap, input channel) rows padded to 896, N = 32 output channels,
@@ -55,6 +58,7 @@ void ck(cudaError_t e, const char* what) {
 
 struct ConvArgs {
     int D, H, W, bw, bh, tiles_h;
+    int n_tiles;                  // tiles of the launch
     const float* bias;            // [32] or null
     int relu;
     const __nv_bfloat16* mask;    // keep where mask > 0 (null: keep all)
@@ -191,6 +195,201 @@ __global__ void __launch_bounds__(128, 1) k_conv3d_tc(const __grid_constant__ CU
     tc::tc_fence_before();
     __syncthreads();
     if (warp == 1) tc::tmem_dealloc(tmem, 32);
+}
+
+// Halo form of the forward / input-gradient convolution, for grids up to 64
+// voxels wide (one tile = 128 voxels = 128 / W lines of W voxels): instead
+// of one 8 KB copy per tap, a tile's input comes in as three boxes, one per
+// x shift (dx = -1, 0, 1), each holding the tile's lines with a one-voxel
+// border in y and z.  The 27 taps' A operands are then line offsets into
+// these boxes (tap (dz, dy) of box dx starts at line dz (bh + 2) + dy; the
+// 128 rows are contiguous and 1 KB aligned, so the SWIZZLE_64B descriptor
+// stays valid), and each input byte crosses from L2 three times per tile
+// instead of twenty-seven.  Persistent CTAs of six warps, one per SM:
+//   warp 4 / lane 0  TMA producer: the weights once, then per tile the three
+//                    boxes, each reused as soon as its nine taps' MMAs are done;
+//   warp 5           allocates 64 TMEM columns (two accumulators); lane 0
+//                    issues the 54 MMAs of a tile into one accumulator while
+//                    the epilogue drains the other;
+//   warps 0-3        epilogue: tcgen05.ld of their 32 lanes, release of the
+//                    accumulator, bias / ReLU / mask, BF16 store.
+// Every wait is bounded; a timeout flags an error and every role stops.
+constexpr int kHaloMaxW = 64;
+__host__ __device__ constexpr int halo_box_bytes(int W) { return (128 + 2 * W) * 3 * 64; }
+constexpr int halo_smem(int W) { return kTaps * kTapB + 3 * halo_box_bytes(W) + 1024; }
+
+__global__ void __launch_bounds__(192, 1) k_conv3d_halo(const __grid_constant__ CUtensorMap hmap,
+                                                        const __grid_constant__ CUtensorMap wmap, ConvArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                           ~static_cast<uintptr_t>(1023));
+    unsigned char* sB = base;
+    unsigned char* sX = base + kTaps * kTapB;
+    const int box_bytes = halo_box_bytes(a.W);
+    __shared__ __align__(8) uint64_t bfull[3], bempty[3], tfull[2], tempty[2], wbar, mdone;
+    __shared__ uint32_t tmem_base;
+    __shared__ volatile int fail;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int per_n = a.D * a.tiles_h;
+    const int box_lines_y = a.bh + 2;
+    if (threadIdx.x == 0) {
+        for (int d = 0; d < 3; ++d) {
+            tc::mbar_init(&bfull[d], 1);
+            tc::mbar_init(&bempty[d], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 128);
+        }
+        tc::mbar_init(&wbar, 1);
+        tc::mbar_init(&mdone, 1);
+        tc::fence_barrier_init();
+        fail = 0;
+    }
+    if (warp == 5) {
+        tc::tmem_alloc(&tmem_base, 64);
+        tc::tmem_relinquish();
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = tmem_base;
+    int last_issue[3] = {-1, -1, -1};   // producer: the tile each box was last loaded for
+    if (warp == 4) {
+        if (lane == 0) {
+            tc::mbar_expect_tx(&wbar, kTaps * kTapB);
+            for (int t = 0; t < kTaps; ++t) tc::tma_load_2d(sB + t * kTapB, &wmap, &wbar, 0, t * kCh);
+            int it = 0;
+            for (int tile = blockIdx.x; tile < a.n_tiles && !fail; tile += gridDim.x, ++it) {
+                const int n = tile / per_n, rem = tile % per_n;
+                const int z = rem / a.tiles_h, y0 = (rem % a.tiles_h) * a.bh;
+                for (int d = 0; d < 3; ++d) {
+                    if (it > 0 && !tc::mbar_wait(&bempty[d], (unsigned)(it - 1) & 1u)) {
+                        atomicOr(a.err, tc::kErrWait);
+                        fail = 1;
+                        break;
+                    }
+                    tc::mbar_expect_tx(&bfull[d], box_bytes);
+                    tc::tma_load_5d(sX + d * box_bytes, &hmap, &bfull[d], 0, d - 1, y0 - 1, z - 1, n);
+                    last_issue[d] = it;
+                }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = tc::idesc_bf16(128, 32);
+            bool ok = tc::mbar_wait(&wbar, 0);
+            int it = 0;
+            for (int tile = blockIdx.x; tile < a.n_tiles && ok && !fail; tile += gridDim.x, ++it) {
+                const int b = it & 1;
+                if (it >= 2 && !tc::mbar_wait(&tempty[b], (unsigned)((it >> 1) - 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t dt = tmem + 32u * (uint32_t)b;
+                bool first = true;
+                for (int d = 0; d < 3 && ok; ++d) {
+                    if (!tc::mbar_wait(&bfull[d], (unsigned)it & 1u)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    for (int dz = 0; dz < 3; ++dz)
+                        for (int dy = 0; dy < 3; ++dy) {
+                            const int t = dz * 9 + dy * 3 + d;
+                            const int line = dz * box_lines_y + dy;
+                            const uint64_t ad = tc::sdesc_sw64(sX + d * box_bytes + line * a.bw * 64);
+                            const uint64_t bd = tc::sdesc_sw64(sB + t * kTapB);
+                            tc::mma_bf16(dt, ad, bd, idesc, first ? 0u : 1u);
+                            tc::mma_bf16(dt, ad + 2, bd + 2, idesc, 1u);   // second half of the 64-byte rows
+                            first = false;
+                        }
+                    tc::mma_commit(&bempty[d]);
+                }
+                if (!ok) break;
+                tc::mma_commit(&tfull[b]);
+            }
+            if (!ok) {
+                atomicOr(a.err, tc::kErrWait);
+                fail = 1;
+            }
+        }
+    } else {
+        int it = 0;
+        for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++it) {
+            const int b = it & 1;
+            const bool got = tc::mbar_wait(&tfull[b], (unsigned)(it >> 1) & 1u);
+            // the TMEM load is warp-collective: the warp decides together
+            if (!__all_sync(0xffffffffu, (got && !fail) ? 1 : 0)) {
+                if (lane == 0) {
+                    atomicOr(a.err, tc::kErrWait);
+                    fail = 1;
+                }
+                break;
+            }
+            tc::tc_fence_after();
+            float acc[32];
+            tc::tmem_ld32(tmem + 32u * (uint32_t)b + ((uint32_t)(warp * 32) << 16), acc);
+            tc::tc_fence_before();
+            tc::mbar_arrive(&tempty[b]);
+            const int n = tile / per_n, rem = tile % per_n;
+            const int z = rem / a.tiles_h, y0 = (rem % a.tiles_h) * a.bh;
+            const int m = warp * 32 + lane;
+            const int yy = y0 + m / a.bw, xx = m % a.bw;
+            const size_t v = (((size_t)n * a.D + z) * a.H + yy) * a.W + xx;
+            float keep[32];
+#pragma unroll
+            for (int c = 0; c < 32; ++c) keep[c] = 1.0f;
+            if (a.mask) {
+                const uint4* mp = reinterpret_cast<const uint4*>(a.mask + v * kCh);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 u = mp[q];
+                    const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) keep[8 * q + j] = __bfloat162float(h[j]) > 0.0f ? 1.0f : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 32; ++c) {
+                float x = acc[c] + (a.bias ? a.bias[c] : 0.0f);
+                if (a.relu) x = fmaxf(x, 0.0f);
+                acc[c] = x * keep[c];
+            }
+            if (a.out) {
+                uint4* op = reinterpret_cast<uint4*>(a.out + v * kCh);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint4 u;
+                    __nv_bfloat16* h = reinterpret_cast<__nv_bfloat16*>(&u);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) h[j] = __float2bfloat16_rn(acc[8 * q + j]);
+                    op[q] = u;
+                }
+            }
+            if (a.out32) {
+#pragma unroll
+                for (int c = 0; c < 32; ++c)
+                    if (c < a.n32) a.out32[v * a.n32 + c] = acc[c];
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 4 && lane == 0) {
+        // every issued copy lands before the CTA leaves
+        tc::mbar_wait(&wbar, 0);
+        for (int d = 0; d < 3; ++d)
+            if (last_issue[d] >= 0) tc::mbar_wait(&bfull[d], (unsigned)last_issue[d] & 1u);
+    }
+    if (warp == 5 && lane == 0) {
+        // every issued MMA completes before the accumulators are freed
+        tc::mma_commit(&mdone);
+        tc::mbar_wait(&mdone, 0);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 5) tc::tmem_dealloc(tmem, 64);
 }
 
 struct GemmArgs {
@@ -447,11 +646,13 @@ EncodeFn encoder() {
 
 }  // namespace
 
-void encode_act_map(CUtensorMap* m, const void* base, int n, int D, int H, int W, int bw, int bh) {
+// box (32 channels, bw, bh, 1, 1); with halo = 1 (32, bw, bh + 2, 3, 1)
+void encode_act_map(CUtensorMap* m, const void* base, int n, int D, int H, int W, int bw, int bh, int halo) {
     const cuuint64_t dims[5] = {(cuuint64_t)kCh, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D, (cuuint64_t)n};
     const cuuint64_t strides[4] = {(cuuint64_t)kCh * 2, (cuuint64_t)W * kCh * 2, (cuuint64_t)H * W * kCh * 2,
                                    (cuuint64_t)D * H * W * kCh * 2};
-    const cuuint32_t box[5] = {(cuuint32_t)kCh, (cuuint32_t)bw, (cuuint32_t)bh, 1, 1};
+    const cuuint32_t box[5] = {(cuuint32_t)kCh, (cuuint32_t)bw, (cuuint32_t)(bh + 2 * halo),
+                               (cuuint32_t)(1 + 2 * halo), 1};
     const cuuint32_t es[5] = {1, 1, 1, 1, 1};
     const CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box,
                                  es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
@@ -637,16 +838,24 @@ void Cnn::ensure(int n, int D_, int H_, int W_) {
     for (int l = 0; l <= L; ++l) encode_act_map(&act_map[l], act[l], n, D, H, W, bw, bh);
     delta_map.resize(2);
     for (int k = 0; k < 2; ++k) encode_act_map(&delta_map[k], delta[k], n, D, H, W, bw, bh);
+    act_hmap.assign(L + 1, CUtensorMap{});
+    delta_hmap.assign(2, CUtensorMap{});
+    if (W <= kHaloMaxW) {
+        for (int l = 0; l <= L; ++l) encode_act_map(&act_hmap[l], act[l], n, D, H, W, bw, bh, 1);
+        for (int k = 0; k < 2; ++k) encode_act_map(&delta_hmap[k], delta[k], n, D, H, W, bw, bh, 1);
+    }
     encode_2d_map(&xcol_map, xcol, (long long)G, kMPad, 128);
     encode_2d_map(&dyt_map, dyt, (long long)G, kCh, kCh);
     ck(cudaStreamSynchronize(st), "sync");
 }
 
-void Cnn::conv(int l, bool transposed, const CUtensorMap& in_map, const __nv_bfloat16* mask, __nv_bfloat16* out,
-               float* o32, int n32, int n) {
+void Cnn::conv(int l, bool transposed, const CUtensorMap& in_map, const CUtensorMap& in_hmap,
+               const __nv_bfloat16* mask, __nv_bfloat16* out, float* o32, int n32, int n) {
     static bool attr = false;
     if (!attr) {
         ck(cudaFuncSetAttribute(k_conv3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem), "attr");
+        ck(cudaFuncSetAttribute(k_conv3d_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, halo_smem(kHaloMaxW)),
+           "attr");
         attr = true;
     }
     ConvArgs a{};
@@ -658,8 +867,16 @@ void Cnn::conv(int l, bool transposed, const CUtensorMap& in_map, const __nv_bfl
     a.out32 = o32;
     a.n32 = n32;
     a.err = err;
-    const int grid = n * D * (H / bh);
-    k_conv3d_tc<<<grid, 128, kConvSmem, st>>>(in_map, transposed ? wt_map[l] : w_map[l], a);
+    a.n_tiles = n * D * (H / bh);
+    if (W <= kHaloMaxW) {
+        // persistent CTAs, one per SM (up to 198 KB of shared memory each)
+        static int sms = 0;
+        if (!sms) ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+        const int grid = std::max(1, std::min(a.n_tiles, sms));
+        k_conv3d_halo<<<grid, 192, halo_smem(W), st>>>(in_hmap, transposed ? wt_map[l] : w_map[l], a);
+    } else {
+        k_conv3d_tc<<<a.n_tiles, 128, kConvSmem, st>>>(in_map, transposed ? wt_map[l] : w_map[l], a);
+    }
     ck(cudaGetLastError(), "conv launch");
 }
 
@@ -667,7 +884,7 @@ const float* Cnn::forward(int n) {
     if (n > n_cap) throw std::invalid_argument("cnn: more samples than ensure() sized");
     ck(cudaSetDevice(dev), "cudaSetDevice");
     for (int l = 0; l < L; ++l)
-        conv(l, false, act_map[l], nullptr, act[l + 1], l == L - 1 ? out32 : nullptr, cout, n);
+        conv(l, false, act_map[l], act_hmap[l], nullptr, act[l + 1], l == L - 1 ? out32 : nullptr, cout, n);
     return out32;
 }
 
@@ -709,8 +926,8 @@ void Cnn::backward(int n, const float* dout, float* dx) {
         wgrad(l, act[l], delta[cur], n);
         if (l > 0 || dx) {
             // input gradient; for l > 0 masked by ReLU'(act[l]) into the next delta
-            conv(l, true, delta_map[cur], l > 0 ? act[l] : nullptr, delta[cur ^ 1], (l == 0 && dx) ? dx : nullptr,
-                 kCh, n);
+            conv(l, true, delta_map[cur], delta_hmap[cur], l > 0 ? act[l] : nullptr, delta[cur ^ 1],
+                 (l == 0 && dx) ? dx : nullptr, kCh, n);
             cur ^= 1;
         }
     }

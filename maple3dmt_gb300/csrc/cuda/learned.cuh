@@ -84,11 +84,14 @@ private:
     int splits = 0;
     long long adam_t = 0;
     std::vector<CUtensorMap> act_map, delta_map, w_map, wt_map;
+    // the same buffers with a halo box (W <= 64): a tile's input and its
+    // one-voxel border in y and z, loaded once per x shift
+    std::vector<CUtensorMap> act_hmap, delta_hmap;
     CUtensorMap xcol_map{}, dyt_map{};
     void free_grid();
     void upload_bf16();
-    void conv(int l, bool transposed, const CUtensorMap& in_map, const __nv_bfloat16* mask, __nv_bfloat16* out,
-              float* o32, int n32, int n);
+    void conv(int l, bool transposed, const CUtensorMap& in_map, const CUtensorMap& in_hmap,
+              const __nv_bfloat16* mask, __nv_bfloat16* out, float* o32, int n32, int n);
     void wgrad(int l, const __nv_bfloat16* x, const __nv_bfloat16* d, int n);
 };
 
@@ -130,7 +133,7 @@ void grid_means(const GridMap& g, const double2* v, int K, float* out, cudaStrea
 void grid_prolong(const GridMap& g, const float* out, int K, float2* z, cudaStream_t s);
 
 // Tensor maps (driver entry point reached through the runtime, no -lcuda).
-void encode_act_map(CUtensorMap* m, const void* base, int n, int D, int H, int W, int bw, int bh);
+void encode_act_map(CUtensorMap* m, const void* base, int n, int D, int H, int W, int bw, int bh, int halo = 0);
 void encode_2d_map(CUtensorMap* m, const void* base, long long cols, int rows, int box_rows);
 
 }  // namespace learn

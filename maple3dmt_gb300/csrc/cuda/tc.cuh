@@ -50,6 +50,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     return ok != 0;
 }
 
+// One arrival of this thread on `bar`.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    unsigned long long state;
+    asm volatile("mbarrier.arrive.shared::cta.b64 %0, [%1];" : "=l"(state) : "r"(smem_u32(bar)) : "memory");
+    (void)state;
+}
+
 // Waits for phase `parity` of `bar`, at most kWaitCycles; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     if (mbar_try_wait(bar, parity)) return true;
