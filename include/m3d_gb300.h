@@ -19,6 +19,9 @@
  *    before it returns; m3d_last_error() gives the message of the last
  *    failure on that handle.
  *  - A solver handle is single-threaded, like the reference (not re-entrant).
+ *    Different handles may be driven from different host threads at the
+ *    same time (each owns its CUDA streams); m3d_group_station_gradients
+ *    does exactly that for per-frequency meshes.
  *  - Solver state follows the reference's ordering rules: a frequency must be
  *    solved (m3d_compute_single_frequency) or factorised before the adjoint,
  *    sensitivity and J.v calls of that frequency
