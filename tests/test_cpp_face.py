@@ -75,6 +75,15 @@ int main(int argc, char** argv) {
         auto Z = s.compute_single_frequency(freq);
         for (auto& z : Z)
             for (int k = 0; k < 4; ++k) std::printf("%.17g %.17g\n", z[k].real(), z[k].imag());
+        // one residual source per station (unit weight on Zxy at that station): per-station gradients
+        std::vector<std::vector<std::array<m3d::Complex, 4>>> wr(ns, std::vector<std::array<m3d::Complex, 4>>(ns));
+        for (int j = 0; j < ns; ++j) wr[j][j][1] = m3d::Complex(1.0, -0.5);
+        auto g = s.station_gradients(wr);
+        for (int j = 0; j < ns; ++j) {
+            double sum = 0.0;
+            for (double v : g[j]) sum += v;
+            std::printf("G %d %.17g\n", j, sum);
+        }
     } catch (const m3d::SolverError& e) {
         std::printf("ERROR %d %s\n", e.code, e.what());
         return 1;
@@ -88,7 +97,8 @@ int main(int argc, char** argv) {
 def test_cpp_face_solves_on_device(lib, tmp_path):
     """The C++ face a maintainer drops under InversionFV: set-up from a leaf
     list, conductivity, stations and one forward solve on the GPU give the
-    reference's impedances (tests/golden/small_block.npz) to 1e-6."""
+    reference's impedances (tests/golden/small_block.npz) to 1e-6, and its
+    per-station gradients equal the Python face's."""
     import numpy as np
     from conftest import load_golden, rel
     from maple3dmt_gb300 import _loader
@@ -115,7 +125,24 @@ def test_cpp_face_solves_on_device(lib, tmp_path):
         f.write(np.int32(st.shape[0]).tobytes()); f.write(st.tobytes())
         f.write(np.float64(freq).tobytes()); f.write(np.float64(g["sigma_bg"]).tobytes())
     out = subprocess.run([str(exe), str(tmp_path / "in.bin")], check=True, capture_output=True, text=True).stdout
-    v = np.array([[float(a) for a in line.split()] for line in out.strip().splitlines()])
+    lines = out.strip().splitlines()
+    v = np.array([[float(a) for a in line.split()] for line in lines if not line.startswith("G ")])
     Z = (v[:, 0] + 1j * v[:, 1]).reshape(-1, 4)
     ns, nf = st.shape[0], g["freqs"].shape[0]
     assert rel(Z, g["ref_Z"].reshape(nf, ns, 4)[0]) < 1e-6
+    # per-station gradients through the C++ face equal the Python face's on the same handle settings
+    gs = np.array([float(line.split()[2]) for line in lines if line.startswith("G ")])
+    from maple3dmt_gb300.solver import ForwardSolverFV
+    from conftest import leaves_from_golden
+    py = ForwardSolverFV(0)
+    py.setup(leaves_from_golden(g), bicgstab_tol=1e-10, bicgstab_maxiter=5000, sigma_bg=float(g["sigma_bg"]),
+             precision=1)
+    py.set_sigma(g["sigma"])
+    py.set_stations(g["stations"])
+    py.compute_single_frequency(freq)
+    wr = np.zeros((ns, ns, 4), np.complex128)
+    for j in range(ns):
+        wr[j, j, 1] = 1.0 - 0.5j
+    gp = py.station_gradients(wr).sum(axis=1)
+    assert gs.shape == (ns,) and np.abs(gp).max() > 0
+    assert rel(gs, gp) < 1e-9

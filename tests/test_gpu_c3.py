@@ -85,6 +85,15 @@ def test_station_gradients_need_a_solved_frequency(g_small):
     assert ex.value.code == 7
 
 
+def test_station_gradients_of_no_source(g_small):
+    """Zero sources is an empty result, not an error (the reference's loop
+    over no stations does nothing)."""
+    s = _gpu(g_small)
+    s.compute_single_frequency(float(g_small["freqs"][0]))
+    G = s.station_gradients(np.zeros((0, s.ns, 4), np.complex128))
+    assert G.shape == (0, s.nc)
+
+
 @pytest.fixture(scope="module")
 def small_c3(lib):
     from maple3dmt_gb300 import mesh
