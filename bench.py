@@ -62,7 +62,10 @@ def parse():
     ap.add_argument("--c3-freqs", type=int, default=16, help="c3: frequencies (meshes) of the 16, evenly spread")
     ap.add_argument("--c3-sources", type=int, default=8,
                     help="c3: station sources per mesh (2 adjoint solves each; the full workload has 121)")
-    ap.add_argument("--c3-concurrent", type=int, default=4, help="c3: meshes run at once (0: all)")
+    ap.add_argument("--c3-concurrent", type=int, default=4, help="c3: handles run at once (0: all)")
+    ap.add_argument("--c3-replicas", type=int, default=1,
+                    help="c3: handles per mesh, the mesh's station sources split across them (each also solves "
+                         "the mesh's forward problem; those repeated forward solves are not counted)")
     # profiling runs only: a smaller mesh of the same survey (octree levels)
     ap.add_argument("--min-level", type=int, default=0, help="override the configuration's min octree level")
     ap.add_argument("--max-level", type=int, default=0, help="override the configuration's max octree level")
@@ -668,15 +671,21 @@ def run_c3(args, rank, world, local_rank):
     t0 = time.perf_counter()
     svs = mesh.c3_surveys(freqs)
     p = solver_params(args, False)
-    solvers = solvers_for_surveys(svs, device=local_rank, **p)
+    reps = max(1, args.c3_replicas)
+    solvers = solvers_for_surveys([sv for sv in svs for _ in range(reps)], device=local_rank, **p)
     setup_s = time.perf_counter() - t0
     rng = np.random.default_rng(42)
-    wr = [workloads.station_sources(s.ns, rng)[:args.c3_sources] for s in solvers]
-    n_solves = sum(2 + 2 * w.shape[0] for w in wr)
+    wr, hfreqs = [], []
+    for i, sv in enumerate(svs):
+        w = workloads.station_sources(len(sv.stations), rng)[:args.c3_sources]
+        wr += [np.ascontiguousarray(part) for part in np.array_split(w, reps)]
+        hfreqs += [float(freqs[i])] * reps
+    # the workload's solves: 2 forward per mesh, 2 adjoint per station source
+    n_solves = sum(2 + 2 * min(args.c3_sources, len(sv.stations)) for sv in svs)
     clocks = ClockSampler(local_rank)
 
     def step():
-        return group_station_gradients(solvers, freqs, wr, max_concurrent=args.c3_concurrent)
+        return group_station_gradients(solvers, hfreqs, wr, max_concurrent=args.c3_concurrent)
 
     for _ in range(args.warmup):
         step()
@@ -692,9 +701,9 @@ def run_c3(args, rank, world, local_rank):
     launches = sum(st["kernel_launches"] for st in sts) - launches0
     tr = [t for st in sts for t in st["true_residual"][:st["n_rhs"]]]
     total = sum(times)
-    # the sequential schedule of the same handles (one mesh at a time) for comparison
+    # the sequential schedule of the same handles (one at a time) for comparison
     t = time.perf_counter()
-    group_station_gradients(solvers, freqs, wr, max_concurrent=1)
+    group_station_gradients(solvers, hfreqs, wr, max_concurrent=1)
     one_at_a_time = n_solves / (time.perf_counter() - t)
     ne = [s.ne for s in solvers]
     h2d = sum(w.size * 16 for w in wr)
@@ -708,14 +717,15 @@ def run_c3(args, rank, world, local_rank):
                                f"log10 sigma + N(0, 0.3^2), 121 stations; per mesh 2 forward + "
                                f"{2 * args.c3_sources} station adjoint solves ({args.c3_sources} station sources) "
                                f"and their per-station gradients ({n_solves} solves per step)",
-                   "tol": TOL, "edges_per_mesh": ne, "meshes_at_once": args.c3_concurrent,
-                   "timing": "host clock between device synchronisations (one stream per mesh)",
+                   "tol": TOL, "edges_per_mesh": ne[::reps], "handles_per_mesh": reps,
+                   "handles_at_once": args.c3_concurrent,
+                   "timing": "host clock between device synchronisations (one stream per handle)",
                    "l2": "inputs larger than L2"},
-        "solver": {**solver_label(args, p, freqs), "parallelism": "meshes run concurrently, one host thread and "
-                                                                   "CUDA stream per mesh"},
+        "solver": {**solver_label(args, p, freqs), "parallelism": "handles run concurrently, one host thread and "
+                                                                   "CUDA stream per handle"},
         "e2e": {"value": n_solves * args.steps / total, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "one_mesh_at_a_time": {"value": one_at_a_time, "unit": UNIT},
+        "one_handle_at_a_time": {"value": one_at_a_time, "unit": UNIT},
         "rhs_at_tol": sum(1 for t in tr if t <= TOL), "rhs_reported": len(tr),
         "setup_s": setup_s, "gpu_launches": launches, "clocks": clk,
     }
