@@ -105,14 +105,11 @@ def test_group_matches_one_handle_at_a_time(small_c3):
     impedances and station gradients of the same handles run one at a time
     (the same arithmetic in the same order: agreement to rounding noise)."""
     from maple3dmt_gb300 import workloads
-    from maple3dmt_gb300.solver import group_station_gradients, solver_for_survey
+    from maple3dmt_gb300.solver import group_station_gradients, solvers_for_surveys
     svs = small_c3
-    sizes = []
-    solvers = []
-    for sv in svs:
-        s = solver_for_survey(sv, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1)
-        solvers.append(s)
-        sizes.append(s.ne)
+    # the handles are set up on host threads, as the C3 bench does
+    solvers = solvers_for_surveys(svs, workers=3, bicgstab_tol=1e-7, bicgstab_maxiter=5000, precision=1)
+    sizes = [s.ne for s in solvers]
     assert len(set(sizes)) > 1, sizes
     rng = np.random.default_rng(3)
     wr = [workloads.station_sources(s.ns, rng)[:12] for s in solvers]
